@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""BFS GTEPS on one GB300: the hybrid top-down / bottom-up BFS of GraphPhi's
+apps/bfs_simd, run through this repository's C ABI (libbfs_gb300.so).
+
+Workload (default, `--workload pokec`): a seeded R-MAT stand-in for Pokec with
+1,632,803 vertices and 30,622,564 directed edges (a=0.57 b=0.19 c=0.19,
+permuted ids, self loops and duplicates removed), tile width 1024, stripe
+length 16, and 64 seeded sources with out-degree > 0.  One step = the 64
+single-source traversals; GTEPS = sum over sources of m(s) (out-degrees of the
+reached vertices) / time.
+
+  value : device time (CUDA events on the launching stream) of the traversals,
+          graph resident in HBM, L2 flushed (256 MiB write) before every traversal
+  e2e   : the same traversals through the public bfs_run() call, levels copied
+          to pinned host memory every traversal, host wall clock
+  --impl reference : the CPU restatement of the reference's algorithm (oracle/,
+          OpenMP on all host cores) on a bounded sample of the same workload
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", default="pokec")
+    ap.add_argument("--mode", choices=["persistent", "stepwise"], default="persistent")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload: str):
+    """Per-launch DRAM bytes of the traversal kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    ent = d.get(workload)
+    return None if ent is None else ent.get("dram_bytes_per_launch")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        for line in (getattr(self, "out", "") or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_bytes(st: dict, n: int, sw: int) -> int:
+    """Bytes a traversal must move at minimum, from its device counters.
+
+    4 B per CSR edge read top-down, 12 B per frontier vertex expanded top-down
+    (queue entry + two row offsets), 4 B per packed tile word streamed
+    bottom-up, S*W/8 B per staged frontier slice, 8 B per reached vertex
+    (level + parent store), the initialisation of levels and parents (8 B per
+    vertex) and two N/8-byte bitmap passes per step.
+    """
+    return (4 * st["td_edges"] + 12 * st["td_vertices"] + 4 * st["bu_words"] + (sw // 8) * st["bu_slices"]
+            + 8 * st["reached"] + 8 * n + st["num_steps"] * 2 * ((n + 7) // 8))
+
+
+def cpu_baseline(wl, src, dst, sources, seconds: float, per_call=None):
+    """The oracle (the reference's algorithm restated, OpenMP on all host cores) on a bounded sample."""
+    from oracle import oracle as O
+    O.build(with_reference=False)
+    arr = O.arrays_from_edges(wl.n, src, dst, wl.w, wl.s)
+    deg = arr["degrees"].astype(np.uint64)
+    threads = O.max_threads()
+    edges = 0
+    secs = 0.0
+    done = []
+    levels = {}
+    t0 = time.perf_counter()
+    for s in sources:
+        cost, _, _, t = O.bfs_hybrid(arr, int(s), threads=threads)
+        edges += int(deg[cost >= 0].sum())
+        secs += t
+        done.append(int(s))
+        levels[int(s)] = cost
+        if time.perf_counter() - t0 > seconds:
+            break
+    return {"value": edges / secs / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
+            "sample": f"{len(done)} of {len(sources)} sources of the same graph, the reference's timed region "
+                      f"(traversal only), oracle/bfs_oracle.c OpenMP build"}, levels, arr
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from bfs_simd_benchmarks_gb300 import workloads
+    import bfs_simd_benchmarks_gb300 as B
+    B.load_library(build_if_missing=True)
+    wl = workloads.get(args.workload)
+    src, dst = wl.edges()
+    from oracle import oracle as O
+    O.build(with_reference=False)
+    arr = O.arrays_from_edges(wl.n, src, dst, wl.w, wl.s)
+    deg = arr["degrees"].astype(np.uint64)
+    sources = wl.sources(arr["degrees"])
+    threads = O.max_threads()
+    per_step = 4
+    it = 0
+
+    def step():
+        nonlocal it
+        e, t = 0, 0.0
+        for _ in range(per_step):
+            s = int(sources[it % len(sources)])
+            it += 1
+            cost, _, _, sec = O.bfs_hybrid(arr, s, threads=threads)
+            e += int(deg[cost >= 0].sum())
+            t += sec
+        return e, t
+
+    for _ in range(args.warmup):
+        step()
+    E, T = 0, 0.0
+    for _ in range(args.steps):
+        e, t = step()
+        E += e
+        T += t
+    val = E / T / 1e9
+    line = {"metric": "BFS GTEPS (1-src & 4096-src batched), query p50/p99 ms; vs plain GPU BFS",
+            "impl": "reference", "value": val, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": T / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded R-MAT)",
+            "config": dict(wl.describe(), step=f"{per_step} single-source traversals on the host cores"),
+            "cpu_baseline": {"value": val, "unit": "GTEPS", "cores": threads, "kind": "port",
+                             "sample": f"{per_step} sources per step, {args.steps} steps, the reference's "
+                                       "timed region, oracle/bfs_oracle.c OpenMP build"},
+            "e2e": {"value": val, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    import bfs_simd_benchmarks_gb300 as B
+    from bfs_simd_benchmarks_gb300 import _native as N
+    from bfs_simd_benchmarks_gb300 import workloads
+    B.load_library(build_if_missing=True)
+    wl = workloads.get(args.workload)
+    t_gen = time.perf_counter()
+    src, dst = wl.edges()
+    g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s)
+    g.set_options(mode=args.mode)
+    info = g.info()
+    t_gen = time.perf_counter() - t_gen
+    degrees = g.degrees()
+    sources = wl.sources(degrees)
+    n = wl.n
+    sw = wl.s * wl.w
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    lev = torch.empty(n, dtype=torch.int32, device=dev)
+    par = torch.empty(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+
+    def traverse(s: int, timed: list | None):
+        with torch.cuda.stream(stream):
+            flush.fill_(s & 0xFF)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.run_device(int(s), lev.data_ptr(), par.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+        st = g.last_stats()  # synchronises on the stream after the traversal
+        if timed is not None:
+            timed.append((e0, e1, st))
+        return st
+
+    # warm-up steps (also records m(s) of every source)
+    for _ in range(args.warmup):
+        for s in sources:
+            traverse(int(s), None)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    timed = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            for s in sources:
+                traverse(int(s), timed)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    trav_ms = [a.elapsed_time(b) for a, b, _ in timed]
+    kern_ms = [st["kernel_ms"] for _, _, st in timed]
+    edges = sum(st["edges_traversed"] for _, _, st in timed)
+    for _, _, st in timed:
+        if st["status"] != 0:
+            raise RuntimeError(f"device status {st['status']}")
+    total_ms = sum(trav_ms)
+    if world > 1:
+        t = torch.tensor([total_ms, float(edges)], dtype=torch.float64, device=dev)
+        tmax = t.clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        total_ms_max, edges_all = float(tmax[0]), float(t[1])
+    else:
+        total_ms_max, edges_all = total_ms, float(edges)
+    value = edges_all / (total_ms_max / 1e3) / 1e9
+
+    # roofline of the traversal kernel (k_bfs_persistent), per launch
+    alg = [algorithmic_bytes(st, n, sw) for _, _, st in timed]
+    achieved = statistics.mean(alg) / (statistics.mean(kern_ms) / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = ncu_traffic(args.workload)
+
+    # e2e through the public call with host buffers
+    lib = N.load()
+    pinned = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    pptr = C.cast(pinned.data_ptr(), C.POINTER(C.c_int32))
+    torch.cuda.synchronize()
+    e2e_edges = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in sources:
+            stc = N.Stats()
+            N.check(lib.bfs_run(g.handle, int(s), pptr, None, C.byref(stc)), "bfs_run")
+            e2e_edges += stc.edges_traversed
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = e2e_edges / e2e_s / 1e9
+
+    cpu = None
+    parity = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, cpu_levels, _ = cpu_baseline(wl, src, dst, sources, args.cpu_seconds)
+        ok = 0
+        for s, ref in cpu_levels.items():
+            got, _, _ = g.run(s, parents=False)
+            ok += int(np.array_equal(got, ref))
+        parity = f"levels bit-exact on {ok}/{len(cpu_levels)} sources checked against the oracle"
+    if rank == 0:
+        clocks = clk.summary()
+        line = {
+            "metric": "BFS GTEPS (1-src & 4096-src batched), query p50/p99 ms; vs plain GPU BFS",
+            "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded R-MAT stand-in, see config)",
+            "config": dict(wl.describe(), step=f"{len(sources)} single-source traversals",
+                           parallelism="replicas" if world > 1 else "single GPU", mode=args.mode,
+                           l2="flushed (256 MiB write) before every traversal; graph 245 MB > L2",
+                           grid_ctas=timed[0][2]["grid_ctas"], column_groups=info["num_groups"],
+                           graph_build_s=round(t_gen, 2)),
+            "single_source": {"gteps": value, "ms_per_traversal_mean": statistics.mean(trav_ms),
+                              "ms_per_traversal_p50": statistics.median(trav_ms),
+                              "ms_per_traversal_p99": float(np.percentile(trav_ms, 99)),
+                              "edges_per_traversal_mean": edges / len(timed),
+                              "dense_steps_mean": statistics.mean(st["dense_steps"] for _, _, st in timed),
+                              "steps_mean": statistics.mean(st["num_steps"] for _, _, st in timed)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_bfs_persistent", "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+                         if peak_kind == "measured" else "fallback",
+                         "algorithmic_bytes_per_launch": statistics.mean(alg),
+                         "launch_ms_mean": statistics.mean(kern_ms)},
+            "e2e": {"value": e2e_value, "unit": "GTEPS", "h2d_bytes_per_step": 4 * len(sources),
+                    "d2h_bytes_per_step": 4 * n * len(sources),
+                    "note": "bfs_run(): source as a launch parameter, int32 levels to pinned host memory"},
+            "gpu_launches": 2 * len(timed),
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+            "parity": parity,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    g.close()
+
+
+if __name__ == "__main__":
+    main()

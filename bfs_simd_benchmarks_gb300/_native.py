@@ -1,0 +1,177 @@
+"""ctypes binding of libbfs_gb300.so (the C ABI declared in include/bfs_gb300.h).
+
+The library is built in-tree by ``bfs_simd_benchmarks_gb300.build.build()``.
+Loading fails loudly when it is missing: there is no CPU fallback for any
+traversal entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+BFS_OK = 0
+BFS_EIO = 1
+BFS_EFORMAT = 2
+BFS_ENOMEM = 3
+BFS_EARG = 4
+BFS_EBUDGET = 5
+BFS_ETIMEOUT = 6
+BFS_ECUDA = 7
+BFS_EUNSUPPORTED = 8
+BFS_ENODEV = 9
+
+BFS_LOAD_WEIGHTED = 0x1
+BFS_LOAD_PREFER_REORDER = 0x2
+BFS_LOAD_HOST_ONLY = 0x4
+
+BFS_MODE_PERSISTENT = 0
+BFS_MODE_STEPWISE = 1
+
+BFS_RMAT_NO_SELF_LOOPS = 0x1
+BFS_RMAT_DEDUP = 0x2
+BFS_RMAT_PERMUTE = 0x4
+
+BFS_TRACE_MAX = 256
+
+_u32p = C.POINTER(C.c_uint32)
+_i32p = C.POINTER(C.c_int32)
+
+
+class GraphInfo(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_uint32),
+        ("tile_width", C.c_uint32),
+        ("num_edges", C.c_uint64),
+        ("stripe_length", C.c_uint32),
+        ("side_length", C.c_uint32),
+        ("num_tiles", C.c_uint64),
+        ("num_stripes", C.c_uint32),
+        ("num_groups", C.c_uint32),
+        ("packed_words", C.c_uint64),
+        ("device_bytes", C.c_uint64),
+        ("max_out_degree", C.c_uint32),
+        ("used_reorder", C.c_uint32),
+        ("base", C.c_char * 1024),
+    ]
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("mode", C.c_uint32),
+        ("to_dense_ratio", C.c_uint32),
+        ("to_sparse_ratio", C.c_uint32),
+        ("warp_max_degree", C.c_uint32),
+        ("cta_max_degree", C.c_uint32),
+        ("reserved", C.c_uint32 * 3),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("num_steps", C.c_uint32),
+        ("dense_steps", C.c_uint32),
+        ("reached", C.c_uint32),
+        ("max_level", C.c_uint32),
+        ("edges_traversed", C.c_uint64),
+        ("td_edges", C.c_uint64),
+        ("td_vertices", C.c_uint64),
+        ("bu_words", C.c_uint64),
+        ("bu_slices", C.c_uint64),
+        ("bu_groups", C.c_uint64),
+        ("device_ms", C.c_double),
+        ("kernel_ms", C.c_double),
+        ("status", C.c_int32),
+        ("grid_ctas", C.c_uint32),
+        ("trace", C.c_uint8 * BFS_TRACE_MAX),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "trace"}
+        d["trace"] = list(self.trace[: min(self.num_steps, BFS_TRACE_MAX)])
+        return d
+
+
+class RmatParams(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_uint32),
+        ("flags", C.c_uint32),
+        ("num_edges", C.c_uint64),
+        ("a", C.c_double),
+        ("b", C.c_double),
+        ("c", C.c_double),
+        ("seed", C.c_uint64),
+    ]
+
+
+# (name, restype, argtypes)
+_SIGNATURES = [
+    ("bfs_status_string", C.c_char_p, [C.c_int]),
+    ("bfs_version", C.c_char_p, []),
+    ("bfs_graph_load", C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_void_p)]),
+    ("bfs_graph_from_edges", C.c_int,
+     [C.c_uint32, C.c_uint64, _u32p, _u32p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_void_p)]),
+    ("bfs_graph_from_arrays", C.c_int,
+     [C.c_uint32, C.c_uint64, _u32p, _u32p, _u32p, _u32p, _u32p, C.c_uint32, C.c_uint32, C.c_uint32,
+      C.POINTER(C.c_void_p)]),
+    ("bfs_graph_free", C.c_int, [C.c_void_p]),
+    ("bfs_graph_get_info", C.c_int, [C.c_void_p, C.POINTER(GraphInfo)]),
+    ("bfs_graph_get_degrees", C.c_int, [C.c_void_p, _u32p]),
+    ("bfs_options_default", C.c_int, [C.POINTER(Options)]),
+    ("bfs_set_options", C.c_int, [C.c_void_p, C.POINTER(Options)]),
+    ("bfs_get_options", C.c_int, [C.c_void_p, C.POINTER(Options)]),
+    ("bfs_run", C.c_int, [C.c_void_p, C.c_uint32, _i32p, _u32p, C.POINTER(Stats)]),
+    ("bfs_run_device", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("bfs_last_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    ("bfs_write_level_dump", C.c_int, [C.c_char_p, C.c_uint32, _i32p]),
+    ("bfs_tool_csr_tiling", C.c_int, [C.c_char_p, C.c_uint32]),
+    ("bfs_tool_coo_tiling", C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, C.c_uint32]),
+    ("bfs_tool_column_major", C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
+    ("bfs_tool_vertex_remap", C.c_int, [C.c_char_p, C.c_uint32]),
+    ("bfs_gen_rmat", C.c_int, [C.POINTER(RmatParams), _u32p, _u32p, C.c_uint64]),
+]
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False) -> C.CDLL:
+    """Loads libbfs_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(
+                f"libbfs_gb300.so is not built ({path}); run __graft_entry__.build() or "
+                "python bfs_simd_benchmarks_gb300/build.py first")
+        _build.build()
+    lib = C.CDLL(path)
+    for name, res, args in _SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_names() -> list[str]:
+    return [name for name, _, _ in _SIGNATURES]
+
+
+class BfsError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        lib = load()
+        msg = lib.bfs_status_string(status).decode()
+        super().__init__(f"{what}: {msg} (status {status})" if what else f"{msg} (status {status})")
+        self.status = status
+
+
+def check(status: int, what: str = "") -> None:
+    if status != BFS_OK:
+        raise BfsError(status, what)

@@ -1,0 +1,521 @@
+// api.cu -- the C ABI of libbfs_gb300.so: graph handles, loading and upload,
+// single-source runs.  See include/bfs_gb300.h for the reference interface
+// each entry point replaces.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+#include "kernels_api.h"
+
+using namespace bfsg;
+
+namespace {
+
+constexpr uint32_t kMaxGroupVertices = 32768;  // shared-memory bitmaps of one column group
+constexpr uint32_t kGroupsPerCta = 2;
+
+struct DevBuf {
+	void *p = nullptr;
+	size_t bytes = 0;
+};
+
+} // namespace
+
+struct bfs_graph {
+	// host-side description
+	uint32_t n = 0;
+	uint64_t m = 0;
+	uint32_t w = 0, s = 0, side = 0, num_stripes = 0;
+	uint32_t max_degree = 0;
+	std::string base;
+	bool used_reorder = false;
+	bool host_only = false;
+	std::vector<uint32_t> degrees;  // kept for info / tests
+	// device
+	int device = 0;
+	int num_sms = 0;
+	DevGraph dg{};
+	RunCtx rc{};
+	uint32_t batch = 1;
+	int grid = 0;
+	size_t smem = 0;
+	std::vector<DevBuf> bufs;
+	size_t device_bytes = 0;
+	int32_t *level_buf = nullptr;    // internal outputs for bfs_run
+	uint32_t *parent_buf = nullptr;
+	DevStats *h_stats = nullptr;     // pinned
+	StepCounters *h_ctr = nullptr;   // pinned (stepwise mode)
+	cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
+	cudaStream_t last_stream = nullptr;
+	bool stats_fresh = false;
+	bool have_run = false;
+	bool stepwise_last = false;
+	bfs_stats host_stats{};          // stepwise-mode bookkeeping
+	bfs_options opt{};
+	uint32_t num_groups = 0;
+	uint64_t packed_words = 0;
+	std::mutex mu;
+};
+
+namespace {
+
+int cuda_ok(cudaError_t e) { return e == cudaSuccess ? BFS_OK : BFS_ECUDA; }
+
+template <class T> int dev_alloc(bfs_graph *g, T **out, size_t count) {
+	size_t bytes = std::max<size_t>(sizeof(T) * count, 16);
+	void *p = nullptr;
+	if (cudaMalloc(&p, bytes) != cudaSuccess) {
+		cudaGetLastError();
+		return BFS_ENOMEM;
+	}
+	g->bufs.push_back({p, bytes});
+	g->device_bytes += bytes;
+	*out = (T *) p;
+	return BFS_OK;
+}
+
+template <class T> int dev_upload(bfs_graph *g, const T **out, const std::vector<T> &v) {
+	T *p = nullptr;
+	int st = dev_alloc(g, &p, v.size());
+	if (st) return st;
+	if (!v.empty() && cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+		return BFS_ECUDA;
+	*out = p;
+	return BFS_OK;
+}
+
+void release(bfs_graph *g) {
+	for (auto &b : g->bufs) cudaFree(b.p);
+	g->bufs.clear();
+	if (g->h_stats) cudaFreeHost(g->h_stats);
+	if (g->h_ctr) cudaFreeHost(g->h_ctr);
+	if (g->ev0) cudaEventDestroy(g->ev0);
+	if (g->ev1) cudaEventDestroy(g->ev1);
+	if (g->evm) cudaEventDestroy(g->evm);
+	g->h_stats = nullptr;
+	g->h_ctr = nullptr;
+	g->ev0 = g->ev1 = g->evm = nullptr;
+}
+
+void default_options(bfs_options *o) {
+	std::memset(o, 0, sizeof(*o));
+	o->mode = BFS_MODE_PERSISTENT;
+	o->to_dense_ratio = 20;   // T_RATIO, apps/bfs_simd/bfs.cpp:1171
+	o->to_sparse_ratio = 20;
+	o->warp_max_degree = 32;
+	o->cta_max_degree = 4096;
+}
+
+// Builds the device copy of a validated host graph.
+int upload(bfs_graph *g, HostGraph &h) {
+	g->n = h.n;
+	g->m = h.m;
+	g->w = h.w;
+	g->s = h.s;
+	g->side = h.side;
+	g->num_stripes = h.num_stripes;
+	g->max_degree = h.max_degree;
+	g->base = h.base;
+	g->used_reorder = h.used_reorder;
+	g->degrees = h.degrees;
+	default_options(&g->opt);
+	if (g->host_only) return BFS_OK;
+
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+		cudaGetLastError();
+		return BFS_ENODEV;
+	}
+	if (cudaGetDevice(&g->device) != cudaSuccess) return BFS_ECUDA;
+	if (cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->device) != cudaSuccess) return BFS_ECUDA;
+	int coop = 0;
+	cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device);
+	if (!coop) return BFS_EUNSUPPORTED;
+
+	PackedTiles pk;
+	int st = pack_tiles(h, (uint32_t) g->num_sms * 2 * kGroupsPerCta, kMaxGroupVertices, pk);
+	if (st) return st;
+	g->num_groups = pk.num_groups;
+	g->packed_words = pk.words.size();
+
+	DevGraph &d = g->dg;
+	d.n = h.n;
+	d.m = (uint32_t) h.m;
+	d.w = h.w;
+	d.s = h.s;
+	d.side = h.side;
+	d.num_stripes = h.num_stripes;
+	d.sw = h.s * h.w;
+	d.vbits = pk.vbits;
+	d.cbits = pk.cbits;
+	d.ushift = pk.vbits + pk.cbits;
+	d.vmask = (1u << pk.vbits) - 1u;
+	d.cmask = (1u << pk.cbits) - 1u;
+	d.num_groups = pk.num_groups;
+	d.max_group_words = (pk.max_group_vertices + 31) / 32;
+	d.slice_words = (d.sw + 31) / 32;
+	d.nwords = (h.n + 31) / 32;
+	if ((st = dev_upload(g, &d.row_off, h.row_off))) return st;
+	if ((st = dev_upload(g, &d.col, h.csr_dst))) return st;
+	if ((st = dev_upload(g, &d.packed, pk.words))) return st;
+	if ((st = dev_upload(g, &d.seg_off, pk.seg_off))) return st;
+	if ((st = dev_upload(g, &d.group_col, pk.group_col))) return st;
+	if ((st = dev_upload(g, &d.hasin, pk.hasin_bits))) return st;
+
+	// Run context.
+	RunCtx &r = g->rc;
+	if ((st = dev_alloc(g, &r.vis, d.nwords))) return st;
+	for (int i = 0; i < 3; ++i) {
+		if ((st = dev_alloc(g, &r.bm[i], d.nwords))) return st;
+		if ((st = dev_alloc(g, &r.sf[i], d.num_stripes))) return st;
+	}
+	for (int set = 0; set < 2; ++set)
+		for (int b = 0; b < 3; ++b)
+			if ((st = dev_alloc(g, &r.q[set][b], h.n))) return st;
+	if ((st = dev_alloc(g, &r.ctr, 3))) return st;
+	if ((st = dev_alloc(g, &r.stats, 1))) return st;
+	if ((st = dev_alloc(g, &r.bar, 2))) return st;
+	if ((st = dev_alloc(g, &r.err, 1))) return st;
+	if ((st = dev_alloc(g, &g->level_buf, h.n))) return st;
+	if ((st = dev_alloc(g, &g->parent_buf, h.n))) return st;
+	if (cudaMallocHost(&g->h_stats, sizeof(DevStats)) != cudaSuccess) return BFS_ENOMEM;
+	if (cudaMallocHost(&g->h_ctr, sizeof(StepCounters) * 3) != cudaSuccess) return BFS_ENOMEM;
+	if (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess ||
+			cudaEventCreate(&g->evm) != cudaSuccess)
+		return BFS_ECUDA;
+
+	g->batch = std::max<uint32_t>(1, std::min<uint32_t>(kMaxSliceBatch, kSliceBudgetWords / std::max<uint32_t>(1, d.slice_words)));
+	if ((st = persistent_grid(d, g->batch, g->num_sms, &g->grid, &g->smem))) return st;
+	return BFS_OK;
+}
+
+int finish_graph(HostGraph &h, uint32_t flags, bfs_graph **out) {
+	bfs_graph *g = new bfs_graph();
+	g->host_only = flags & BFS_LOAD_HOST_ONLY;
+	int st = upload(g, h);
+	if (st) {
+		release(g);
+		delete g;
+		return st;
+	}
+	*out = g;
+	return BFS_OK;
+}
+
+int check_shape(uint32_t n, uint64_t m, uint32_t w, uint32_t s) {
+	if (n == 0 || w == 0 || s == 0) return BFS_EARG;
+	if (m > 0xFFFFFFFFull) return BFS_EUNSUPPORTED;
+	return BFS_OK;
+}
+
+void init_shape(HostGraph &h, uint32_t n, uint64_t m, uint32_t w, uint32_t s) {
+	h.n = n;
+	h.m = m;
+	h.w = w;
+	h.s = s;
+	h.side = side_length_of(n, w);
+	h.num_stripes = (h.side + s - 1) / s;
+}
+
+int resolve_base(const std::string &data, uint32_t w, uint32_t s, uint32_t flags, std::string *base, bool *reorder) {
+	std::string cands[2] = {data, data + "_reorder"};
+	if (flags & BFS_LOAD_PREFER_REORDER) std::swap(cands[0], cands[1]);
+	for (int i = 0; i < 2; ++i) {
+		std::string col = cands[i] + "_col-" + std::to_string(s) + "-coo-tiled-" + std::to_string(w) + "-0";
+		std::string csr = cands[i] + "_untiled-0";
+		if (file_exists(col) && file_exists(csr)) {
+			*base = cands[i];
+			*reorder = (cands[i] != data);
+			return BFS_OK;
+		}
+	}
+	return BFS_EIO;
+}
+
+// Host side of a traversal in stepwise mode.
+int run_stepwise(bfs_graph *g, const RunCtx &r, const StepParams &p, cudaStream_t st) {
+	const DevGraph &d = g->dg;
+	int rc;
+	if ((rc = launch_step(kStepSeed, d, r, p, 0, g->batch, g->grid, g->smem, st))) return rc;
+	bfs_stats &hs = g->host_stats;
+	std::memset(&hs, 0, sizeof(hs));
+	bool last_dense = false;
+	uint32_t step = 0;
+	for (;; ++step) {
+		if (cudaMemcpyAsync(g->h_ctr, r.ctr, sizeof(StepCounters) * 3, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+				cudaStreamSynchronize(st) != cudaSuccess)
+			return BFS_ECUDA;
+		const StepCounters &in = g->h_ctr[(step + 2) % 3];
+		hs.reached += in.count;
+		hs.edges_traversed += in.degsum;
+		if (in.count == 0) break;
+		bool dense = false;
+		if (step > 0) {
+			unsigned long long thr = last_dense ? p.to_sparse_threshold : p.to_dense_threshold;
+			dense = (unsigned long long) in.count + in.degsum > thr;
+		}
+		if ((rc = launch_step(kStepClear, d, r, p, step, g->batch, g->grid, g->smem, st))) return rc;
+		if (dense) {
+			if (!last_dense && (rc = launch_step(kStepToDense, d, r, p, step, g->batch, g->grid, g->smem, st))) return rc;
+			if ((rc = launch_step(kStepDense, d, r, p, step, g->batch, g->grid, g->smem, st))) return rc;
+		} else {
+			if (last_dense && (rc = launch_step(kStepToSparse, d, r, p, step, g->batch, g->grid, g->smem, st))) return rc;
+			if ((rc = launch_step(kStepExpand, d, r, p, step, g->batch, g->grid, g->smem, st))) return rc;
+		}
+		if (step < BFS_TRACE_MAX) hs.trace[step] = dense ? 1 : 0;
+		hs.dense_steps += dense;
+		last_dense = dense;
+	}
+	hs.num_steps = step;
+	return BFS_OK;
+}
+
+int run_impl(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, cudaStream_t st) {
+	if (g->host_only) return BFS_EUNSUPPORTED;
+	if (source >= g->n || !levels) return BFS_EARG;
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	RunCtx r = g->rc;
+	r.level = levels;
+	r.parent = parents;
+	StepParams p{};
+	p.source = source;
+	p.warp_max_degree = g->opt.warp_max_degree;
+	p.cta_max_degree = g->opt.cta_max_degree;
+	p.to_dense_threshold = g->m / std::max<uint32_t>(1, g->opt.to_dense_ratio);
+	p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
+	int rc;
+	if (cudaEventRecord(g->ev0, st) != cudaSuccess) return BFS_ECUDA;
+	if ((rc = launch_init(g->dg, r, st, g->num_sms))) return rc;
+	if (cudaEventRecord(g->evm, st) != cudaSuccess) return BFS_ECUDA;
+	g->stepwise_last = g->opt.mode == BFS_MODE_STEPWISE;
+	if (g->stepwise_last) {
+		if ((rc = run_stepwise(g, r, p, st))) return rc;
+	} else {
+		if ((rc = launch_persistent(g->dg, r, p, g->batch, g->grid, g->smem, st))) return rc;
+	}
+	if (cudaEventRecord(g->ev1, st) != cudaSuccess) return BFS_ECUDA;
+	g->last_stream = st;
+	g->stats_fresh = false;
+	g->have_run = true;
+	return BFS_OK;
+}
+
+int collect_stats(bfs_graph *g, bfs_stats *out) {
+	if (!g->have_run) return BFS_EARG;
+	// The device statistics are copied only when asked for, so that a run
+	// enqueues nothing but its kernels.
+	if (!g->stats_fresh) {
+		if (cudaMemcpyAsync(g->h_stats, g->rc.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, g->last_stream) != cudaSuccess ||
+				cudaStreamSynchronize(g->last_stream) != cudaSuccess)
+			return BFS_ECUDA;
+		g->stats_fresh = true;
+	}
+	const DevStats &d = *g->h_stats;
+	bfs_stats s{};
+	if (g->stepwise_last) {
+		s = g->host_stats;
+	} else {
+		s.num_steps = d.num_steps;
+		s.dense_steps = d.dense_steps;
+		s.reached = (uint32_t) d.reached;
+		s.edges_traversed = d.edges_traversed;
+		std::memcpy(s.trace, d.trace, sizeof(s.trace));
+	}
+	s.td_edges = d.td_edges;
+	s.td_vertices = d.td_vertices;
+	s.bu_words = d.bu_words;
+	s.bu_slices = d.bu_slices;
+	s.bu_groups = d.bu_groups;
+	s.status = g->stepwise_last ? BFS_OK : d.status;
+	s.max_level = s.num_steps ? s.num_steps - 1 : 0;
+	s.grid_ctas = (uint32_t) g->grid;
+	float ms = 0, kms = 0;
+	cudaEventElapsedTime(&ms, g->ev0, g->ev1);
+	cudaEventElapsedTime(&kms, g->evm, g->ev1);
+	s.device_ms = ms;
+	s.kernel_ms = kms;
+	if (out) *out = s;
+	return s.status;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *bfs_status_string(int status) {
+	switch (status) {
+	case BFS_OK: return "ok";
+	case BFS_EIO: return "cannot open file";
+	case BFS_EFORMAT: return "malformed or inconsistent input";
+	case BFS_ENOMEM: return "out of memory";
+	case BFS_EARG: return "invalid argument";
+	case BFS_EBUDGET: return "over the device-memory budget";
+	case BFS_ETIMEOUT: return "device wait timed out";
+	case BFS_ECUDA: return "CUDA error";
+	case BFS_EUNSUPPORTED: return "unsupported tile width / stripe length";
+	case BFS_ENODEV: return "no CUDA device";
+	default: return "unknown status";
+	}
+}
+
+const char *bfs_version(void) { return "bfs_gb300 0.1 (sm_103a)"; }
+
+int bfs_graph_load(const char *data, uint32_t tile_width, uint32_t stripe_length, uint32_t flags, bfs_graph **out) {
+	if (!data || !out || tile_width == 0 || stripe_length == 0) return BFS_EARG;
+	*out = nullptr;
+	HostGraph h;
+	int st = resolve_base(data, tile_width, stripe_length, flags, &h.base, &h.used_reorder);
+	if (st) return st;
+	const bool weighted = flags & BFS_LOAD_WEIGHTED;
+	const std::string colp = h.base + "_col-" + std::to_string(stripe_length) + "-coo-tiled-" + std::to_string(tile_width);
+	const std::string csrp = h.base + "_untiled";
+	uint32_t n, n2;
+	uint64_t m, m2;
+	if ((st = read_header(colp + "-0", &n, &m))) return st;
+	if ((st = read_header(csrp + "-0", &n2, &m2))) return st;
+	if (n != n2 || m != m2) return BFS_EFORMAT;
+	if ((st = check_shape(n, m, tile_width, stripe_length))) return st;
+	init_shape(h, n, m, tile_width, stripe_length);
+	const uint64_t num_tiles = (uint64_t) h.side * h.side;
+	h.tile_offsets.resize(num_tiles);
+	if ((st = read_u32_lines(colp + "-offsets", num_tiles, h.tile_offsets.data()))) return st;
+	h.heads.resize(m);
+	h.tails.resize(m);
+	if ((st = read_split_family(colp, m, weighted, n, h.heads.data(), h.tails.data()))) return st;
+	h.degrees.resize(n);
+	if ((st = read_u32_lines(csrp + "-nneibor", n, h.degrees.data()))) return st;
+	std::vector<uint32_t> csr_src(m);
+	h.csr_dst.resize(m);
+	if ((st = read_split_family(csrp, m, weighted, n, csr_src.data(), h.csr_dst.data()))) return st;
+	if ((st = finish_csr(h))) return st;
+	// The CSR sources must match the out-degree file.
+	for (uint32_t v = 0; v < n; ++v)
+		for (uint32_t e = h.row_off[v]; e < h.row_off[v + 1]; ++e)
+			if (csr_src[e] != v) return BFS_EFORMAT;
+	if ((st = validate_colmajor(h))) return st;
+	return finish_graph(h, flags, out);
+}
+
+int bfs_graph_from_edges(uint32_t num_vertices, uint64_t num_edges, const uint32_t *src, const uint32_t *dst,
+		uint32_t tile_width, uint32_t stripe_length, uint32_t flags, bfs_graph **out) {
+	if (!out || (num_edges && (!src || !dst))) return BFS_EARG;
+	*out = nullptr;
+	int st = check_shape(num_vertices, num_edges, tile_width, stripe_length);
+	if (st) return st;
+	HostGraph h;
+	init_shape(h, num_vertices, num_edges, tile_width, stripe_length);
+	std::vector<uint32_t> cs;
+	if ((st = csr_from_edges(num_vertices, num_edges, src, dst, cs, h.csr_dst, h.degrees))) return st;
+	if ((st = finish_csr(h))) return st;
+	if ((st = colmajor_from_csr(num_vertices, num_edges, tile_width, stripe_length, cs.data(), h.csr_dst.data(),
+				 h.heads, h.tails, nullptr)))
+		return st;
+	return finish_graph(h, flags, out);
+}
+
+int bfs_graph_from_arrays(uint32_t num_vertices, uint64_t num_edges, const uint32_t *degrees, const uint32_t *csr_dst,
+		const uint32_t *heads, const uint32_t *tails, const uint32_t *tile_offsets, uint32_t tile_width,
+		uint32_t stripe_length, uint32_t flags, bfs_graph **out) {
+	if (!out || !degrees || (num_edges && (!csr_dst || !heads || !tails))) return BFS_EARG;
+	*out = nullptr;
+	int st = check_shape(num_vertices, num_edges, tile_width, stripe_length);
+	if (st) return st;
+	HostGraph h;
+	init_shape(h, num_vertices, num_edges, tile_width, stripe_length);
+	h.degrees.assign(degrees, degrees + num_vertices);
+	h.csr_dst.assign(csr_dst, csr_dst + num_edges);
+	for (uint64_t i = 0; i < num_edges; ++i)
+		if (h.csr_dst[i] >= num_vertices) return BFS_EFORMAT;
+	if ((st = finish_csr(h))) return st;
+	h.heads.assign(heads, heads + num_edges);
+	h.tails.assign(tails, tails + num_edges);
+	if (tile_offsets) h.tile_offsets.assign(tile_offsets, tile_offsets + (uint64_t) h.side * h.side);
+	if ((st = validate_colmajor(h))) return st;
+	return finish_graph(h, flags, out);
+}
+
+int bfs_graph_free(bfs_graph *g) {
+	if (!g) return BFS_EARG;
+	release(g);
+	delete g;
+	return BFS_OK;
+}
+
+int bfs_graph_get_info(const bfs_graph *g, bfs_graph_info *info) {
+	if (!g || !info) return BFS_EARG;
+	std::memset(info, 0, sizeof(*info));
+	info->num_vertices = g->n;
+	info->num_edges = g->m;
+	info->tile_width = g->w;
+	info->stripe_length = g->s;
+	info->side_length = g->side;
+	info->num_tiles = (uint64_t) g->side * g->side;
+	info->num_stripes = g->num_stripes;
+	info->num_groups = g->num_groups;
+	info->packed_words = g->packed_words;
+	info->device_bytes = g->device_bytes;
+	info->max_out_degree = g->max_degree;
+	info->used_reorder = g->used_reorder ? 1u : 0u;
+	std::snprintf(info->base, sizeof(info->base), "%s", g->base.c_str());
+	return BFS_OK;
+}
+
+int bfs_graph_get_degrees(const bfs_graph *g, uint32_t *degrees) {
+	if (!g || !degrees) return BFS_EARG;
+	std::memcpy(degrees, g->degrees.data(), sizeof(uint32_t) * g->n);
+	return BFS_OK;
+}
+
+int bfs_options_default(bfs_options *opt) {
+	if (!opt) return BFS_EARG;
+	default_options(opt);
+	return BFS_OK;
+}
+
+int bfs_set_options(bfs_graph *g, const bfs_options *opt) {
+	if (!g || !opt) return BFS_EARG;
+	if (opt->mode > BFS_MODE_STEPWISE || opt->to_dense_ratio == 0 || opt->to_sparse_ratio == 0 ||
+			opt->warp_max_degree == 0 || opt->cta_max_degree < opt->warp_max_degree)
+		return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	g->opt = *opt;
+	return BFS_OK;
+}
+
+int bfs_get_options(const bfs_graph *g, bfs_options *opt) {
+	if (!g || !opt) return BFS_EARG;
+	*opt = g->opt;
+	return BFS_OK;
+}
+
+int bfs_run(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, bfs_stats *stats) {
+	if (!g) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	int st = run_impl(g, source, g->level_buf, g->parent_buf, 0);
+	if (st) return st;
+	st = collect_stats(g, stats);
+	if (st) return st;
+	if (levels && cudaMemcpy(levels, g->level_buf, sizeof(int32_t) * g->n, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return BFS_ECUDA;
+	if (parents && cudaMemcpy(parents, g->parent_buf, sizeof(uint32_t) * g->n, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return BFS_ECUDA;
+	return BFS_OK;
+}
+
+int bfs_run_device(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, void *stream) {
+	if (!g) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	return run_impl(g, source, levels, parents, (cudaStream_t) stream);
+}
+
+int bfs_last_stats(bfs_graph *g, bfs_stats *stats) {
+	if (!g) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	return collect_stats(g, stats);
+}
+
+} // extern "C"

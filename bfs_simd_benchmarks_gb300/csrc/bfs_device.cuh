@@ -1,0 +1,78 @@
+// bfs_device.cuh -- device-side data structures of the single-source BFS.
+#pragma once
+
+#include <cstdint>
+
+namespace bfsg {
+
+// The graph as it sits in HBM (all read-only during a traversal).
+struct DevGraph {
+	uint32_t n;            // vertices
+	uint32_t m;            // edges (< 2^32, like the reference's NEDGES)
+	uint32_t w, s;         // tile width, stripe length
+	uint32_t side;         // ceil(n / w)
+	uint32_t num_stripes;  // ceil(side / s)
+	uint32_t sw;           // s * w : sources per stripe
+	uint32_t vbits, cbits, ushift;
+	uint32_t vmask, cmask;
+	uint32_t num_groups;
+	uint32_t max_group_words;   // 32-bit words of the largest group bitmap
+	uint32_t slice_words;       // 32-bit words of one stripe's frontier slice
+	uint32_t nwords;            // ceil(n / 32)
+	const uint32_t *row_off;    // [n+1] CSR row starts
+	const uint32_t *col;        // [m]   CSR destinations
+	const uint32_t *packed;     // packed column-major stream (16-byte aligned segments)
+	const uint32_t *seg_off;    // [num_stripes*num_groups+1]
+	const uint32_t *group_col;  // [num_groups+1]
+	const uint32_t *hasin;      // [nwords] in-degree > 0
+};
+
+// Counters of the frontier a step produces (three slots rotate by step).
+struct StepCounters {
+	unsigned int tail[3];       // queue bucket tails (top-down appends, to_sparse)
+	unsigned int count;         // vertices discovered by the step
+	unsigned long long degsum;  // their out-degree sum
+	unsigned int work;          // dynamic work counter (column groups)
+	unsigned int pad;
+};
+
+// Per-run statistics gathered on the device.
+struct DevStats {
+	unsigned long long td_edges;
+	unsigned long long td_vertices;
+	unsigned long long bu_words;
+	unsigned long long bu_slices;
+	unsigned long long bu_groups;
+	unsigned long long reached;
+	unsigned long long edges_traversed;
+	unsigned int num_steps;
+	unsigned int dense_steps;
+	int status;
+	unsigned int pad;
+	unsigned char trace[256];
+};
+
+// Scratch of one traversal context (owned by the graph's run context).
+struct RunCtx {
+	int32_t *level;        // [n] output levels
+	uint32_t *parent;      // [n] output parents (may be null)
+	uint32_t *vis;         // [nwords] visited bitmap
+	uint32_t *bm[3];       // [nwords] rotating frontier bitmaps
+	uint8_t *sf[3];        // [num_stripes] rotating "stripe has a frontier vertex" flags
+	uint32_t *q[2][3];     // [2 sets][3 buckets][n] frontier queues
+	StepCounters *ctr;     // [3]
+	DevStats *stats;
+	unsigned *bar;         // [2] grid barrier
+	int *err;              // device status word
+};
+
+struct StepParams {
+	uint32_t source;
+	uint32_t warp_max_degree;
+	uint32_t cta_max_degree;
+	uint32_t pad;
+	unsigned long long to_dense_threshold;   // dense when frontier + degsum > this
+	unsigned long long to_sparse_threshold;  // stay dense while frontier + degsum > this
+};
+
+} // namespace bfsg

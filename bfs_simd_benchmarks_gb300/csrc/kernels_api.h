@@ -1,0 +1,29 @@
+// kernels_api.h -- host-side entry points of bfs_kernels.cu (internal).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/bfs_gb300.h"
+#include "bfs_device.cuh"
+
+namespace bfsg {
+
+constexpr uint32_t kSentinelWord = 0xFFFFFFFFu;
+constexpr uint32_t kUnvisitedWord = 0xFFFFFFFFu;
+constexpr uint32_t kMaxSliceBatch = 16;   // frontier slices staged together by the bottom-up step
+constexpr uint32_t kSliceBudgetWords = 8192;
+
+enum StepKind { kStepSeed = 0, kStepClear, kStepToDense, kStepToSparse, kStepExpand, kStepDense };
+
+size_t dense_smem_bytes(const DevGraph &g, uint32_t batch);
+int persistent_grid(const DevGraph &g, uint32_t batch, int num_sms, int *grid, size_t *smem);
+int launch_init(const DevGraph &g, const RunCtx &r, cudaStream_t st, int num_sms);
+int launch_persistent(const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t batch, int grid,
+		size_t smem, cudaStream_t st);
+int launch_step(int kind, const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t step,
+		uint32_t batch, int grid, size_t smem, cudaStream_t st);
+int kernel_threads();
+
+} // namespace bfsg

@@ -1,0 +1,210 @@
+"""Host-side mirror of the reference's BFS interface over the C ABI.
+
+``Graph.load(data, tile_width, stripe_length)`` is graph_input
+(apps/bfs_simd/bfs.cpp:968-1118); ``Graph.run(source)`` is graph_prepare
+(apps/bfs_simd/bfs.cpp:753-963) returning the h_cost levels and the parents;
+``write_level_dump`` is the ONEDEBUG dump (:927-954); the ``tool_*`` functions
+are the CLIs of tools/csr_tiling, tools/coo_tiling, tools/column_major_tile and
+tools/vertex_id_remap.  Errors raise ``BfsError`` with the library's status
+code, where the reference calls exit(1).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+def _u32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class Graph:
+    """A graph resident in HBM (CSR + packed column-major COO tiles)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+
+    # ---- construction -------------------------------------------------
+    @classmethod
+    def load(cls, data: str, tile_width: int, stripe_length: int, weighted: bool = False,
+             prefer_reorder: bool = False, host_only: bool = False) -> "Graph":
+        lib = N.load()
+        flags = (N.BFS_LOAD_WEIGHTED if weighted else 0) | (N.BFS_LOAD_PREFER_REORDER if prefer_reorder else 0)
+        flags |= N.BFS_LOAD_HOST_ONLY if host_only else 0
+        h = C.c_void_p()
+        N.check(lib.bfs_graph_load(data.encode(), tile_width, stripe_length, flags, C.byref(h)),
+                f"bfs_graph_load({data}, {tile_width}, {stripe_length})")
+        return cls(h)
+
+    @classmethod
+    def from_edges(cls, num_vertices: int, src, dst, tile_width: int, stripe_length: int,
+                   host_only: bool = False) -> "Graph":
+        lib = N.load()
+        s, d = _u32(src), _u32(dst)
+        if s.shape != d.shape:
+            raise ValueError("src and dst differ in length")
+        h = C.c_void_p()
+        flags = N.BFS_LOAD_HOST_ONLY if host_only else 0
+        N.check(lib.bfs_graph_from_edges(num_vertices, s.size, _ptr(s, C.c_uint32), _ptr(d, C.c_uint32),
+                                         tile_width, stripe_length, flags, C.byref(h)), "bfs_graph_from_edges")
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, num_vertices: int, degrees, csr_dst, heads, tails, tile_offsets,
+                    tile_width: int, stripe_length: int, host_only: bool = False) -> "Graph":
+        lib = N.load()
+        deg, cd, hd, tl = _u32(degrees), _u32(csr_dst), _u32(heads), _u32(tails)
+        off = None if tile_offsets is None else _u32(tile_offsets)
+        h = C.c_void_p()
+        flags = N.BFS_LOAD_HOST_ONLY if host_only else 0
+        N.check(lib.bfs_graph_from_arrays(
+            num_vertices, cd.size, _ptr(deg, C.c_uint32), _ptr(cd, C.c_uint32), _ptr(hd, C.c_uint32),
+            _ptr(tl, C.c_uint32), None if off is None else _ptr(off, C.c_uint32), tile_width, stripe_length,
+            flags, C.byref(h)), "bfs_graph_from_arrays")
+        return cls(h)
+
+    # ---- lifetime -----------------------------------------------------
+    def close(self) -> None:
+        if self._h:
+            N.load().bfs_graph_free(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    # ---- queries ------------------------------------------------------
+    def info(self) -> dict:
+        inf = N.GraphInfo()
+        N.check(N.load().bfs_graph_get_info(self._h, C.byref(inf)), "bfs_graph_get_info")
+        d = {k: getattr(inf, k) for k, _ in N.GraphInfo._fields_}
+        d["base"] = inf.base.decode()
+        return d
+
+    @property
+    def num_vertices(self) -> int:
+        return self.info()["num_vertices"]
+
+    def degrees(self) -> np.ndarray:
+        n = self.num_vertices
+        out = np.empty(n, dtype=np.uint32)
+        N.check(N.load().bfs_graph_get_degrees(self._h, _ptr(out, C.c_uint32)), "bfs_graph_get_degrees")
+        return out
+
+    def options(self) -> dict:
+        o = N.Options()
+        N.check(N.load().bfs_get_options(self._h, C.byref(o)), "bfs_get_options")
+        return {k: getattr(o, k) for k, _ in N.Options._fields_ if k != "reserved"}
+
+    def set_options(self, **kw) -> None:
+        o = N.Options()
+        lib = N.load()
+        N.check(lib.bfs_get_options(self._h, C.byref(o)), "bfs_get_options")
+        for k, v in kw.items():
+            if k == "mode" and isinstance(v, str):
+                v = {"persistent": N.BFS_MODE_PERSISTENT, "stepwise": N.BFS_MODE_STEPWISE}[v]
+            setattr(o, k, int(v))
+        N.check(lib.bfs_set_options(self._h, C.byref(o)), "bfs_set_options")
+
+    # ---- traversal ----------------------------------------------------
+    def run(self, source: int, parents: bool = True):
+        """Levels (int32, -1 unreached), parents (uint32) and stats of one traversal."""
+        n = self.num_vertices
+        lev = np.empty(n, dtype=np.int32)
+        par = np.empty(n, dtype=np.uint32) if parents else None
+        st = N.Stats()
+        N.check(N.load().bfs_run(self._h, int(source), _ptr(lev, C.c_int32),
+                                 None if par is None else _ptr(par, C.c_uint32), C.byref(st)),
+                f"bfs_run(source={source})")
+        return lev, par, st.as_dict()
+
+    def run_device(self, source: int, levels_ptr: int, parents_ptr: int = 0, stream: int = 0) -> None:
+        """Enqueues a traversal writing caller-owned device buffers on `stream`."""
+        N.check(N.load().bfs_run_device(self._h, int(source), C.c_void_p(levels_ptr),
+                                        C.c_void_p(parents_ptr) if parents_ptr else None,
+                                        C.c_void_p(stream) if stream else None), "bfs_run_device")
+
+    def last_stats(self) -> dict:
+        st = N.Stats()
+        N.check(N.load().bfs_last_stats(self._h, C.byref(st)), "bfs_last_stats")
+        return st.as_dict()
+
+
+# ---- tools (the reference's tools/ CLIs) ------------------------------
+def tool_csr_tiling(edge_list: str, weighted: bool = False) -> None:
+    N.check(N.load().bfs_tool_csr_tiling(edge_list.encode(), N.BFS_LOAD_WEIGHTED if weighted else 0),
+            f"csr_tiling {edge_list}")
+
+
+def tool_coo_tiling(data: str, min_w: int, max_w: int) -> None:
+    N.check(N.load().bfs_tool_coo_tiling(data.encode(), min_w, max_w, 0), f"coo_tiling {data}")
+
+
+def tool_column_major(data: str, w: int, min_s: int, max_s: int) -> None:
+    N.check(N.load().bfs_tool_column_major(data.encode(), w, min_s, max_s, 0), f"column_major_tile {data}")
+
+
+def tool_vertex_remap(data: str) -> None:
+    N.check(N.load().bfs_tool_vertex_remap(data.encode(), 0), f"vertex_id_remap {data}")
+
+
+def write_level_dump(directory: str, levels) -> None:
+    lev = np.ascontiguousarray(levels, dtype=np.int32)
+    N.check(N.load().bfs_write_level_dump(directory.encode(), lev.size, _ptr(lev, C.c_int32)),
+            f"level dump {directory}")
+
+
+def write_edge_list(path: str, num_vertices: int, src, dst) -> None:
+    """The "N M" + 1-indexed "u v" input format of README.md:19-24."""
+    s, d = _u32(src), _u32(dst)
+    with open(path, "w") as f:
+        f.write(f"{num_vertices} {s.size}\n")
+        if s.size:
+            np.savetxt(f, np.stack([s.astype(np.int64) + 1, d.astype(np.int64) + 1], axis=1), fmt="%d")
+
+
+# ---- synthetic inputs ---------------------------------------------------
+def gen_rmat(num_vertices: int, num_edges: int, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 1, dedup: bool = True, no_self_loops: bool = True, permute: bool = False):
+    """Seeded R-MAT edge list (uint32 src, dst) with exactly num_edges edges."""
+    p = N.RmatParams()
+    p.num_vertices = num_vertices
+    p.num_edges = num_edges
+    p.a, p.b, p.c = a, b, c
+    p.seed = seed
+    p.flags = ((N.BFS_RMAT_DEDUP if dedup else 0) | (N.BFS_RMAT_NO_SELF_LOOPS if no_self_loops else 0)
+               | (N.BFS_RMAT_PERMUTE if permute else 0))
+    src = np.empty(num_edges, dtype=np.uint32)
+    dst = np.empty(num_edges, dtype=np.uint32)
+    N.check(N.load().bfs_gen_rmat(C.byref(p), _ptr(src, C.c_uint32), _ptr(dst, C.c_uint32), num_edges),
+            "bfs_gen_rmat")
+    return src, dst
+
+
+def pick_sources(degrees, count: int, seed: int) -> np.ndarray:
+    """`count` seeded source vertices with out-degree > 0 (repeats allowed when few exist)."""
+    deg = np.asarray(degrees)
+    cand = np.flatnonzero(deg > 0)
+    if cand.size == 0:
+        raise ValueError("no vertex has an out-edge")
+    rng = np.random.default_rng(seed)
+    return cand[rng.integers(0, cand.size, size=count)].astype(np.uint32)

@@ -1,0 +1,214 @@
+/*
+ * bfs_gb300.h -- C ABI of the GB300-native GraphPhi BFS path.
+ *
+ * One shared library (libbfs_gb300.so) behind plain pointers and sizes.  It
+ * replaces the hot path of the reference's apps/bfs_simd/bfs.cpp (and the
+ * scalar twin apps/bfs_serial/bfs.cpp): the file loader, the hybrid
+ * top-down / bottom-up traversal and its level output, plus the preprocessing
+ * tools that write the tiled input files.  Each entry point names the
+ * reference interface it replaces.
+ *
+ * Conventions (all follow the reference):
+ *   - vertex ids are uint32_t, 0-based in memory, 1-based in the text files;
+ *   - levels are int32_t, -1 for unreached, 0 for the source (h_cost);
+ *   - parents are uint32_t, 0xFFFFFFFF for unreached, the source is its own
+ *     parent (h_graph_parents);
+ *   - every call returns a status code (BFS_OK == 0).
+ */
+#ifndef BFS_GB300_H
+#define BFS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+/* The reference exits with status 1 on a failed fopen
+ * (apps/bfs_simd/bfs.cpp:988-992, :1032-1035); the CLI maps every non-zero
+ * status below to that exit(1) with a message on stderr. */
+enum bfs_status {
+	BFS_OK = 0,
+	BFS_EIO = 1,          /* a file is missing or cannot be read/written */
+	BFS_EFORMAT = 2,      /* a file or array is truncated, garbled or inconsistent */
+	BFS_ENOMEM = 3,       /* host or device allocation failed */
+	BFS_EARG = 4,         /* invalid argument */
+	BFS_EBUDGET = 5,      /* admission refused: over the device-memory budget */
+	BFS_ETIMEOUT = 6,     /* a device-side wait hit its bound and returned */
+	BFS_ECUDA = 7,        /* a CUDA runtime call failed */
+	BFS_EUNSUPPORTED = 8, /* the tile width / stripe length cannot be packed */
+	BFS_ENODEV = 9        /* no CUDA device is available */
+};
+
+/* Short text for a status code (static storage). */
+const char *bfs_status_string(int status);
+
+/* ---- graph handle ------------------------------------------------------ */
+typedef struct bfs_graph bfs_graph;
+
+#define BFS_LOAD_WEIGHTED 0x1u     /* files carry "u v w" lines (-w); weights are dropped */
+#define BFS_LOAD_PREFER_REORDER 0x2u /* try <data>_reorder_* before <data>_* */
+#define BFS_LOAD_HOST_ONLY 0x4u    /* parse and validate only; allocate nothing on the GPU */
+
+/*
+ * Loads a graph from the reference's tiled text files and uploads it to HBM.
+ * Replaces graph_input (apps/bfs_simd/bfs.cpp:968-1118; apps/bfs_serial/bfs.cpp:762-910).
+ *
+ * Reads <base>_col-<S>-coo-tiled-<W>-{0..63,offsets} (column-major COO tiles,
+ * tools/column_major_tile) and <base>_untiled-{0..63,nneibor} (CSR,
+ * tools/csr_tiling), where <base> is `data` (the bfs_serial / README naming,
+ * README.md:64-67) or, when those files are absent, `data`_reorder (the
+ * bfs_simd naming, apps/bfs_simd/bfs.cpp:983).  BFS_LOAD_PREFER_REORDER
+ * reverses that order.
+ */
+int bfs_graph_load(const char *data, uint32_t tile_width, uint32_t stripe_length,
+		uint32_t flags, bfs_graph **out);
+
+/*
+ * Builds the same graph from an in-memory directed edge list (0-based, any
+ * order, duplicates and self loops kept as given).  Equivalent to running
+ * tools/csr_tiling, tools/coo_tiling and tools/column_major_tile on the list
+ * and loading the result with bfs_graph_load.
+ */
+int bfs_graph_from_edges(uint32_t num_vertices, uint64_t num_edges, const uint32_t *src,
+		const uint32_t *dst, uint32_t tile_width, uint32_t stripe_length, uint32_t flags,
+		bfs_graph **out);
+
+/*
+ * Builds the graph from the arrays graph_input produces
+ * (apps/bfs_simd/bfs.cpp:968-1118): CSR out-degrees (graph_degrees[N]) and
+ * destinations (graph_edges[E]), the column-major COO edges
+ * (graph_heads[E], graph_tails[E], 0-based) and tile_offsets[SIDE*SIDE].
+ * tile_offsets may be NULL (derived from the edges).
+ */
+int bfs_graph_from_arrays(uint32_t num_vertices, uint64_t num_edges, const uint32_t *degrees,
+		const uint32_t *csr_dst, const uint32_t *heads, const uint32_t *tails,
+		const uint32_t *tile_offsets, uint32_t tile_width, uint32_t stripe_length,
+		uint32_t flags, bfs_graph **out);
+
+int bfs_graph_free(bfs_graph *g);
+
+typedef struct bfs_graph_info {
+	uint32_t num_vertices;     /* NNODES */
+	uint32_t tile_width;       /* TILE_WIDTH */
+	uint64_t num_edges;        /* NEDGES */
+	uint32_t stripe_length;    /* ROW_STEP */
+	uint32_t side_length;      /* SIDE_LENGTH = ceil(N / W) */
+	uint64_t num_tiles;        /* SIDE_LENGTH^2 */
+	uint32_t num_stripes;      /* ceil(SIDE / S) */
+	uint32_t num_groups;       /* destination column groups of the packed tile stream */
+	uint64_t packed_words;     /* 32-bit words of the packed column-major stream (edges + padding) */
+	uint64_t device_bytes;     /* HBM held by the graph */
+	uint32_t max_out_degree;
+	uint32_t used_reorder;     /* 1 if the <data>_reorder files were loaded */
+	char base[1024];           /* the file base that was loaded, "" for in-memory graphs */
+} bfs_graph_info;
+
+int bfs_graph_get_info(const bfs_graph *g, bfs_graph_info *info);
+
+/* Out-degrees (graph_degrees) and CSR destinations copied to host memory. */
+int bfs_graph_get_degrees(const bfs_graph *g, uint32_t *degrees);
+
+/* ---- traversal options ------------------------------------------------- */
+#define BFS_MODE_PERSISTENT 0u /* the whole traversal in one cooperative launch */
+#define BFS_MODE_STEPWISE 1u   /* one launch per step, host-driven (profiling / plain form) */
+
+typedef struct bfs_options {
+	uint32_t mode;             /* BFS_MODE_* */
+	uint32_t to_dense_ratio;   /* go dense when frontier + out_degree > E / to_dense_ratio
+	                              (the reference's T_RATIO = 20, apps/bfs_simd/bfs.cpp:832,1171) */
+	uint32_t to_sparse_ratio;  /* stay dense while frontier + out_degree > E / to_sparse_ratio
+	                              (the reference uses the same ratio for both) */
+	uint32_t warp_max_degree;  /* top-down: degree <= this -> warp-cooperative gather */
+	uint32_t cta_max_degree;   /* top-down: degree <= this -> one CTA per vertex; above -> grid-strided */
+	uint32_t reserved[3];
+} bfs_options;
+
+/* Fills the defaults (reference switch rule, persistent mode). */
+int bfs_options_default(bfs_options *opt);
+int bfs_set_options(bfs_graph *g, const bfs_options *opt);
+int bfs_get_options(const bfs_graph *g, bfs_options *opt);
+
+/* ---- single-source traversal ------------------------------------------- */
+#define BFS_TRACE_MAX 256
+
+typedef struct bfs_stats {
+	uint32_t num_steps;        /* traversal steps run (the reference's loop iterations + 1) */
+	uint32_t dense_steps;      /* steps run bottom-up over the column-major tiles */
+	uint32_t reached;          /* vertices with level >= 0 */
+	uint32_t max_level;
+	uint64_t edges_traversed;  /* m(s): sum of out-degrees of reached vertices (TEPS numerator) */
+	uint64_t td_edges;         /* CSR edges read by top-down steps */
+	uint64_t td_vertices;      /* frontier vertices expanded top-down */
+	uint64_t bu_words;         /* packed tile words streamed by bottom-up steps */
+	uint64_t bu_slices;        /* frontier slices staged by bottom-up steps */
+	uint64_t bu_groups;        /* column groups visited by bottom-up steps */
+	double device_ms;          /* device time of the traversal, initialisation included (CUDA events) */
+	double kernel_ms;          /* device time of the traversal kernel(s) alone */
+	int32_t status;            /* device-side status of the run (BFS_OK or BFS_ETIMEOUT) */
+	uint32_t grid_ctas;        /* CTAs of the persistent launch */
+	uint8_t trace[BFS_TRACE_MAX]; /* trace[i] = 1 if step i was dense (first BFS_TRACE_MAX steps) */
+} bfs_stats;
+
+/*
+ * One traversal from `source`, outputs to HOST memory (either may be NULL).
+ * Replaces graph_prepare (apps/bfs_simd/bfs.cpp:753-963): the same first
+ * top-down step, the same dense/sparse switch rule by default, the same
+ * h_cost levels.  Synchronous.
+ */
+int bfs_run(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, bfs_stats *stats);
+
+/*
+ * The same traversal with caller-owned DEVICE outputs (levels[N] int32,
+ * parents[N] uint32 or NULL), enqueued on `stream` (a cudaStream_t, NULL for
+ * the default stream).  Asynchronous: nothing is copied to the host.
+ * bfs_last_stats() synchronises and returns the stats of the last run.
+ */
+int bfs_run_device(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, void *stream);
+int bfs_last_stats(bfs_graph *g, bfs_stats *stats);
+
+/* ---- level dump --------------------------------------------------------- */
+/* Writes <dir>/path<t>.txt, t = 0..63, "<v>) cost:<level>\n", floor(N/64)
+ * vertices per file, the last taking the rest: the ONEDEBUG dump of
+ * apps/bfs_simd/bfs.cpp:927-954. */
+int bfs_write_level_dump(const char *dir, uint32_t num_vertices, const int32_t *levels);
+
+/* ---- preprocessing tools (the reference's tools/ CLIs) ------------------ */
+/* tools/csr_tiling/page_rank.cpp main: <edge_list> -> <edge_list>_untiled-{0..63,nneibor}. */
+int bfs_tool_csr_tiling(const char *edge_list, uint32_t flags);
+/* tools/coo_tiling/page_rank.cpp main: <data>_untiled-* -> <data>_coo-tiled-<W>-*,
+ * W from min_w to max_w doubling. */
+int bfs_tool_coo_tiling(const char *data, uint32_t min_w, uint32_t max_w, uint32_t flags);
+/* tools/column_major_tile/kcore.cpp main: <data>_coo-tiled-<W>-* ->
+ * <data>_col-<S>-coo-tiled-<W>-*, S from min_s to max_s doubling. */
+int bfs_tool_column_major(const char *data, uint32_t w, uint32_t min_s, uint32_t max_s,
+		uint32_t flags);
+/* tools/vertex_id_remap/bfs.cpp main: <data>_untiled-* -> <data>_reorder
+ * (BFS-discovery relabelling from vertex 0). */
+int bfs_tool_vertex_remap(const char *data, uint32_t flags);
+
+/* ---- synthetic inputs (no counterpart in the reference) ------------------ */
+#define BFS_RMAT_NO_SELF_LOOPS 0x1u
+#define BFS_RMAT_DEDUP 0x2u
+#define BFS_RMAT_PERMUTE 0x4u   /* random relabelling of the vertex ids */
+
+typedef struct bfs_rmat_params {
+	uint32_t num_vertices;   /* N, any value >= 1 (ids >= N are rejected and redrawn) */
+	uint32_t flags;          /* BFS_RMAT_* */
+	uint64_t num_edges;      /* exact E after the cleaning the flags ask for */
+	double a, b, c;          /* quadrant probabilities, d = 1 - a - b - c */
+	uint64_t seed;
+} bfs_rmat_params;
+
+/* Seeded, platform-independent R-MAT edge list into src/dst (capacity >= num_edges). */
+int bfs_gen_rmat(const bfs_rmat_params *p, uint32_t *src, uint32_t *dst, uint64_t capacity);
+
+/* Library version string. */
+const char *bfs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BFS_GB300_H */

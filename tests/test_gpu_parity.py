@@ -1,0 +1,193 @@
+"""Parity of the CUDA path (through the C ABI) with the reference's levels.
+
+Golden levels come from the reference's own bfs_simd; bigger graphs are
+checked against the oracle's restatement of it.  Levels must be bit-exact;
+parents must form a valid BFS tree; the direction trace must equal the
+oracle's under the reference's switch rule.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import golden_case_names, load_case
+
+pytestmark = pytest.mark.gpu
+CASES = golden_case_names()
+
+
+def _check_run(B, oracle, arr, g, src, expect=None, trace=True):
+    lev, par, st = g.run(int(src))
+    if expect is None:
+        expect = oracle.bfs_levels(arr, int(src))
+    np.testing.assert_array_equal(lev, expect, err_msg=f"levels differ from source {src}")
+    assert oracle.check_parents(arr, int(src), lev, par) == 0, "parents are not a BFS tree"
+    assert st["status"] == 0
+    assert st["reached"] == int((lev >= 0).sum())
+    deg = arr["degrees"].astype(np.uint64)
+    assert st["edges_traversed"] == int(deg[lev >= 0].sum())
+    if trace:
+        _, _, otrace, _ = oracle.bfs_hybrid(arr, int(src))
+        n = min(len(otrace), st["num_steps"])
+        assert st["trace"][:n] == otrace[:n], "direction trace differs from the reference rule"
+    return lev, st
+
+
+@pytest.mark.parametrize("mode", ["persistent", "stepwise"])
+@pytest.mark.parametrize("name", CASES)
+def test_golden_levels_from_edges(native, oracle, name, mode):
+    import bfs_simd_benchmarks_gb300 as B
+    c = load_case(name)
+    arr = oracle.arrays_from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"])
+    with B.Graph.from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"]) as g:
+        g.set_options(mode=mode)
+        for i, src in enumerate(c["sources"]):
+            _check_run(B, oracle, arr, g, src, expect=c["levels"][i])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_golden_levels_from_reference_files(native, oracle, name, tmp_path):
+    """bfs_graph_load on files written by the product tools (the README pipeline)."""
+    import bfs_simd_benchmarks_gb300 as B
+    c = load_case(name)
+    arr = oracle.arrays_from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"])
+    base = str(tmp_path / "out.x")
+    B.write_edge_list(base, c["n"], c["src"], c["dst"])
+    B.tool_csr_tiling(base)
+    B.tool_coo_tiling(base, c["w"], c["w"])
+    B.tool_column_major(base, c["w"], c["s"], c["s"])
+    with B.Graph.load(base, c["w"], c["s"]) as g:
+        for i, src in enumerate(c["sources"]):
+            _check_run(B, oracle, arr, g, src, expect=c["levels"][i], trace=False)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_golden_levels_from_arrays(native, oracle, name):
+    import bfs_simd_benchmarks_gb300 as B
+    c = load_case(name)
+    arr = oracle.arrays_from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"])
+    with B.Graph.from_arrays(c["n"], arr["degrees"], arr["csr_dst"], arr["heads"], arr["tails"],
+                             arr["tile_offsets"], c["w"], c["s"]) as g:
+        for i, src in enumerate(c["sources"]):
+            _check_run(B, oracle, arr, g, src, expect=c["levels"][i], trace=False)
+
+
+@pytest.mark.parametrize("w,s", [(512, 8), (1024, 16), (2048, 32), (4096, 8), (96, 7)])
+def test_tile_shapes_scale14(native, oracle, w, s):
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 14
+    src, dst = B.gen_rmat(n, 16 * n, seed=1400 + w + s, permute=True)
+    arr = oracle.arrays_from_edges(n, src, dst, w, s)
+    srcs = B.pick_sources(arr["degrees"], 4, seed=w * 7 + s)
+    with B.Graph.from_edges(n, src, dst, w, s) as g:
+        for sv in srcs:
+            _check_run(B, oracle, arr, g, sv)
+
+
+def test_direction_thresholds_do_not_change_levels(native, oracle):
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 15
+    src, dst = B.gen_rmat(n, 16 * n, seed=77)
+    arr = oracle.arrays_from_edges(n, src, dst, 1024, 16)
+    sv = int(B.pick_sources(arr["degrees"], 1, seed=5)[0])
+    ref = oracle.bfs_levels(arr, sv)
+    with B.Graph.from_edges(n, src, dst, 1024, 16) as g:
+        seen = set()
+        for td, ts, wmax, cmax in [(20, 20, 32, 4096), (1, 1, 32, 4096), (100000, 100000, 32, 4096),
+                                   (5, 50, 8, 64), (200, 10, 64, 100000)]:
+            g.set_options(to_dense_ratio=td, to_sparse_ratio=ts, warp_max_degree=wmax, cta_max_degree=cmax)
+            lev, par, st = g.run(sv)
+            np.testing.assert_array_equal(lev, ref)
+            assert oracle.check_parents(arr, sv, lev, par) == 0
+            seen.add(tuple(st["trace"]))
+        assert len(seen) > 1, "the options should change the direction trace"
+
+
+def test_edge_cases(native, oracle):
+    import bfs_simd_benchmarks_gb300 as B
+    # no edges at all
+    with B.Graph.from_edges(10, np.zeros(0, np.uint32), np.zeros(0, np.uint32), 4, 2) as g:
+        lev, par, st = g.run(3)
+        exp = np.full(10, -1, np.int32)
+        exp[3] = 0
+        np.testing.assert_array_equal(lev, exp)
+        assert par[3] == 3 and st["reached"] == 1
+    # a single vertex with a self loop
+    with B.Graph.from_edges(1, np.zeros(1, np.uint32), np.zeros(1, np.uint32), 1024, 16) as g:
+        lev, _, _ = g.run(0)
+        assert lev.tolist() == [0]
+    # source without out-edges in a non-trivial graph; N not a multiple of 32
+    n = 1000
+    src, dst = B.gen_rmat(n, 8000, seed=3)
+    arr = oracle.arrays_from_edges(n, src, dst, 64, 3)
+    sink = int(np.flatnonzero(arr["degrees"] == 0)[0])
+    with B.Graph.from_edges(n, src, dst, 64, 3) as g:
+        lev, _, st = g.run(sink)
+        assert (lev >= 0).sum() == 1 and lev[sink] == 0
+        with pytest.raises(B.BfsError):
+            g.run(n)  # source out of range
+
+
+def test_run_device_on_torch_stream(native, oracle):
+    torch = pytest.importorskip("torch")
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 14
+    src, dst = B.gen_rmat(n, 16 * n, seed=9)
+    arr = oracle.arrays_from_edges(n, src, dst, 1024, 16)
+    sv = int(B.pick_sources(arr["degrees"], 1, seed=1)[0])
+    with B.Graph.from_edges(n, src, dst, 1024, 16) as g:
+        lev = torch.empty(n, dtype=torch.int32, device="cuda")
+        par = torch.empty(n, dtype=torch.int32, device="cuda")
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            g.run_device(sv, lev.data_ptr(), par.data_ptr(), s.cuda_stream)
+        st = g.last_stats()
+        s.synchronize()
+        np.testing.assert_array_equal(lev.cpu().numpy(), oracle.bfs_levels(arr, sv))
+        assert oracle.check_parents(arr, sv, lev.cpu().numpy(), par.cpu().numpy().view(np.uint32)) == 0
+        assert st["status"] == 0
+
+
+def test_cli_dump_matches_reference_format(native, oracle, tmp_path):
+    import bfs_simd_benchmarks_gb300 as B
+    from bfs_simd_benchmarks_gb300 import build
+    c = load_case("rmat10_w64_s3")
+    base = str(tmp_path / "out.x")
+    B.write_edge_list(base, c["n"], c["src"], c["dst"])
+    B.tool_csr_tiling(base)
+    B.tool_coo_tiling(base, 64, 64)
+    B.tool_column_major(base, 64, 3, 3)
+    (tmp_path / "path").mkdir()
+    env = dict(os.environ, BFS_PATH_DUMP="1", BFS_RUNS="3")
+    r = subprocess.run([build.CLI, base, "64", "3", "-x"], capture_output=True, text=True, cwd=tmp_path, env=env)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    assert len(lines) == 4 and lines[-1].startswith("Average: ")
+    assert all(len(l.split()) == 2 for l in lines[:3])
+    ref = tmp_path / "ref"
+    ref.mkdir()
+    oracle.write_path_dump(str(ref), c["levels"][0])   # source 0 = the CLI default
+    for t in range(64):
+        assert (tmp_path / "path" / f"path{t}.txt").read_bytes() == (ref / f"path{t}.txt").read_bytes()
+
+
+def test_pokec_shape_64_sources(native, oracle):
+    """1,632,803 vertices / 30,622,564 edges, permuted R-MAT, W=1024 S=16, 64 sources."""
+    import bfs_simd_benchmarks_gb300 as B
+    from bfs_simd_benchmarks_gb300 import workloads
+    wl = workloads.get("pokec")
+    src, dst = wl.edges()
+    arr = oracle.arrays_from_edges(wl.n, src, dst, wl.w, wl.s)
+    srcs = wl.sources(arr["degrees"])
+    assert len(srcs) == 64
+    with B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s) as g:
+        for sv in srcs:
+            lev, par, st = g.run(int(sv))
+            ref, _, trace, _ = oracle.bfs_hybrid(arr, int(sv))
+            np.testing.assert_array_equal(lev, ref, err_msg=f"source {sv}")
+            k = min(len(trace), st["num_steps"])
+            assert st["trace"][:k] == trace[:k]
+        assert oracle.check_parents(arr, int(sv), lev, par) == 0
