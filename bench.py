@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--mode", choices=["persistent", "stepwise"], default="persistent")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sources", type=int, default=0, help="use only the first K sources (profiling runs)")
     return ap.parse_args()
 
 
@@ -233,6 +234,8 @@ def main():
     t_gen = time.perf_counter() - t_gen
     degrees = g.degrees()
     sources = wl.sources(degrees)
+    if args.sources:
+        sources = sources[: args.sources]
     n = wl.n
     sw = wl.s * wl.w
     dev = torch.device("cuda", local)
