@@ -337,7 +337,12 @@ def main():
                               "ms_per_traversal_p99": float(np.percentile(trav_ms, 99)),
                               "edges_per_traversal_mean": edges / len(timed),
                               "dense_steps_mean": statistics.mean(st["dense_steps"] for _, _, st in timed),
-                              "steps_mean": statistics.mean(st["num_steps"] for _, _, st in timed)},
+                              "steps_mean": statistics.mean(st["num_steps"] for _, _, st in timed),
+                              "phase_ms_mean": {k: statistics.mean(st[k] for _, _, st in timed)
+                                                for k in ("dense_ms", "to_dense_ms", "sparse_ms", "to_sparse_ms")},
+                              "example_steps": {"trace": timed[0][2]["trace"], "step_ms": timed[0][2]["step_ms"]},
+                              "bu_cycles_per_cta_mean": [round(statistics.mean(st["bu_cycles"][i] for _, _, st in timed)
+                                                               / max(1, timed[0][2]["grid_ctas"])) for i in range(6)]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_bfs_persistent", "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"

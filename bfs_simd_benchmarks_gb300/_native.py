@@ -85,11 +85,20 @@ class Stats(C.Structure):
         ("status", C.c_int32),
         ("grid_ctas", C.c_uint32),
         ("trace", C.c_uint8 * BFS_TRACE_MAX),
+        ("dense_ms", C.c_double),
+        ("to_dense_ms", C.c_double),
+        ("sparse_ms", C.c_double),
+        ("to_sparse_ms", C.c_double),
+        ("step_ms", C.c_float * BFS_TRACE_MAX),
+        ("bu_cycles", C.c_uint64 * 8),
     ]
 
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "trace"}
-        d["trace"] = list(self.trace[: min(self.num_steps, BFS_TRACE_MAX)])
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("trace", "step_ms", "bu_cycles")}
+        d["bu_cycles"] = list(self.bu_cycles[:6])
+        k = min(self.num_steps, BFS_TRACE_MAX)
+        d["trace"] = list(self.trace[:k])
+        d["step_ms"] = [round(x, 5) for x in self.step_ms[:k]]
         return d
 
 

@@ -16,7 +16,7 @@ using namespace bfsg;
 namespace {
 
 constexpr uint32_t kMaxGroupVertices = 32768;  // shared-memory bitmaps of one column group
-constexpr uint32_t kGroupsPerCta = 2;
+constexpr uint32_t kGroupsPerCta = 1;
 
 struct DevBuf {
 	void *p = nullptr;
@@ -137,7 +137,7 @@ int upload(bfs_graph *g, HostGraph &h) {
 	if (!coop) return BFS_EUNSUPPORTED;
 
 	PackedTiles pk;
-	int st = pack_tiles(h, (uint32_t) g->num_sms * 2 * kGroupsPerCta, kMaxGroupVertices, pk);
+	int st = pack_tiles(h, (uint32_t) g->num_sms * 2 * kGroupsPerCta, kMaxGroupVertices, pk);  // about one group per CTA
 	if (st) return st;
 	g->num_groups = pk.num_groups;
 	g->packed_words = pk.words.size();
@@ -159,6 +159,9 @@ int upload(bfs_graph *g, HostGraph &h) {
 	d.max_group_words = (pk.max_group_vertices + 31) / 32;
 	d.slice_words = (d.sw + 31) / 32;
 	d.nwords = (h.n + 31) / 32;
+	d.bm_words = d.num_stripes * d.slice_words;  // bulk copies read whole slices
+	d.tma = (d.sw % 128 == 0) ? 1u : 0u;
+	d.tma_batch = std::max<uint32_t>(1, std::min<uint32_t>(kMaxSliceBatch, kTmaSliceWords / d.slice_words));
 	if ((st = dev_upload(g, &d.row_off, h.row_off))) return st;
 	if ((st = dev_upload(g, &d.col, h.csr_dst))) return st;
 	if ((st = dev_upload(g, &d.packed, pk.words))) return st;
@@ -170,7 +173,7 @@ int upload(bfs_graph *g, HostGraph &h) {
 	RunCtx &r = g->rc;
 	if ((st = dev_alloc(g, &r.vis, d.nwords))) return st;
 	for (int i = 0; i < 3; ++i) {
-		if ((st = dev_alloc(g, &r.bm[i], d.nwords))) return st;
+		if ((st = dev_alloc(g, &r.bm[i], d.bm_words))) return st;
 		if ((st = dev_alloc(g, &r.sf[i], d.num_stripes))) return st;
 	}
 	for (int set = 0; set < 2; ++set)
@@ -324,7 +327,18 @@ int collect_stats(bfs_graph *g, bfs_stats *out) {
 		s.reached = (uint32_t) d.reached;
 		s.edges_traversed = d.edges_traversed;
 		std::memcpy(s.trace, d.trace, sizeof(s.trace));
+		// Phase timers from the device timestamps.
+		for (uint32_t i = 0; i < s.num_steps && i < BFS_TRACE_MAX && i + 1 < 257; ++i) {
+			const unsigned long long t0 = d.t_step[i], t1 = d.t_step[i + 1];
+			if (!t0 || t1 < t0) continue;
+			double total = (t1 - t0) * 1e-6, conv = 0;
+			if (d.t_conv[i] >= t0 && d.t_conv[i] <= t1 && d.t_conv[i]) conv = (d.t_conv[i] - t0) * 1e-6;
+			s.step_ms[i] = (float) total;
+			if (s.trace[i]) { s.dense_ms += total - conv; s.to_dense_ms += conv; }
+			else { s.sparse_ms += total - conv; s.to_sparse_ms += conv; }
+		}
 	}
+	for (int i = 0; i < 8; ++i) s.bu_cycles[i] = d.bu_cycles[i];
 	s.td_edges = d.td_edges;
 	s.td_vertices = d.td_vertices;
 	s.bu_words = d.bu_words;

@@ -19,10 +19,13 @@ struct DevGraph {
 	uint32_t max_group_words;   // 32-bit words of the largest group bitmap
 	uint32_t slice_words;       // 32-bit words of one stripe's frontier slice
 	uint32_t nwords;            // ceil(n / 32)
+	uint32_t bm_words;          // words of a frontier bitmap, padded to whole stripe slices
+	uint32_t tma;               // 1: the bottom-up step streams segments and slices with bulk copies
+	uint32_t tma_batch;         // frontier slices per bulk-copy stage
 	const uint32_t *row_off;    // [n+1] CSR row starts
 	const uint32_t *col;        // [m]   CSR destinations
 	const uint32_t *packed;     // packed column-major stream (16-byte aligned segments)
-	const uint32_t *seg_off;    // [num_stripes*num_groups+1]
+	const uint32_t *seg_off;    // [num_groups*num_stripes+1], group-major
 	const uint32_t *group_col;  // [num_groups+1]
 	const uint32_t *hasin;      // [nwords] in-degree > 0
 };
@@ -50,6 +53,13 @@ struct DevStats {
 	int status;
 	unsigned int pad;
 	unsigned char trace[256];
+	// globaltimer stamps taken by CTA 0 after the grid barriers: the start of
+	// every step and the end of its queue<->bitmap conversion (if any)
+	unsigned long long t_step[257];
+	unsigned long long t_conv[256];
+	// SM cycles summed over CTAs inside the bottom-up step: group setup,
+	// window lists, consumer wait, consumer work, producer wait, publish
+	unsigned long long bu_cycles[8];
 };
 
 // Scratch of one traversal context (owned by the graph's run context).

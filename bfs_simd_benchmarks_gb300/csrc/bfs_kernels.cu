@@ -46,45 +46,94 @@ __device__ __forceinline__ uint32_t bucket_of(uint32_t deg, const StepParams &p)
 	return deg <= p.warp_max_degree ? 0u : (deg <= p.cta_max_degree ? 1u : 2u);
 }
 
-__device__ __forceinline__ bool try_claim(uint32_t *vis, uint32_t v) {
-	uint32_t bit = 1u << (v & 31);
-	uint32_t *w = vis + (v >> 5);
-	if (ld_cg(w) & bit) return false;
-	return !(atomicOr(w, bit) & bit);
+constexpr int kTdPerLane = 4;  // candidate edges a lane handles per top-down iteration
+
+// All 32 lanes of the warp call this with up to kTdPerLane candidate edges
+// u[q] -> v[q] each (has[q] false for an empty slot).  The visited checks,
+// the claiming atomicOr's and the degree loads of the claimed vertices are
+// each issued for all candidates before any result is used, so a lane waits
+// for one round trip per stage rather than one per edge.  Claimed vertices
+// get their level and parent and are appended to the next queue bucket of
+// their out-degree with one atomicAdd per warp and bucket.
+__device__ __forceinline__ void visit_and_append(const bool (&has)[kTdPerLane], const uint32_t (&u)[kTdPerLane],
+		const uint32_t (&v)[kTdPerLane], int32_t next_level, const DevGraph &g, const RunCtx &r,
+		uint32_t *const *qn, unsigned *tails, const StepParams &p, ThreadAcc &acc) {
+	bool cand[kTdPerLane];
+	uint32_t word[kTdPerLane];
+#pragma unroll
+	for (int q = 0; q < kTdPerLane; ++q) {
+		cand[q] = has[q];
+		word[q] = cand[q] ? ld_cg(r.vis + (v[q] >> 5)) : 0u;
+	}
+#pragma unroll
+	for (int q = 0; q < kTdPerLane; ++q) {
+		const uint32_t bit = 1u << (v[q] & 31);
+		if (cand[q] && (word[q] & bit)) cand[q] = false;
+		if (cand[q]) word[q] = atomicOr(r.vis + (v[q] >> 5), bit);
+	}
+	uint32_t deg[kTdPerLane];
+	bool claimed[kTdPerLane];
+#pragma unroll
+	for (int q = 0; q < kTdPerLane; ++q) {
+		claimed[q] = cand[q] && !(word[q] & (1u << (v[q] & 31)));
+		deg[q] = claimed[q] ? __ldg(g.row_off + v[q] + 1) - __ldg(g.row_off + v[q]) : 0u;
+	}
+	uint32_t cnt[3] = {0, 0, 0};
+#pragma unroll
+	for (int q = 0; q < kTdPerLane; ++q) {
+		if (!claimed[q]) continue;
+		r.level[v[q]] = next_level;
+		if (r.parent) r.parent[v[q]] = u[q];
+		acc.count++;
+		acc.degsum += deg[q];
+		cnt[bucket_of(deg[q], p)]++;
+	}
+	if (!__ballot_sync(kFull, cnt[0] | cnt[1] | cnt[2])) return;
+	const unsigned lane = lane_id();
+	uint32_t pos[3];
+#pragma unroll
+	for (int bk = 0; bk < 3; ++bk) {
+		const uint32_t incl = warp_incl_scan(cnt[bk]);
+		const uint32_t tot = __shfl_sync(kFull, incl, 31);
+		uint32_t base = 0;
+		if (lane == 31 && tot) base = atomicAdd(&tails[bk], tot);
+		base = __shfl_sync(kFull, base, 31);
+		pos[bk] = base + incl - cnt[bk];
+	}
+#pragma unroll
+	for (int q = 0; q < kTdPerLane; ++q) {
+		if (!claimed[q]) continue;
+		const uint32_t bk = bucket_of(deg[q], p);
+		qn[bk][pos[bk]++] = v[q];
+	}
 }
 
-// All 32 lanes of the warp call this with one candidate edge u->v each.
-__device__ __forceinline__ void visit_and_append(bool has, uint32_t u, uint32_t v, int32_t next_level,
-		const DevGraph &g, const RunCtx &r, uint32_t *const *qn, unsigned *tails,
-		const StepParams &p, ThreadAcc &acc) {
-	bool claimed = false;
-	uint32_t deg = 0;
-	if (has && try_claim(r.vis, v)) {
-		claimed = true;
-		r.level[v] = next_level;
-		if (r.parent) r.parent[v] = u;
-		deg = __ldg(g.row_off + v + 1) - __ldg(g.row_off + v);
-		acc.count++;
-		acc.degsum += deg;
+// Vertices of a top-down chunk staged in shared memory.
+struct ExpandShared {
+	uint32_t u[kThreads], beg[kThreads], pre[kThreads];
+	uint32_t wsum[kWarps];
+};
+__device__ __shared__ ExpandShared xsh;
+
+// CTA-wide inclusive scan (all threads call).
+__device__ __forceinline__ uint32_t block_incl_scan(uint32_t x) {
+	const unsigned lane = lane_id(), wid = warp_id();
+	uint32_t incl = warp_incl_scan(x);
+	if (lane == 31) xsh.wsum[wid] = incl;
+	__syncthreads();
+	if (wid == 0) {
+		uint32_t w = lane < kWarps ? xsh.wsum[lane] : 0u;
+		uint32_t wi = warp_incl_scan(w);
+		if (lane < kWarps) xsh.wsum[lane] = wi - w;
 	}
-	if (!__ballot_sync(kFull, claimed)) return;
-	const uint32_t b = bucket_of(deg, p);
-#pragma unroll
-	for (uint32_t bk = 0; bk < 3; ++bk) {
-		unsigned mask = __ballot_sync(kFull, claimed && b == bk);
-		if (!mask) continue;
-		int leader = __ffs(mask) - 1;
-		unsigned base = 0;
-		if (lane_id() == (unsigned) leader) base = atomicAdd(&tails[bk], (unsigned) __popc(mask));
-		base = __shfl_sync(kFull, base, leader);
-		if (claimed && b == bk) qn[bk][base + __popc(mask & lanemask_lt())] = v;
-	}
+	__syncthreads();
+	return incl + xsh.wsum[wid];
 }
 
 // ---------------------------------------------------------------------------
 // Top-down step (BFS_kernel_sparse + update_sparse, apps/bfs_simd/bfs.cpp:467-711)
 // ---------------------------------------------------------------------------
-__device__ void phase_expand(const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t step,
+__device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t step,
 		ThreadAcc &acc) {
 	const uint32_t cur = step & 1, nxt = (step + 1) & 1;
 	const StepCounters *in = r.ctr + (step + 2) % 3;
@@ -99,56 +148,124 @@ __device__ void phase_expand(const DevGraph &g, const RunCtx &r, const StepParam
 	const unsigned lane = lane_id(), wid = warp_id();
 	const uint64_t gwarp = (uint64_t) blockIdx.x * kWarps + wid;
 	const uint64_t nwarps = (uint64_t) gridDim.x * kWarps;
+	constexpr uint32_t kSpan = 32 * kTdPerLane;  // edges per warp iteration
+	bool has[kTdPerLane];
+	uint32_t uu[kTdPerLane], vv[kTdPerLane];
 
-	// Large out-degree: every warp of the grid takes a strided share of the edges.
-	for (uint32_t i = 0; i < nL; ++i) {
-		uint32_t u = ld_cg(qL + i);
-		uint32_t beg = __ldg(g.row_off + u), end = __ldg(g.row_off + u + 1);
-		for (uint64_t e0 = beg + gwarp * 32; e0 < end; e0 += nwarps * 32) {
-			uint64_t e = e0 + lane;
-			bool has = e < end;
-			uint32_t v = has ? __ldg(g.col + e) : 0u;
-			visit_and_append(has, u, v, nl, g, r, qn, tails, p, acc);
+	// Large out-degree: the edges of all large vertices form one flat range
+	// that every warp of the grid shares evenly.  Each CTA stages a chunk of
+	// up to kThreads large vertices with the inclusive prefix of their degrees
+	// in shared memory; a lane finds the owner of its edge by binary search.
+	for (uint32_t c0 = 0; c0 < nL; c0 += kThreads) {
+		const uint32_t cn = min((uint32_t) kThreads, nL - c0);
+		uint32_t deg = 0, u = 0, beg = 0;
+		if (threadIdx.x < cn) {
+			u = ld_cg(qL + c0 + threadIdx.x);
+			beg = __ldg(g.row_off + u);
+			deg = __ldg(g.row_off + u + 1) - beg;
 		}
-		if (blockIdx.x == 0 && threadIdx.x == 0) { acc.td_edges += end - beg; acc.td_vertices++; }
-	}
-	// Medium out-degree: one CTA per vertex.
-	for (uint32_t i = blockIdx.x; i < nM; i += gridDim.x) {
-		uint32_t u = ld_cg(qM + i);
-		uint32_t beg = __ldg(g.row_off + u), end = __ldg(g.row_off + u + 1);
-		for (uint64_t e0 = beg + (uint64_t) wid * 32; e0 < end; e0 += kThreads) {
-			uint64_t e = e0 + lane;
-			bool has = e < end;
-			uint32_t v = has ? __ldg(g.col + e) : 0u;
-			visit_and_append(has, u, v, nl, g, r, qn, tails, p, acc);
-		}
-		if (threadIdx.x == 0) { acc.td_edges += end - beg; acc.td_vertices++; }
-	}
-	// Small out-degree: one warp expands 32 vertices together.
-	for (uint64_t base = gwarp * 32; base < nS; base += nwarps * 32) {
-		uint64_t i = base + lane;
-		bool valid = i < nS;
-		uint32_t u = valid ? ld_cg(qS + i) : 0u;
-		uint32_t beg = valid ? __ldg(g.row_off + u) : 0u;
-		uint32_t deg = valid ? __ldg(g.row_off + u + 1) - beg : 0u;
-		uint32_t incl = warp_incl_scan(deg);
-		uint32_t total = __shfl_sync(kFull, incl, 31);
-		uint32_t excl = incl - deg;
-		for (uint32_t f0 = 0; f0 < total; f0 += 32) {
-			uint32_t f = f0 + lane;
-			bool has = f < total;
-			// owner = number of lanes whose inclusive degree sum is <= f
-			int lo = 0;
+		const uint32_t incl = block_incl_scan(deg);
+		xsh.u[threadIdx.x] = u;
+		xsh.beg[threadIdx.x] = beg;
+		xsh.pre[threadIdx.x] = incl;
+		__syncthreads();
+		const uint32_t total = xsh.pre[cn - 1];
+		const uint64_t per = ((total + nwarps - 1) / nwarps + kSpan - 1) / kSpan * kSpan;
+		const uint64_t lo = min((uint64_t) total, gwarp * per), hi = min((uint64_t) total, lo + per);
+		for (uint64_t f0 = lo; f0 < hi; f0 += kSpan) {
 #pragma unroll
-			for (int st = 16; st >= 1; st >>= 1) {
-				uint32_t val = __shfl_sync(kFull, incl, lo + st - 1);
-				if (val <= f) lo += st;
+			for (int q = 0; q < kTdPerLane; ++q) {
+				const uint64_t f = f0 + q * 32 + lane;
+				has[q] = f < hi;
+				uint32_t j = 0;  // owner: the number of entries whose inclusive prefix is <= f
+				if (has[q]) {
+#pragma unroll
+					for (uint32_t sp = kThreads / 2; sp >= 1; sp >>= 1)
+						if (j + sp < cn && xsh.pre[j + sp - 1] <= f) j += sp;
+				}
+				const uint32_t jj = min(j, cn - 1);
+				const uint32_t prev = jj ? xsh.pre[jj - 1] : 0u;
+				uu[q] = xsh.u[jj];
+				vv[q] = has[q] ? __ldg(g.col + xsh.beg[jj] + (uint32_t) (f - prev)) : 0u;
 			}
-			uint32_t ou = __shfl_sync(kFull, u, lo);
-			uint32_t ob = __shfl_sync(kFull, beg, lo);
-			uint32_t oe = __shfl_sync(kFull, excl, lo);
-			uint32_t v = has ? __ldg(g.col + ob + (f - oe)) : 0u;
-			visit_and_append(has, ou, v, nl, g, r, qn, tails, p, acc);
+			visit_and_append(has, uu, vv, nl, g, r, qn, tails, p, acc);
+		}
+		if (blockIdx.x == 0 && threadIdx.x == 0) { acc.td_edges += total; acc.td_vertices += cn; }
+		__syncthreads();
+	}
+	// Medium out-degree: a CTA expands a chunk of up to 32 vertices as one
+	// flat edge list (one vertex per chunk when there are fewer vertices than
+	// CTAs, so every CTA gets work).
+	{
+		const uint32_t chunk = max(1u, min(32u, nM / gridDim.x));
+		const uint32_t nchunks = (nM + chunk - 1) / chunk;
+		for (uint32_t ci = blockIdx.x; ci < nchunks; ci += gridDim.x) {
+			const uint32_t c0 = ci * chunk, cn = min(chunk, nM - c0);
+			if (wid == 0) {
+				uint32_t deg = 0, u = 0, beg = 0;
+				if (lane < cn) {
+					u = ld_cg(qM + c0 + lane);
+					beg = __ldg(g.row_off + u);
+					deg = __ldg(g.row_off + u + 1) - beg;
+				}
+				const uint32_t incl = warp_incl_scan(deg);
+				xsh.u[lane] = u;
+				xsh.beg[lane] = beg;
+				xsh.pre[lane] = incl;
+			}
+			__syncthreads();
+			const uint32_t total = xsh.pre[cn - 1];
+			for (uint64_t f0 = (uint64_t) wid * kSpan; f0 < total; f0 += (uint64_t) kWarps * kSpan) {
+#pragma unroll
+				for (int q = 0; q < kTdPerLane; ++q) {
+					const uint64_t f = f0 + q * 32 + lane;
+					has[q] = f < total;
+					uint32_t j = 0;
+					if (has[q]) {
+#pragma unroll
+						for (uint32_t sp = 16; sp >= 1; sp >>= 1)
+							if (j + sp < cn && xsh.pre[j + sp - 1] <= f) j += sp;
+					}
+					const uint32_t jj = min(j, cn - 1);
+					const uint32_t prev = jj ? xsh.pre[jj - 1] : 0u;
+					uu[q] = xsh.u[jj];
+					vv[q] = has[q] ? __ldg(g.col + xsh.beg[jj] + (uint32_t) (f - prev)) : 0u;
+				}
+				visit_and_append(has, uu, vv, nl, g, r, qn, tails, p, acc);
+			}
+			if (threadIdx.x == 0) { acc.td_edges += total; acc.td_vertices += cn; }
+			__syncthreads();
+		}
+	}
+	// Small out-degree: one warp expands 32 vertices together; lanes take
+	// consecutive edges of the warp's combined edge list.
+	for (uint64_t base = gwarp * 32; base < nS; base += nwarps * 32) {
+		const uint64_t i = base + lane;
+		const bool valid = i < nS;
+		const uint32_t u = valid ? ld_cg(qS + i) : 0u;
+		const uint32_t beg = valid ? __ldg(g.row_off + u) : 0u;
+		const uint32_t deg = valid ? __ldg(g.row_off + u + 1) - beg : 0u;
+		const uint32_t incl = warp_incl_scan(deg);
+		const uint32_t total = __shfl_sync(kFull, incl, 31);
+		const uint32_t excl = incl - deg;
+		for (uint32_t f0 = 0; f0 < total; f0 += kSpan) {
+#pragma unroll
+			for (int q = 0; q < kTdPerLane; ++q) {
+				const uint32_t f = f0 + q * 32 + lane;
+				has[q] = f < total;
+				// owner = number of lanes whose inclusive degree sum is <= f
+				int lo = 0;
+#pragma unroll
+				for (int st = 16; st >= 1; st >>= 1) {
+					const uint32_t val = __shfl_sync(kFull, incl, lo + st - 1);
+					if (val <= f) lo += st;
+				}
+				uu[q] = __shfl_sync(kFull, u, lo);
+				const uint32_t ob = __shfl_sync(kFull, beg, lo);
+				const uint32_t oe = __shfl_sync(kFull, excl, lo);
+				vv[q] = has[q] ? __ldg(g.col + ob + (f - oe)) : 0u;
+			}
+			visit_and_append(has, uu, vv, nl, g, r, qn, tails, p, acc);
 		}
 		const unsigned nvalid = (unsigned) __popc(__ballot_sync(kFull, valid));
 		if (lane == 0) {
@@ -161,7 +278,7 @@ __device__ void phase_expand(const DevGraph &g, const RunCtx &r, const StepParam
 // ---------------------------------------------------------------------------
 // Queue -> bitmap (to_dense, apps/bfs_simd/bfs.cpp:54-88)
 // ---------------------------------------------------------------------------
-__device__ void phase_to_dense(const DevGraph &g, const RunCtx &r, uint32_t step) {
+__device__ __forceinline__ void phase_to_dense(const DevGraph &g, const RunCtx &r, uint32_t step) {
 	const StepCounters *in = r.ctr + (step + 2) % 3;
 	const uint32_t cur = step & 1;
 	uint32_t n0 = ld_volatile(&in->tail[0]), n1 = ld_volatile(&in->tail[1]), n2 = ld_volatile(&in->tail[2]);
@@ -182,7 +299,7 @@ __device__ void phase_to_dense(const DevGraph &g, const RunCtx &r, uint32_t step
 // ---------------------------------------------------------------------------
 // Bitmap -> queue (to_sparse, apps/bfs_simd/bfs.cpp:400-465)
 // ---------------------------------------------------------------------------
-__device__ void phase_to_sparse(const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t step) {
+__device__ __forceinline__ void phase_to_sparse(const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t step) {
 	const uint32_t *bm = r.bm[(step + 2) % 3];
 	const uint32_t cur = step & 1;
 	StepCounters *slot = r.ctr + (step + 2) % 3;
@@ -222,95 +339,231 @@ __device__ void phase_to_sparse(const DevGraph &g, const RunCtx &r, const StepPa
 // apps/bfs_simd/bfs.cpp:91-388)
 // ---------------------------------------------------------------------------
 struct DenseShared {
-	uint32_t group, unsettled, nlist, pad;
+	uint32_t group, unsettled, nlist, stop;
 	uint32_t wcount[kWarps], woff[kWarps];
 	uint32_t prefix[kMaxSliceBatch + 1];
+	uint32_t seq;  // bulk-copy batches this CTA has consumed (keeps the mbarrier parities)
+	uint32_t fail; // a bulk-copy wait of this CTA ran out
 };
 
-__device__ void phase_dense(const DevGraph &g, const RunCtx &r, uint32_t step, uint32_t batch,
+// One bulk-copy stage: which stripes its entries belong to and where their
+// vectors start (entries are packed back to back in the stage buffer).
+struct TmaMeta {
+	uint32_t nent;
+	uint32_t kfirst;  // stripe of the first slice in the stage
+	uint32_t k[kMaxSliceBatch];
+	uint32_t pre[kMaxSliceBatch + 1];  // vector prefix; pre[nent] = vectors in the stage
+};
+
+struct DenseGroup {
+	uint64_t v0, v1;   // destination vertex range of the group
+	uint32_t gi, gw;   // group index, bitmap words
+};
+
+__device__ __shared__ DenseShared dsh;
+__device__ __shared__ TmaMeta tma_meta[kTmaStages];
+__device__ __shared__ alignas(8) uint64_t tma_bar[kTmaStages];    // stage filled
+__device__ __shared__ alignas(8) uint64_t tma_empty[kTmaStages];  // stage released by every consumer warp
+
+// Claims the next column group; loads its visited bits into vis_s and a copy
+// into nxt_s, and counts the vertices with an in-edge that are still unvisited.
+// Returns false when no group is left.  Uniform across the CTA.
+__device__ __forceinline__ bool dense_group_begin(const DevGraph &g, const RunCtx &r, StepCounters *out, uint32_t *vis_s,
+		uint32_t *nxt_s, DenseGroup &gr) {
+	__syncthreads();
+	if (threadIdx.x == 0) { dsh.group = atomicAdd(&out->work, 1u); dsh.unsettled = 0; dsh.stop = 0; }
+	__syncthreads();
+	gr.gi = dsh.group;
+	if (gr.gi >= g.num_groups) return false;
+	const uint32_t c0 = __ldg(g.group_col + gr.gi), c1 = __ldg(g.group_col + gr.gi + 1);
+	gr.v0 = (uint64_t) c0 * g.w;
+	gr.v1 = min((uint64_t) c1 * g.w, (uint64_t) g.n);
+	gr.gw = (uint32_t) ((gr.v1 - gr.v0 + 31) / 32);
+	uint32_t uns = 0;
+	for (uint32_t j = threadIdx.x; j < gr.gw; j += kThreads) {
+		uint32_t vb = bits_at(r.vis, gr.v0 + 32ull * j, gr.v1, kFull);
+		uint32_t hb = bits_at(g.hasin, gr.v0 + 32ull * j, gr.v1, 0u);
+		vis_s[j] = vb;
+		nxt_s[j] = vb;  // visited bits at the start: the new frontier is vis_s & ~nxt_s
+		uns += __popc(hb & ~vb);
+	}
+	if (threadIdx.x == 0) vis_s[gr.gw] = kFull;  // the slot padding words point at
+	uns = warp_sum(uns);
+	if (lane_id() == 0 && uns) atomicAdd(&dsh.unsettled, uns);
+	__syncthreads();
+	return true;
+}
+
+// Graph constants of the bottom-up step, held in registers.
+struct DenseRegs {
+	uint32_t vbits, cmask, vmask, w, ushift, dmask, sw;
+	int32_t *level;
+	uint32_t *parent;
+};
+
+__device__ __forceinline__ DenseRegs dense_regs(const DevGraph &g, const RunCtx &r) {
+	DenseRegs d;
+	d.vbits = g.vbits;
+	d.cmask = g.cmask;
+	d.vmask = g.vmask;
+	d.w = g.w;
+	d.ushift = g.ushift;
+	d.dmask = (g.vbits + g.cbits >= 32) ? 0xFFFFFFFFu : ((1u << (g.vbits + g.cbits)) - 1u);
+	d.sw = g.sw;
+	d.level = r.level;
+	d.parent = r.parent;
+	return d;
+}
+
+// The bottom-up test of one vector (four packed edge words) of a stage
+// (bfs_kernel_dense, apps/bfs_simd/bfs.cpp:194-217): an edge is a candidate
+// when its destination is not visited yet (a visited destination's scan is
+// over; padding words land on an always-visited slot) and its source is in
+// the stripe's frontier slice.  Both tests are done for all four words
+// without branches; only candidates, a few percent of the edges, take the
+// claiming branch, and a warp with no candidate skips it as a whole.  With
+// a power-of-two tile width the destination is the low bits of the word.
+// A claim sets the destination's bit in vis_s (the group's new frontier is
+// vis_s & ~vis0_s at publish time, where the levels are written) and stores
+// its parent.  Returns the number of destinations this thread claimed.
+// All 32 lanes of the warp must call it; `active` false lanes take part
+// without testing anything.
+template <bool kPow2W>
+__device__ __forceinline__ uint32_t dense_vec(bool active, const uint4 &x4, const DenseRegs &dr, uint32_t v0,
+		uint32_t *vis_s, uint32_t *nxt_s, const uint32_t *sl, uint32_t ubase, int32_t nl) {
+	const uint32_t e[4] = {x4.x, x4.y, x4.z, x4.w};
+	uint32_t d[4], ul[4], cand = 0;
+#pragma unroll
+	for (int q = 0; q < 4; ++q) {
+		d[q] = kPow2W ? (e[q] & dr.dmask) : ((e[q] >> dr.vbits) & dr.cmask) * dr.w + (e[q] & dr.vmask);
+		ul[q] = e[q] >> dr.ushift;
+		const uint32_t vw = vis_s[d[q] >> 5];
+		const uint32_t fw = sl[ul[q] >> 5];
+		cand |= (((~vw >> (d[q] & 31)) & (fw >> (ul[q] & 31))) & 1u) << q;
+	}
+	if (!active) cand = 0;
+	if (!__any_sync(kFull, cand)) return 0;
+	uint32_t claims = 0;
+#pragma unroll
+	for (int q = 0; q < 4; ++q) {
+		if ((cand >> q) & 1u) {
+			const uint32_t bit = 1u << (d[q] & 31);
+			if (!(atomicOr(&vis_s[d[q] >> 5], bit) & bit)) {
+				if (dr.parent) dr.parent[v0 + d[q]] = ubase + ul[q];
+				++claims;
+			}
+		}
+	}
+	return claims;
+}
+
+// Per-warp sum of claims, taken off the group's count of unsettled vertices.
+__device__ __forceinline__ void dense_settle(uint32_t claims) {
+	claims = warp_sum(claims);
+	if (lane_id() == 0 && claims) atomicSub(&dsh.unsettled, claims);
+}
+
+// Publishes the group's newly found vertices: next-frontier and visited bits,
+// and the "stripe has a frontier vertex" flags of the next step.  Counts them
+// and sums their out-degrees (for the direction switch) with coalesced reads
+// of the row offsets: a lane per vertex, four bitmap words per warp in flight.
+__device__ __forceinline__ void dense_group_publish(const DevGraph &g, const RunCtx &r, const DenseGroup &gr,
+		const uint32_t *vis_s, const uint32_t *vis0_s, int32_t nl, uint32_t *nxt, uint8_t *sf_nxt, ThreadAcc &acc) {
+	const unsigned lane = lane_id();
+	const uint32_t v0 = (uint32_t) gr.v0, sw = g.sw;
+	for (uint32_t j0 = warp_id() * 4; j0 < gr.gw; j0 += kWarps * 4) {
+		uint32_t bits[4], deg[4];
+#pragma unroll
+		for (int q = 0; q < 4; ++q) {
+			const uint32_t j = j0 + q;
+			bits[q] = (j < gr.gw) ? (vis_s[j] & ~vis0_s[j]) : 0u;
+			deg[q] = 0;
+			if ((bits[q] >> lane) & 1u) {
+				const uint32_t v = v0 + 32u * j + lane;
+				deg[q] = __ldg(g.row_off + v + 1) - __ldg(g.row_off + v);
+				r.level[v] = nl;
+				sf_nxt[v / sw] = 1;
+			}
+		}
+#pragma unroll
+		for (int q = 0; q < 4; ++q) {
+			acc.degsum += deg[q];
+			if (lane == 0 && bits[q]) {
+				const uint64_t vb = gr.v0 + 32ull * (j0 + q);
+				acc.count += __popc(bits[q]);
+				or_bits_at(nxt, vb, bits[q]);
+				or_bits_at(r.vis, vb, bits[q]);
+			}
+		}
+	}
+}
+
+// Lists the group's non-empty segments in the active stripes [kb, kb+kThreads)
+// in stripe order (the reference skips tiles whose row has no frontier vertex,
+// bfs.cpp:274-277; here the unit is the stripe).  Returns the count.
+__device__ __forceinline__ uint32_t dense_window(const DevGraph &g, const uint8_t *sf_cur, uint32_t gi, uint32_t kb,
+		uint32_t *list_k, uint32_t *list_start, uint32_t *list_nw) {
+	const unsigned tid = threadIdx.x, lane = lane_id(), wid = warp_id();
+	const uint32_t k = kb + tid;
+	bool act = false;
+	uint32_t st = 0, nw = 0;
+	if (k < g.num_stripes && ld_cg_u8(sf_cur + k)) {
+		uint64_t j = (uint64_t) gi * g.num_stripes + k;
+		st = __ldg(g.seg_off + j);
+		nw = __ldg(g.seg_off + j + 1) - st;
+		act = nw > 0;
+	}
+	unsigned bal = __ballot_sync(kFull, act);
+	if (lane == 0) dsh.wcount[wid] = __popc(bal);
+	__syncthreads();
+	if (wid == 0) {
+		uint32_t cnt = lane < kWarps ? dsh.wcount[lane] : 0u;
+		uint32_t inc = warp_incl_scan(cnt);
+		if (lane < kWarps) dsh.woff[lane] = inc - cnt;
+		if (lane == 31) dsh.nlist = inc;
+	}
+	__syncthreads();
+	if (act) {
+		uint32_t pos = dsh.woff[wid] + __popc(bal & lanemask_lt());
+		list_k[pos] = k;
+		list_start[pos] = st;
+		list_nw[pos] = nw;
+	}
+	__syncthreads();
+	return dsh.nlist;
+}
+
+// Generic bottom-up step: slices staged with plain loads (any tile width).
+__device__ __forceinline__ void phase_dense_generic(const DevGraph &g, const RunCtx &r, uint32_t step, uint32_t batch,
 		uint32_t *smem, ThreadAcc &acc) {
-	__shared__ DenseShared sh;
 	const uint32_t *cur = r.bm[(step + 2) % 3];
 	uint32_t *nxt = r.bm[step % 3];
 	const uint8_t *sf_cur = r.sf[(step + 2) % 3];
 	uint8_t *sf_nxt = r.sf[step % 3];
 	StepCounters *out = r.ctr + step % 3;
 	const int32_t nl = (int32_t) step + 1;
-	const unsigned tid = threadIdx.x, lane = lane_id(), wid = warp_id();
-
+	const unsigned tid = threadIdx.x;
 	uint32_t *vis_s = smem;
-	uint32_t *nxt_s = vis_s + g.max_group_words;
-	uint32_t *slices = nxt_s + g.max_group_words;
+	uint32_t *nxt_s = vis_s + g.max_group_words + 1;
+	uint32_t *slices = nxt_s + g.max_group_words + 1;
+	const DenseRegs dr = dense_regs(g, r);
 	uint32_t *list_k = slices + (size_t) batch * g.slice_words;
 	uint32_t *list_start = list_k + kThreads;
-	uint32_t *list_nvec = list_start + kThreads;
-
-	const uint32_t w = g.w, vbits = g.vbits, vmask = g.vmask, cmask = g.cmask, ushift = g.ushift;
-
-	for (;;) {
-		__syncthreads();
-		if (tid == 0) sh.group = atomicAdd(&out->work, 1u);
-		__syncthreads();
-		const uint32_t gi = sh.group;
-		if (gi >= g.num_groups) break;
-		const uint32_t c0 = __ldg(g.group_col + gi), c1 = __ldg(g.group_col + gi + 1);
-		const uint64_t v0 = (uint64_t) c0 * w;
-		const uint64_t v1 = min((uint64_t) c1 * w, (uint64_t) g.n);
-		const uint32_t gw = (uint32_t) ((v1 - v0 + 31) / 32);
-		if (tid == 0) sh.unsettled = 0;
-		__syncthreads();
-		uint32_t uns = 0;
-		for (uint32_t j = tid; j < gw; j += kThreads) {
-			uint32_t vb = bits_at(r.vis, v0 + 32ull * j, v1, kFull);
-			uint32_t hb = bits_at(g.hasin, v0 + 32ull * j, v1, 0u);
-			vis_s[j] = vb;
-			nxt_s[j] = 0;
-			uns += __popc(hb & ~vb);
-		}
-		uns = warp_sum(uns);
-		if (lane == 0 && uns) atomicAdd(&sh.unsettled, uns);
-		__syncthreads();
-		if (sh.unsettled == 0) continue;
+	uint32_t *list_nw = list_start + kThreads;
+	DenseGroup gr;
+	while (dense_group_begin(g, r, out, vis_s, nxt_s, gr)) {
+		if (dsh.unsettled == 0) continue;
 		if (tid == 0) acc.bu_groups++;
-
 		bool done = false;
 		for (uint32_t kb = 0; kb < g.num_stripes && !done; kb += kThreads) {
-			// Active, non-empty segments of this group in stripes [kb, kb+kThreads).
-			const uint32_t k = kb + tid;
-			bool act = false;
-			uint32_t st = 0, nvec = 0;
-			if (k < g.num_stripes && ld_cg_u8(sf_cur + k)) {
-				uint64_t j = (uint64_t) k * g.num_groups + gi;
-				st = __ldg(g.seg_off + j);
-				nvec = (__ldg(g.seg_off + j + 1) - st) >> 2;
-				act = nvec > 0;
-			}
-			unsigned bal = __ballot_sync(kFull, act);
-			if (lane == 0) sh.wcount[wid] = __popc(bal);
-			__syncthreads();
-			if (wid == 0) {
-				uint32_t cnt = lane < kWarps ? sh.wcount[lane] : 0u;
-				uint32_t inc = warp_incl_scan(cnt);
-				if (lane < kWarps) sh.woff[lane] = inc - cnt;
-				if (lane == 31) sh.nlist = inc;
-			}
-			__syncthreads();
-			if (act) {
-				uint32_t pos = sh.woff[wid] + __popc(bal & lanemask_lt());
-				list_k[pos] = k;
-				list_start[pos] = st;
-				list_nvec[pos] = nvec;
-			}
-			__syncthreads();
-			const uint32_t nlist = sh.nlist;
+			const uint32_t nlist = dense_window(g, sf_cur, gr.gi, kb, list_k, list_start, list_nw);
 			for (uint32_t b0 = 0; b0 < nlist; b0 += batch) {
 				const uint32_t nb = min(batch, nlist - b0);
 				if (tid == 0) {
 					uint32_t a = 0;
-					for (uint32_t j = 0; j < nb; ++j) { sh.prefix[j] = a; a += list_nvec[b0 + j]; }
-					sh.prefix[nb] = a;
+					for (uint32_t j = 0; j < nb; ++j) { dsh.prefix[j] = a; a += list_nw[b0 + j] >> 2; }
+					dsh.prefix[nb] = a;
 				}
-				// Stage the frontier slices of the nb stripes.
 				for (uint32_t x = tid; x < nb * g.slice_words; x += kThreads) {
 					uint32_t j = x / g.slice_words, wd = x - j * g.slice_words;
 					uint64_t sb = (uint64_t) list_k[b0 + j] * g.sw;
@@ -318,60 +571,233 @@ __device__ void phase_dense(const DevGraph &g, const RunCtx &r, uint32_t step, u
 					slices[x] = bits_at(cur, sb + 32ull * wd, se, 0u);
 				}
 				__syncthreads();
-				const uint32_t total = sh.prefix[nb];
-				for (uint32_t i = tid; i < total; i += kThreads) {
+				const uint32_t total = dsh.prefix[nb];
+				uint32_t claims = 0;
+				// warp-uniform trip count: lanes past the end take part inactive
+				for (uint32_t i0 = tid - lane_id(); i0 < total; i0 += kThreads) {
+					const uint32_t i = i0 + lane_id();
+					const bool act = i < total;
 					uint32_t j = 0;
-					while (j + 1 < nb && sh.prefix[j + 1] <= i) ++j;
+					while (act && j + 1 < nb && dsh.prefix[j + 1] <= i) ++j;
 					const uint32_t *sl = slices + j * g.slice_words;
 					const uint32_t kk = list_k[b0 + j];
-					uint4 x4 = ldg_v4(g.packed + list_start[b0 + j] + 4ull * (i - sh.prefix[j]));
-					uint32_t wv[4] = {x4.x, x4.y, x4.z, x4.w};
-#pragma unroll
-					for (int q = 0; q < 4; ++q) {
-						uint32_t e = wv[q];
-						if (e == kSentinelWord) continue;
-						uint32_t d = ((e >> vbits) & cmask) * w + (e & vmask);
-						uint32_t bit = 1u << (d & 31);
-						if (vis_s[d >> 5] & bit) continue;           // destination already found
-						uint32_t ul = e >> ushift;
-						if (!((sl[ul >> 5] >> (ul & 31)) & 1u)) continue; // source not in the frontier
-						if (atomicOr(&vis_s[d >> 5], bit) & bit) continue;
-						atomicOr(&nxt_s[d >> 5], bit);
-						uint32_t v = (uint32_t) (v0 + d);
-						r.level[v] = nl;
-						if (r.parent) r.parent[v] = kk * g.sw + ul;
-						uint32_t deg = __ldg(g.row_off + v + 1) - __ldg(g.row_off + v);
-						acc.count++;
-						acc.degsum += deg;
-						atomicSub(&sh.unsettled, 1u);
-					}
+					const uint4 x4 = act ? ldg_v4(g.packed + list_start[b0 + j] + 4ull * (i - dsh.prefix[j]))
+					                     : make_uint4(0, 0, 0, 0);
+					claims += dense_vec<false>(act, x4, dr, (uint32_t) gr.v0, vis_s, nxt_s, sl, kk * g.sw, nl);
 				}
+				dense_settle(claims);
 				if (tid == 0) { acc.bu_words += 4ull * total; acc.bu_slices += nb; }
 				__syncthreads();
-				if (sh.unsettled == 0) { done = true; break; }
+				if (dsh.unsettled == 0) { done = true; break; }
 			}
 		}
-		// Publish the group's new frontier and visited bits.
-		for (uint32_t j = tid; j < gw; j += kThreads) {
-			uint32_t bits = nxt_s[j];
-			if (!bits) continue;
-			uint64_t vb = v0 + 32ull * j;
-			or_bits_at(nxt, vb, bits);
-			or_bits_at(r.vis, vb, bits);
-			uint64_t kf = (vb + (__ffs(bits) - 1)) / g.sw, kl = (vb + (31 - __clz(bits))) / g.sw;
-			for (uint64_t k = kf; k <= kl; ++k) sf_nxt[k] = 1;
-		}
+		dense_group_publish(g, r, gr, vis_s, nxt_s, nl, nxt, sf_nxt, acc);
 	}
+}
+
+// Producer side of the bulk-copy pipeline (lane 0 of warp 0): fills stage
+// `st` with the next run of the window's segments -- consecutive list
+// entries whose words are contiguous (group-major layout), spanning at most
+// tma_batch stripes and kTmaEdgeWords words -- with ONE bulk copy for the
+// edges and ONE for the frontier slices of stripes k_first..k_last, and arms
+// the stage's "full" mbarrier with the exact byte count.  A stage with
+// nent == 0 marks the end of the window.
+struct TmaCursor {
+	uint32_t li, lo;   // list entry and word offset inside it
+};
+
+__device__ __forceinline__ bool tma_issue(const DevGraph &g, const uint32_t *cur, uint32_t *smem_stages, uint32_t st,
+		const uint32_t *list_k, const uint32_t *list_start, const uint32_t *list_nw, uint32_t nlist,
+		TmaCursor &c, bool stop, ThreadAcc &acc) {
+	const uint32_t stage_words = kTmaEdgeWords + g.tma_batch * g.slice_words;
+	uint32_t *edges = smem_stages + (size_t) st * stage_words;
+	uint32_t *slices = edges + kTmaEdgeWords;
+	TmaMeta &mt = tma_meta[st];
+	uint32_t nent = 0, used = 0;
+	uint32_t src = 0, kfirst = 0, next_word = 0;
+	while (!stop && nent < kMaxSliceBatch && c.li < nlist && used < kTmaEdgeWords) {
+		const uint32_t k = list_k[c.li];
+		const uint32_t w0 = list_start[c.li] + c.lo;
+		if (nent == 0) {
+			src = w0;
+			kfirst = k;
+		} else if (w0 != next_word || k - kfirst >= g.tma_batch) {
+			break;  // not contiguous with the run, or its slice does not fit
+		}
+		const uint32_t take = min(list_nw[c.li] - c.lo, kTmaEdgeWords - used);
+		mt.k[nent] = k;
+		mt.pre[nent] = used >> 2;
+		++nent;
+		used += take;
+		next_word = w0 + take;
+		c.lo += take;
+		if (c.lo == list_nw[c.li]) { c.li++; c.lo = 0; }
+	}
+	mt.nent = nent;
+	mt.pre[nent] = used >> 2;
+	mt.kfirst = kfirst;
+	const uint32_t nslices = nent ? mt.k[nent - 1] - kfirst + 1 : 0;
+	acc.bu_words += used;
+	acc.bu_slices += nslices;
+	mbar_arrive_expect_tx(&tma_bar[st], 4u * (used + nslices * g.slice_words));
+	if (nent) {
+		bulk_copy_g2s(edges, g.packed + src, 4u * used, &tma_bar[st]);
+		bulk_copy_g2s(slices, cur + (size_t) kfirst * g.slice_words, 4u * nslices * g.slice_words, &tma_bar[st]);
+	}
+	return nent != 0;
+}
+
+__device__ void dense_tma_init() {
+	if (threadIdx.x == 0) {
+		for (uint32_t s = 0; s < kTmaStages; ++s) {
+			mbar_init(&tma_bar[s], 1);
+			mbar_init(&tma_empty[s], kWarps - 1);
+		}
+		dsh.seq = 0;
+		dsh.fail = 0;
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncthreads();
+}
+
+// Bottom-up step streaming each group's segments and the stripes' frontier
+// slices into a ring of shared-memory stages with 1-D bulk copies (TMA).
+// Warp 0 is the producer; warps 1.. consume: they wait on a stage's "full"
+// barrier, test its edges and release the stage on its "empty" barrier, so
+// no CTA-wide barrier separates batches.  Needs S*W to be a multiple of 128
+// so that every slice starts on a 16-byte boundary.
+__device__ __forceinline__ void phase_dense_tma(const DevGraph &g, const RunCtx &r, uint32_t step, uint32_t *smem, ThreadAcc &acc) {
+	const uint32_t *cur = r.bm[(step + 2) % 3];
+	uint32_t *nxt = r.bm[step % 3];
+	const uint8_t *sf_cur = r.sf[(step + 2) % 3];
+	uint8_t *sf_nxt = r.sf[step % 3];
+	StepCounters *out = r.ctr + step % 3;
+	const int32_t nl = (int32_t) step + 1;
+	const unsigned tid = threadIdx.x, wid = warp_id(), lane = lane_id();
+	const uint32_t stage_words = kTmaEdgeWords + g.tma_batch * g.slice_words;
+	uint32_t *stages = smem;
+	uint32_t *vis_s = stages + (size_t) kTmaStages * stage_words;
+	uint32_t *nxt_s = vis_s + g.max_group_words + 1;
+	uint32_t *list_k = nxt_s + g.max_group_words + 1;
+	const DenseRegs dr = dense_regs(g, r);
+	const bool pow2w = (g.w & (g.w - 1)) == 0;
+	const uint32_t slice_words = g.slice_words;
+	uint32_t *list_start = list_k + kThreads;
+	uint32_t *list_nw = list_start + kThreads;
+	constexpr uint32_t kConsumers = kThreads - 32;
+	// The frontier bitmap was written by other CTAs through the generic
+	// proxy; order those writes before this CTA's bulk copies read it.
+	if (tid == 0) fence_proxy_async_global();
+	DenseGroup gr;
+	unsigned long long cyc[6] = {0, 0, 0, 0, 0, 0};
+	long long t0 = clock64();
+	while (dense_group_begin(g, r, out, vis_s, nxt_s, gr)) {
+		{ long long t1 = clock64(); cyc[0] += t1 - t0; t0 = t1; }
+		const uint32_t v0 = (uint32_t) gr.v0;
+		if (dsh.unsettled == 0) continue;
+		if (tid == 0) acc.bu_groups++;
+		for (uint32_t kb = 0; kb < g.num_stripes; kb += kThreads) {
+			if (dsh.unsettled == 0 || dsh.fail) break;
+			const uint32_t seq0 = dsh.seq;  // read before the barriers inside dense_window
+			const uint32_t nlist = dense_window(g, sf_cur, gr.gi, kb, list_k, list_start, list_nw);
+			{ long long t1 = clock64(); cyc[1] += t1 - t0; t0 = t1; }
+			if (nlist == 0) continue;
+			if (wid == 0) {
+				if (lane == 0) {
+					TmaCursor c{0, 0};
+					for (uint32_t t = seq0;; ++t) {
+						const uint32_t st = t % kTmaStages;
+						const long long w0 = clock64();
+						if (t >= kTmaStages &&
+								!mbar_wait_bounded(&tma_empty[st], ((t / kTmaStages) + 1) & 1u, r.err, 4000)) {
+							dsh.fail = 1;
+							break;
+						}
+						cyc[4] += clock64() - w0;
+						fence_proxy_async_shared();
+						const bool stop = *(volatile uint32_t *) &dsh.unsettled == 0;
+						if (!tma_issue(g, cur, stages, st, list_k, list_start, list_nw, nlist, c, stop, acc)) {
+							dsh.seq = t + 1;
+							break;
+						}
+					}
+				}
+			} else {
+				const uint32_t ct = tid - 32;
+				for (uint32_t t = seq0;; ++t) {
+					const uint32_t st = t % kTmaStages;
+					const long long w0 = clock64();
+					if (!mbar_wait_bounded(&tma_bar[st], (t / kTmaStages) & 1u, r.err)) {
+						dsh.fail = 1;
+						break;
+					}
+					const long long w1 = clock64();
+					cyc[2] += w1 - w0;
+					const TmaMeta &mt = tma_meta[st];
+					const uint32_t nent = mt.nent;
+					uint32_t claims = 0;
+					const uint4 *edges4 = (const uint4 *) (stages + (size_t) st * stage_words);
+					const uint32_t *slices = stages + (size_t) st * stage_words + kTmaEdgeWords;
+					// Warp cw takes chunks of 32 consecutive vectors (one per lane);
+					// a lane finds its entry (stripe) with a branch-free search over
+					// the stage's few entries -- the lanes of a chunk mostly read the
+					// same prefix words, which shared memory broadcasts.
+					const uint32_t total = mt.pre[nent];
+					const uint32_t cw = wid - 1;
+					for (uint32_t c0 = cw * 32; c0 < total; c0 += (kWarps - 1) * 32) {
+						const uint32_t i = c0 + lane;
+						const bool act = i < total;
+						uint32_t j = 0;
+#pragma unroll
+						for (uint32_t sp = kMaxSliceBatch / 2; sp >= 1; sp >>= 1)
+							j += (j + sp < nent && mt.pre[j + sp] <= i) ? sp : 0u;
+						const uint32_t kk = mt.k[j];
+						const uint32_t *sl = slices + (size_t) (kk - mt.kfirst) * slice_words;
+						const uint4 x4 = edges4[act ? i : 0];
+						if (pow2w) claims += dense_vec<true>(act, x4, dr, v0, vis_s, nxt_s, sl, kk * dr.sw, nl);
+						else claims += dense_vec<false>(act, x4, dr, v0, vis_s, nxt_s, sl, kk * dr.sw, nl);
+					}
+					dense_settle(claims);
+					__syncwarp();
+					cyc[3] += clock64() - w1;
+					if (lane == 0) mbar_arrive(&tma_empty[st]);
+					if (nent == 0) break;
+				}
+			}
+			__syncthreads();
+			t0 = clock64();
+		}
+		if (dsh.fail) break;
+		dense_group_publish(g, r, gr, vis_s, nxt_s, nl, nxt, sf_nxt, acc);
+		{ long long t1 = clock64(); cyc[5] += t1 - t0; t0 = t1; }
+	}
+	// thread 0 reports setup/window/publish and producer wait, warp 1 lane 0 the consumer side
+	if (tid == 0) {
+		atomicAdd(&r.stats->bu_cycles[0], cyc[0]);
+		atomicAdd(&r.stats->bu_cycles[1], cyc[1]);
+		atomicAdd(&r.stats->bu_cycles[4], cyc[4]);
+		atomicAdd(&r.stats->bu_cycles[5], cyc[5]);
+	}
+	if (tid == 32) {
+		atomicAdd(&r.stats->bu_cycles[2], cyc[2]);
+		atomicAdd(&r.stats->bu_cycles[3], cyc[3]);
+	}
+}
+
+__device__ __forceinline__ void phase_dense(const DevGraph &g, const RunCtx &r, uint32_t step, uint32_t batch,
+		uint32_t *smem, ThreadAcc &acc) {
+	if (g.tma) phase_dense_tma(g, r, step, smem, acc);
+	else phase_dense_generic(g, r, step, batch, smem, acc);
 }
 
 // ---------------------------------------------------------------------------
 // Step bookkeeping
 // ---------------------------------------------------------------------------
-__device__ void clear_slot(const DevGraph &g, const RunCtx &r, uint32_t slot) {
+__device__ __forceinline__ void clear_slot(const DevGraph &g, const RunCtx &r, uint32_t slot) {
 	uint32_t *bm = r.bm[slot];
 	uint8_t *sf = r.sf[slot];
 	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
-	for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < g.nwords; i += stride) bm[i] = 0;
+	for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < g.bm_words; i += stride) bm[i] = 0;
 	for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < g.num_stripes; i += stride) sf[i] = 0;
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		StepCounters *c = r.ctr + slot;
@@ -383,7 +809,7 @@ __device__ void clear_slot(const DevGraph &g, const RunCtx &r, uint32_t slot) {
 }
 
 // Adds the CTA's accumulated counts to the step slot and the run statistics.
-__device__ void flush_acc(ThreadAcc &acc, StepCounters *slot, DevStats *stats) {
+__device__ __forceinline__ void flush_acc(ThreadAcc &acc, StepCounters *slot, DevStats *stats) {
 	__shared__ unsigned long long red[7][kWarps];
 	unsigned long long v[7] = {acc.count, acc.degsum, acc.td_edges, acc.td_vertices, acc.bu_words, acc.bu_slices, acc.bu_groups};
 	const unsigned lane = lane_id(), wid = warp_id();
@@ -436,8 +862,8 @@ __global__ void __launch_bounds__(kThreads) k_init(DevGraph g, RunCtx r) {
 		r.level[i] = -1;
 		if (r.parent) r.parent[i] = kUnvisitedWord;
 	}
-	for (uint64_t i = t0; i < g.nwords; i += stride) {
-		r.vis[i] = 0;
+	for (uint64_t i = t0; i < g.nwords; i += stride) r.vis[i] = 0;
+	for (uint64_t i = t0; i < g.bm_words; i += stride) {
 		r.bm[0][i] = 0;
 		r.bm[1][i] = 0;
 		r.bm[2][i] = 0;
@@ -454,9 +880,10 @@ __global__ void k_seed(DevGraph g, RunCtx r, StepParams p) {
 }
 
 __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunCtx r, StepParams p, uint32_t batch) {
-	extern __shared__ uint32_t smem[];
+	extern __shared__ __align__(128) uint32_t smem[];
 	ThreadAcc acc{0, 0, 0, 0, 0, 0, 0};
 	bool ok = true;
+	dense_tma_init();
 	if (blockIdx.x == 0 && threadIdx.x == 0) seed_source(g, r, p);
 	ok = grid_barrier(r.bar, r.err);
 	bool last_dense = false;
@@ -468,6 +895,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 		if (blockIdx.x == 0 && threadIdx.x == 0) {
 			r.stats->reached += fsize;
 			r.stats->edges_traversed += dsum;
+			if (step < 257) r.stats->t_step[step] = global_timer_ns();
 		}
 		if (fsize == 0) break;
 		bool dense = false;
@@ -480,12 +908,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 			if (!last_dense) {
 				phase_to_dense(g, r, step);
 				if (!(ok = grid_barrier(r.bar, r.err))) break;
+				if (blockIdx.x == 0 && threadIdx.x == 0 && step < 256) r.stats->t_conv[step] = global_timer_ns();
 			}
 			phase_dense(g, r, step, batch, smem, acc);
 		} else {
 			if (last_dense) {
 				phase_to_sparse(g, r, p, step);
 				if (!(ok = grid_barrier(r.bar, r.err))) break;
+				if (blockIdx.x == 0 && threadIdx.x == 0 && step < 256) r.stats->t_conv[step] = global_timer_ns();
 			}
 			phase_expand(g, r, p, step, acc);
 		}
@@ -519,8 +949,9 @@ __global__ void __launch_bounds__(kThreads) k_step_expand(DevGraph g, RunCtx r, 
 	flush_acc(acc, r.ctr + step % 3, r.stats);
 }
 __global__ void __launch_bounds__(kThreads, 2) k_step_dense(DevGraph g, RunCtx r, uint32_t step, uint32_t batch) {
-	extern __shared__ uint32_t smem[];
+	extern __shared__ __align__(128) uint32_t smem[];
 	ThreadAcc acc{0, 0, 0, 0, 0, 0, 0};
+	dense_tma_init();
 	phase_dense(g, r, step, batch, smem, acc);
 	flush_acc(acc, r.ctr + step % 3, r.stats);
 }
@@ -529,7 +960,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_dense(DevGraph g, RunCtx r
 // Host-side launchers
 // ---------------------------------------------------------------------------
 size_t dense_smem_bytes(const DevGraph &g, uint32_t batch) {
-	return sizeof(uint32_t) * ((size_t) 2 * g.max_group_words + (size_t) batch * g.slice_words + 3 * kThreads);
+	size_t words = (size_t) 2 * (g.max_group_words + 1) + 3 * kThreads;
+	if (g.tma) words += (size_t) kTmaStages * (kTmaEdgeWords + (size_t) g.tma_batch * g.slice_words);
+	else words += (size_t) batch * g.slice_words;
+	return sizeof(uint32_t) * words;
 }
 
 int persistent_grid(const DevGraph &g, uint32_t batch, int num_sms, int *grid, size_t *smem) {

@@ -102,7 +102,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
 					ok = 0;
 					break;
 				}
-				__nanosleep(32);
+				__nanosleep(it < 64 ? 32 : 256);
 			}
 		}
 		__threadfence();
@@ -112,6 +112,57 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
 	__syncthreads();
 	return s_ok != 0;
 }
+
+// ---- shared-memory barriers and 1-D bulk copies (TMA) ---------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+	return (uint32_t) __cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+	asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+			::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+	asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+			"selp.u32 %0, 1, 0, p;\n\t}"
+			: "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+	return ok != 0;
+}
+// The same test with a suspend-time hint: the thread sleeps until the phase
+// completes or `hint_ns` passes, instead of spinning and taking issue slots
+// from the warps that do the work.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity, uint32_t hint_ns) {
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+			"selp.u32 %0, 1, 0, p;\n\t}"
+			: "=r"(ok) : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns) : "memory");
+	return ok != 0;
+}
+// Waits for the phase with the given parity; gives up (returning false and
+// recording BFS_ETIMEOUT) after the wait limit.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *err, uint32_t hint_ns = 1000) {
+	if (mbar_try_wait(bar, parity)) return true;
+	uint64_t t0 = global_timer_ns();
+	for (uint32_t it = 0; it < kWaitLimitIters; ++it) {
+		if (mbar_try_wait_sleep(bar, parity, hint_ns)) return true;
+		if (global_timer_ns() - t0 > kWaitLimitNs) break;
+	}
+	atomicExch(err, 6 /* BFS_ETIMEOUT */);
+	return false;
+}
+// Global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+			::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
 // Warp-wide inclusive scan of a 32-bit value.
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {

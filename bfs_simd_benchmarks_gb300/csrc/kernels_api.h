@@ -14,6 +14,11 @@ constexpr uint32_t kSentinelWord = 0xFFFFFFFFu;
 constexpr uint32_t kUnvisitedWord = 0xFFFFFFFFu;
 constexpr uint32_t kMaxSliceBatch = 16;   // frontier slices staged together by the bottom-up step
 constexpr uint32_t kSliceBudgetWords = 8192;
+// Bulk-copy pipeline of the bottom-up step: stages per CTA, packed words per
+// stage and the shared-memory budget of the frontier slices of one stage.
+constexpr uint32_t kTmaStages = 3;
+constexpr uint32_t kTmaEdgeWords = 4096;
+constexpr uint32_t kTmaSliceWords = 4096;
 
 enum StepKind { kStepSeed = 0, kStepClear, kStepToDense, kStepToSparse, kStepExpand, kStepDense };
 

@@ -17,16 +17,18 @@
 //   Tile columns are cut into column groups (runs of whole columns with about
 //   equal edge counts).  For stripe k and group g the edges of the group's
 //   columns inside stripe k are one contiguous run of the column-major order;
-//   each becomes one segment, padded with 0xFFFFFFFF words to a multiple of
+//   each becomes one segment, padded with dummy words to a multiple of
 //   four words so that every segment starts on a 16-byte boundary (the TMA
-//   rule).  Segments are stored stripe-major: seg_off[k*G + g].
+//   rule).  Segments are stored group-major, seg_off[g*num_stripes + k], so
+//   that a group's segments of consecutive stripes are one contiguous range
+//   and a single bulk copy moves several of them.
 //   An edge u->v of stripe k, column c of group g is one 32-bit word:
 //       bits [0, vbits)            v - c*W          (destination inside its column)
 //       bits [vbits, vbits+cbits)  c - group_col[g] (column inside the group)
 //       bits [vbits+cbits, 32)     u - k*S*W        (source inside the stripe)
 //   vbits = ceil(log2 W), ubits = ceil(log2 (S*W)), cbits = 32 - vbits - ubits.
-//   A group spans at most 2^cbits - 1 columns, so no edge word equals the
-//   padding word.
+//   Padding words name a dummy destination just past the group's vertices
+//   (see pack_tiles), which the kernel treats as already visited.
 #include <algorithm>
 #include <atomic>
 #include <cstring>
@@ -162,7 +164,12 @@ int pack_tiles(const HostGraph &g, uint32_t target_groups, uint32_t max_group_ve
 	out.ubits = ceil_log2((uint64_t) s * w);
 	if (out.vbits + out.ubits > 31) return BFS_EUNSUPPORTED;
 	out.cbits = std::min<uint32_t>(32 - out.vbits - out.ubits, 16);  // keeps every shift below 32
-	uint64_t max_cols = (1ull << out.cbits) - 1;
+	// A group spans at most cmask - ceil(32/W) columns so that the padding
+	// word of any group can still name the group's dummy slot (below).
+	const uint64_t cmask = (1ull << out.cbits) - 1;
+	const uint64_t pad_cols = (32 + w - 1) / w;
+	if (cmask < pad_cols + 1) return BFS_EUNSUPPORTED;
+	uint64_t max_cols = cmask - pad_cols;
 	if (max_cols > 0xFFFF) max_cols = 0xFFFF;
 	uint64_t cols_by_smem = std::max<uint64_t>(1, max_group_vertices / w);
 	if (w > max_group_vertices) return BFS_EUNSUPPORTED;
@@ -209,7 +216,7 @@ int pack_tiles(const HostGraph &g, uint32_t target_groups, uint32_t max_group_ve
 	std::vector<uint64_t> seg_count(nseg, 0);
 	for (uint64_t i = 0; i < g.m; ++i) {
 		uint32_t k = g.heads[i] / w / s;
-		seg_count[(uint64_t) k * out.num_groups + group_of[g.tails[i] / w]]++;
+		seg_count[(uint64_t) group_of[g.tails[i] / w] * stripes + k]++;
 	}
 	out.seg_off.assign(nseg + 1, 0);
 	uint64_t words = 0;
@@ -219,7 +226,21 @@ int pack_tiles(const HostGraph &g, uint32_t target_groups, uint32_t max_group_ve
 		if (words > 0xFFFFFFF0ull) return BFS_EUNSUPPORTED;
 	}
 	out.seg_off[nseg] = (uint32_t) words;
-	out.words.assign(words, kSentinel);
+	out.words.assign(words, 0);
+	// Padding words decode to destination 32*ceil(group_vertices/32): the slot
+	// right after the group's bitmap, which the kernel keeps "visited", so a
+	// padding word is skipped by the ordinary visited test.
+	std::vector<uint32_t> pad_word(out.num_groups);
+	for (uint32_t gi = 0; gi < out.num_groups; ++gi) {
+		uint64_t v0 = (uint64_t) out.group_col[gi] * w;
+		uint64_t v1 = std::min<uint64_t>((uint64_t) out.group_col[gi + 1] * w, g.n);
+		uint64_t d = (v1 - v0 + 31) / 32 * 32;
+		pad_word[gi] = (uint32_t) (d % w) | (uint32_t) ((d / w) << out.vbits);
+	}
+	for (uint64_t j = 0; j < nseg; ++j) {
+		uint32_t gi = (uint32_t) (j / stripes);
+		for (uint64_t x = out.seg_off[j] + seg_count[j]; x < out.seg_off[j + 1]; ++x) out.words[x] = pad_word[gi];
+	}
 
 	// Fill in file order: each edge goes to the next slot of its segment.
 	std::vector<uint64_t> fill(out.seg_off.begin(), out.seg_off.end() - 1);
@@ -227,7 +248,7 @@ int pack_tiles(const HostGraph &g, uint32_t target_groups, uint32_t max_group_ve
 	for (uint64_t i = 0; i < g.m; ++i) {
 		uint32_t u = g.heads[i], v = g.tails[i];
 		uint32_t k = u / w / s, c = v / w, gi = group_of[c];
-		uint64_t j = (uint64_t) k * out.num_groups + gi;
+		uint64_t j = (uint64_t) gi * stripes + k;
 		uint32_t word = (v - c * w) | ((c - out.group_col[gi]) << cshift) | ((u - k * s * w) << ushift);
 		out.words[fill[j]++] = word;
 	}

@@ -150,6 +150,14 @@ typedef struct bfs_stats {
 	int32_t status;            /* device-side status of the run (BFS_OK or BFS_ETIMEOUT) */
 	uint32_t grid_ctas;        /* CTAs of the persistent launch */
 	uint8_t trace[BFS_TRACE_MAX]; /* trace[i] = 1 if step i was dense (first BFS_TRACE_MAX steps) */
+	/* Phase timers, the counterpart of the reference's dense_time, to_dense_time,
+	 * sparse_time and to_sparse_time (apps/bfs_simd/bfs.cpp:733-751), taken on the
+	 * device between grid barriers (persistent mode only; 0 otherwise). */
+	double dense_ms, to_dense_ms, sparse_ms, to_sparse_ms;
+	float step_ms[BFS_TRACE_MAX]; /* duration of each step, conversion included */
+	/* Bottom-up step profile: SM cycles summed over CTAs spent in group setup,
+	 * segment lists, consumer wait, consumer work, producer wait and publish. */
+	uint64_t bu_cycles[8];
 } bfs_stats;
 
 /*
