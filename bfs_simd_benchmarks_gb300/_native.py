@@ -133,6 +133,7 @@ _SIGNATURES = [
     ("bfs_run", C.c_int, [C.c_void_p, C.c_uint32, _i32p, _u32p, C.POINTER(Stats)]),
     ("bfs_run_device", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("bfs_last_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    ("bfs_run_noalloc", C.c_int, [C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("bfs_write_level_dump", C.c_int, [C.c_char_p, C.c_uint32, _i32p]),
     ("bfs_tool_csr_tiling", C.c_int, [C.c_char_p, C.c_uint32]),
     ("bfs_tool_coo_tiling", C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, C.c_uint32]),

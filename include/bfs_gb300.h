@@ -177,6 +177,31 @@ int bfs_run(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, b
 int bfs_run_device(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, void *stream);
 int bfs_last_stats(bfs_graph *g, bfs_stats *stats);
 
+/* ---- allocation-free traversal (no counterpart in the reference) -------- */
+#define BFS_NOALLOC_MAX_VERTICES (1u << 20)
+
+/*
+ * Top-down BFS from `source` over a CSR the caller already holds in device
+ * memory (row_offsets[num_vertices+1], columns[row_offsets[num_vertices]],
+ * 0-based), writing int32 levels (-1 unreached) into the caller's device
+ * buffer levels[num_vertices] on `stream` (a cudaStream_t, NULL for the
+ * default stream).  If `status` (a device int) is not NULL it receives
+ * BFS_OK or BFS_ETIMEOUT when the traversal ends.  Asynchronous.
+ *
+ * This entry point allocates nothing, for callers that cannot call
+ * cudaMalloc: plug-ins whose host framework reserves the device memory and
+ * hands none out, or request paths that cannot take the device-wide
+ * synchronisation and unbounded latency of cudaMalloc / cudaFree.  Its
+ * scratch is a fixed file-scope device array of about 8.1 MB per device,
+ * sized for at most BFS_NOALLOC_MAX_VERTICES vertices (more returns
+ * BFS_EUNSUPPORTED), held until the process exits and shared by every call
+ * on that device: calls that overlap on the GPU race, so serialise them.
+ * The first call on a device does a one-time set-up (it looks up the
+ * scratch array's device address); make that call before any stream capture.
+ */
+int bfs_run_noalloc(uint32_t num_vertices, const uint32_t *row_offsets, const uint32_t *columns,
+		uint32_t source, int32_t *levels, int32_t *status, void *stream);
+
 /* ---- level dump --------------------------------------------------------- */
 /* Writes <dir>/path<t>.txt, t = 0..63, "<v>) cost:<level>\n", floor(N/64)
  * vertices per file, the last taking the rest: the ONEDEBUG dump of
