@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", default="pokec")
     ap.add_argument("--mode", choices=["persistent", "stepwise"], default="persistent")
+    ap.add_argument("--bottom-up", choices=["pull", "stream"], default="pull")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sources", type=int, default=0, help="use only the first K sources (profiling runs)")
@@ -123,16 +124,20 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def algorithmic_bytes(st: dict, n: int, sw: int) -> int:
+def algorithmic_bytes(st: dict, n: int, sw: int, pull: bool) -> int:
     """Bytes a traversal must move at minimum, from its device counters.
 
-    4 B per CSR edge read top-down, 12 B per frontier vertex expanded top-down
-    (queue entry + two row offsets), 4 B per packed tile word streamed
-    bottom-up, S*W/8 B per staged frontier slice, 8 B per reached vertex
-    (level + parent store), the initialisation of levels and parents (8 B per
-    vertex) and two N/8-byte bitmap passes per step.
+    Top-down: 4 B per CSR edge read, 12 B per frontier vertex expanded (queue
+    entry + two row offsets).  Bottom-up, pull: 8 B per in-edge read (its
+    source id + the frontier word tested), 8 B per destination tested (two
+    in-list offsets) and 2 N/8-byte bitmap reads per step (visited, has-in);
+    stream: 4 B per packed tile word and S*W/8 B per frontier slice staged.
+    Always: 8 B per reached vertex (level + parent), 8 B per vertex of
+    initialisation, two N/8-byte bitmap passes per step.
     """
-    return (4 * st["td_edges"] + 12 * st["td_vertices"] + 4 * st["bu_words"] + (sw // 8) * st["bu_slices"]
+    bu = (8 * st["bu_words"] + 8 * st["bu_vertices"] + st["dense_steps"] * 2 * ((n + 7) // 8)) if pull else \
+        (4 * st["bu_words"] + (sw // 8) * st["bu_slices"])
+    return (4 * st["td_edges"] + 12 * st["td_vertices"] + bu
             + 8 * st["reached"] + 8 * n + st["num_steps"] * 2 * ((n + 7) // 8))
 
 
@@ -229,7 +234,7 @@ def main():
     t_gen = time.perf_counter()
     src, dst = wl.edges()
     g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s)
-    g.set_options(mode=args.mode)
+    g.set_options(mode=args.mode, bottom_up=args.bottom_up)
     info = g.info()
     t_gen = time.perf_counter() - t_gen
     degrees = g.degrees()
@@ -290,7 +295,7 @@ def main():
     value = edges_all / (total_ms_max / 1e3) / 1e9
 
     # roofline of the traversal kernel (k_bfs_persistent), per launch
-    alg = [algorithmic_bytes(st, n, sw) for _, _, st in timed]
+    alg = [algorithmic_bytes(st, n, sw, args.bottom_up == "pull") for _, _, st in timed]
     achieved = statistics.mean(alg) / (statistics.mean(kern_ms) / 1e3) / 1e9
     peak, peak_kind = peaks()
     traffic = ncu_traffic(args.workload)
@@ -329,6 +334,7 @@ def main():
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded R-MAT stand-in, see config)",
             "config": dict(wl.describe(), step=f"{len(sources)} single-source traversals",
                            parallelism="replicas" if world > 1 else "single GPU", mode=args.mode,
+                           bottom_up=args.bottom_up,
                            l2="flushed (256 MiB write) before every traversal; graph 245 MB > L2",
                            grid_ctas=timed[0][2]["grid_ctas"], column_groups=info["num_groups"],
                            graph_build_s=round(t_gen, 2)),

@@ -29,6 +29,9 @@ BFS_LOAD_HOST_ONLY = 0x4
 BFS_MODE_PERSISTENT = 0
 BFS_MODE_STEPWISE = 1
 
+BFS_BU_PULL = 0
+BFS_BU_STREAM = 1
+
 BFS_RMAT_NO_SELF_LOOPS = 0x1
 BFS_RMAT_DEDUP = 0x2
 BFS_RMAT_PERMUTE = 0x4
@@ -64,7 +67,8 @@ class Options(C.Structure):
         ("to_sparse_ratio", C.c_uint32),
         ("warp_max_degree", C.c_uint32),
         ("cta_max_degree", C.c_uint32),
-        ("reserved", C.c_uint32 * 3),
+        ("bottom_up", C.c_uint32),
+        ("reserved", C.c_uint32 * 2),
     ]
 
 
@@ -80,6 +84,7 @@ class Stats(C.Structure):
         ("bu_words", C.c_uint64),
         ("bu_slices", C.c_uint64),
         ("bu_groups", C.c_uint64),
+        ("bu_vertices", C.c_uint64),
         ("device_ms", C.c_double),
         ("kernel_ms", C.c_double),
         ("status", C.c_int32),

@@ -48,7 +48,7 @@ struct bfs_graph {
 	int32_t *level_buf = nullptr;    // internal outputs for bfs_run
 	uint32_t *parent_buf = nullptr;
 	DevStats *h_stats = nullptr;     // pinned
-	StepCounters *h_ctr = nullptr;   // pinned (stepwise mode)
+	unsigned long long *h_part = nullptr;  // pinned (stepwise mode): one slot's per-CTA partials
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
 	cudaStream_t last_stream = nullptr;
 	bool stats_fresh = false;
@@ -92,12 +92,12 @@ void release(bfs_graph *g) {
 	for (auto &b : g->bufs) cudaFree(b.p);
 	g->bufs.clear();
 	if (g->h_stats) cudaFreeHost(g->h_stats);
-	if (g->h_ctr) cudaFreeHost(g->h_ctr);
+	if (g->h_part) cudaFreeHost(g->h_part);
 	if (g->ev0) cudaEventDestroy(g->ev0);
 	if (g->ev1) cudaEventDestroy(g->ev1);
 	if (g->evm) cudaEventDestroy(g->evm);
 	g->h_stats = nullptr;
-	g->h_ctr = nullptr;
+	g->h_part = nullptr;
 	g->ev0 = g->ev1 = g->evm = nullptr;
 }
 
@@ -108,6 +108,7 @@ void default_options(bfs_options *o) {
 	o->to_sparse_ratio = 20;
 	o->warp_max_degree = 32;
 	o->cta_max_degree = 4096;
+	o->bottom_up = BFS_BU_PULL;
 }
 
 // Builds the device copy of a validated host graph.
@@ -162,12 +163,25 @@ int upload(bfs_graph *g, HostGraph &h) {
 	d.bm_words = d.num_stripes * d.slice_words;  // bulk copies read whole slices
 	d.tma = (d.sw % 128 == 0) ? 1u : 0u;
 	d.tma_batch = std::max<uint32_t>(1, std::min<uint32_t>(kMaxSliceBatch, kTmaSliceWords / d.slice_words));
+	d.pull_long_cap = 4096;
 	if ((st = dev_upload(g, &d.row_off, h.row_off))) return st;
 	if ((st = dev_upload(g, &d.col, h.csr_dst))) return st;
 	if ((st = dev_upload(g, &d.packed, pk.words))) return st;
 	if ((st = dev_upload(g, &d.seg_off, pk.seg_off))) return st;
 	if ((st = dev_upload(g, &d.group_col, pk.group_col))) return st;
 	if ((st = dev_upload(g, &d.hasin, pk.hasin_bits))) return st;
+	{
+		// In-edge lists: the column tiles sorted by destination, sources
+		// ascending within a list (a stable bucketing of the CSR order).
+		std::vector<uint32_t> in_off((size_t) h.n + 1, 0), in_src(h.m);
+		for (uint64_t i = 0; i < h.m; ++i) in_off[h.csr_dst[i] + 1]++;
+		for (uint32_t v = 0; v < h.n; ++v) in_off[v + 1] += in_off[v];
+		std::vector<uint32_t> fill(in_off.begin(), in_off.end() - 1);
+		for (uint32_t u = 0; u < h.n; ++u)
+			for (uint32_t e = h.row_off[u]; e < h.row_off[u + 1]; ++e) in_src[fill[h.csr_dst[e]]++] = u;
+		if ((st = dev_upload(g, &d.in_off, in_off))) return st;
+		if ((st = dev_upload(g, &d.in_src, in_src))) return st;
+	}
 
 	// Run context.
 	RunCtx &r = g->rc;
@@ -180,13 +194,14 @@ int upload(bfs_graph *g, HostGraph &h) {
 		for (int b = 0; b < 3; ++b)
 			if ((st = dev_alloc(g, &r.q[set][b], h.n))) return st;
 	if ((st = dev_alloc(g, &r.ctr, 3))) return st;
+	if ((st = dev_alloc(g, &r.part, 6 * (size_t) kMaxGrid))) return st;
 	if ((st = dev_alloc(g, &r.stats, 1))) return st;
 	if ((st = dev_alloc(g, &r.bar, 2))) return st;
 	if ((st = dev_alloc(g, &r.err, 1))) return st;
 	if ((st = dev_alloc(g, &g->level_buf, h.n))) return st;
 	if ((st = dev_alloc(g, &g->parent_buf, h.n))) return st;
 	if (cudaMallocHost(&g->h_stats, sizeof(DevStats)) != cudaSuccess) return BFS_ENOMEM;
-	if (cudaMallocHost(&g->h_ctr, sizeof(StepCounters) * 3) != cudaSuccess) return BFS_ENOMEM;
+	if (cudaMallocHost(&g->h_part, sizeof(unsigned long long) * 2 * kMaxGrid) != cudaSuccess) return BFS_ENOMEM;
 	if (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess ||
 			cudaEventCreate(&g->evm) != cudaSuccess)
 		return BFS_ECUDA;
@@ -249,17 +264,24 @@ int run_stepwise(bfs_graph *g, const RunCtx &r, const StepParams &p, cudaStream_
 	bool last_dense = false;
 	uint32_t step = 0;
 	for (;; ++step) {
-		if (cudaMemcpyAsync(g->h_ctr, r.ctr, sizeof(StepCounters) * 3, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+		// the step totals: sum of the per-CTA partials of the frontier's slot
+		const uint32_t slot = (step + 2) % 3;
+		if (cudaMemcpyAsync(g->h_part, r.part + (size_t) slot * 2 * kMaxGrid, sizeof(unsigned long long) * 2 * kMaxGrid,
+				    cudaMemcpyDeviceToHost, st) != cudaSuccess ||
 				cudaStreamSynchronize(st) != cudaSuccess)
 			return BFS_ECUDA;
-		const StepCounters &in = g->h_ctr[(step + 2) % 3];
-		hs.reached += in.count;
-		hs.edges_traversed += in.degsum;
-		if (in.count == 0) break;
+		unsigned long long count = 0, degsum = 0;
+		for (int i = 0; i < g->grid; ++i) {
+			count += g->h_part[i];
+			degsum += g->h_part[kMaxGrid + i];
+		}
+		hs.reached += (uint32_t) count;
+		hs.edges_traversed += degsum;
+		if (count == 0) break;
 		bool dense = false;
 		if (step > 0) {
 			unsigned long long thr = last_dense ? p.to_sparse_threshold : p.to_dense_threshold;
-			dense = (unsigned long long) in.count + in.degsum > thr;
+			dense = count + degsum > thr;
 		}
 		if ((rc = launch_step(kStepClear, d, r, p, step, g->batch, g->grid, g->smem, st))) return rc;
 		if (dense) {
@@ -288,6 +310,7 @@ int run_impl(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, 
 	p.source = source;
 	p.warp_max_degree = g->opt.warp_max_degree;
 	p.cta_max_degree = g->opt.cta_max_degree;
+	p.bottom_up = g->opt.bottom_up;
 	p.to_dense_threshold = g->m / std::max<uint32_t>(1, g->opt.to_dense_ratio);
 	p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
 	int rc;
@@ -344,6 +367,7 @@ int collect_stats(bfs_graph *g, bfs_stats *out) {
 	s.bu_words = d.bu_words;
 	s.bu_slices = d.bu_slices;
 	s.bu_groups = d.bu_groups;
+	s.bu_vertices = d.bu_vertices;
 	s.status = g->stepwise_last ? BFS_OK : d.status;
 	s.max_level = s.num_steps ? s.num_steps - 1 : 0;
 	s.grid_ctas = (uint32_t) g->grid;
@@ -492,7 +516,7 @@ int bfs_options_default(bfs_options *opt) {
 
 int bfs_set_options(bfs_graph *g, const bfs_options *opt) {
 	if (!g || !opt) return BFS_EARG;
-	if (opt->mode > BFS_MODE_STEPWISE || opt->to_dense_ratio == 0 || opt->to_sparse_ratio == 0 ||
+	if (opt->mode > BFS_MODE_STEPWISE || opt->bottom_up > BFS_BU_STREAM || opt->to_dense_ratio == 0 || opt->to_sparse_ratio == 0 ||
 			opt->warp_max_degree == 0 || opt->cta_max_degree < opt->warp_max_degree)
 		return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);

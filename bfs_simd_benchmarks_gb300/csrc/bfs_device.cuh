@@ -5,6 +5,9 @@
 
 namespace bfsg {
 
+// Upper bound of the persistent grid: per-CTA partial sums are indexed by CTA.
+constexpr uint32_t kMaxGrid = 2048;
+
 // The graph as it sits in HBM (all read-only during a traversal).
 struct DevGraph {
 	uint32_t n;            // vertices
@@ -22,21 +25,21 @@ struct DevGraph {
 	uint32_t bm_words;          // words of a frontier bitmap, padded to whole stripe slices
 	uint32_t tma;               // 1: the bottom-up step streams segments and slices with bulk copies
 	uint32_t tma_batch;         // frontier slices per bulk-copy stage
+	uint32_t pull_long_cap;     // shared-memory queue of destinations needing a long in-edge scan
 	const uint32_t *row_off;    // [n+1] CSR row starts
 	const uint32_t *col;        // [m]   CSR destinations
 	const uint32_t *packed;     // packed column-major stream (16-byte aligned segments)
 	const uint32_t *seg_off;    // [num_groups*num_stripes+1], group-major
 	const uint32_t *group_col;  // [num_groups+1]
 	const uint32_t *hasin;      // [nwords] in-degree > 0
+	const uint32_t *in_off;     // [n+1] in-edge list starts (destination-sorted column tiles)
+	const uint32_t *in_src;     // [m]   sources of the in-edges, ascending within a list
 };
 
 // Counters of the frontier a step produces (three slots rotate by step).
 struct StepCounters {
 	unsigned int tail[3];       // queue bucket tails (top-down appends, to_sparse)
-	unsigned int count;         // vertices discovered by the step
-	unsigned long long degsum;  // their out-degree sum
 	unsigned int work;          // dynamic work counter (column groups)
-	unsigned int pad;
 };
 
 // Per-run statistics gathered on the device.
@@ -46,6 +49,7 @@ struct DevStats {
 	unsigned long long bu_words;
 	unsigned long long bu_slices;
 	unsigned long long bu_groups;
+	unsigned long long bu_vertices;   // destinations tested by pull steps
 	unsigned long long reached;
 	unsigned long long edges_traversed;
 	unsigned int num_steps;
@@ -71,6 +75,7 @@ struct RunCtx {
 	uint8_t *sf[3];        // [num_stripes] rotating "stripe has a frontier vertex" flags
 	uint32_t *q[2][3];     // [2 sets][3 buckets][n] frontier queues
 	StepCounters *ctr;     // [3]
+	unsigned long long *part;  // [3 slots][2 (count, degsum)][kMaxGrid] per-CTA step totals
 	DevStats *stats;
 	unsigned *bar;         // [2] grid barrier
 	int *err;              // device status word
@@ -80,7 +85,7 @@ struct StepParams {
 	uint32_t source;
 	uint32_t warp_max_degree;
 	uint32_t cta_max_degree;
-	uint32_t pad;
+	uint32_t bottom_up;   // 0: pull over in-edge lists, 1: stream the packed tiles
 	unsigned long long to_dense_threshold;   // dense when frontier + degsum > this
 	unsigned long long to_sparse_threshold;  // stay dense while frontier + degsum > this
 };

@@ -39,7 +39,7 @@ constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 
 struct ThreadAcc {
-	unsigned long long count, degsum, td_edges, td_vertices, bu_words, bu_slices, bu_groups;
+	unsigned long long count, degsum, td_edges, td_vertices, bu_words, bu_slices, bu_groups, bu_vertices;
 };
 
 __device__ __forceinline__ uint32_t bucket_of(uint32_t deg, const StepParams &p) {
@@ -48,16 +48,46 @@ __device__ __forceinline__ uint32_t bucket_of(uint32_t deg, const StepParams &p)
 
 constexpr int kTdPerLane = 4;  // candidate edges a lane handles per top-down iteration
 
+// Next-frontier appends of one warp are staged in a shared-memory buffer per
+// degree bucket and moved to the global queue in blocks, so the queue tails
+// see one atomicAdd per block of up to kWqCap vertices instead of one per
+// warp iteration (the three tails share a cache line that every CTA hits).
+constexpr uint32_t kWqCap = 32 * kTdPerLane;
+
+struct WarpQ {
+	uint32_t *buf;           // this warp's 3 x kWqCap entries
+	uint32_t n[3];           // staged entries per bucket (warp-uniform)
+	uint32_t *const *qn;     // the global next-frontier queues
+	unsigned *tails;
+};
+
+__device__ __forceinline__ void wq_flush(WarpQ &wq, int bk) {
+	__syncwarp();
+	const unsigned lane = lane_id();
+	uint32_t base = 0;
+	if (lane == 0) base = atomicAdd(&wq.tails[bk], wq.n[bk]);
+	base = __shfl_sync(kFull, base, 0);
+	for (uint32_t i = lane; i < wq.n[bk]; i += 32) wq.qn[bk][base + i] = wq.buf[bk * kWqCap + i];
+	__syncwarp();
+	wq.n[bk] = 0;
+}
+
+__device__ __forceinline__ void wq_flush_all(WarpQ &wq) {
+#pragma unroll
+	for (int bk = 0; bk < 3; ++bk)
+		if (wq.n[bk]) wq_flush(wq, bk);
+}
+
 // All 32 lanes of the warp call this with up to kTdPerLane candidate edges
 // u[q] -> v[q] each (has[q] false for an empty slot).  The visited checks,
 // the claiming atomicOr's and the degree loads of the claimed vertices are
 // each issued for all candidates before any result is used, so a lane waits
 // for one round trip per stage rather than one per edge.  Claimed vertices
-// get their level and parent and are appended to the next queue bucket of
-// their out-degree with one atomicAdd per warp and bucket.
+// get their level and parent and are staged for the next queue bucket of
+// their out-degree.
 __device__ __forceinline__ void visit_and_append(const bool (&has)[kTdPerLane], const uint32_t (&u)[kTdPerLane],
-		const uint32_t (&v)[kTdPerLane], int32_t next_level, const DevGraph &g, const RunCtx &r,
-		uint32_t *const *qn, unsigned *tails, const StepParams &p, ThreadAcc &acc) {
+		const uint32_t (&v)[kTdPerLane], int32_t next_level, const DevGraph &g, const RunCtx &r, WarpQ &wq,
+		const StepParams &p, ThreadAcc &acc) {
 	bool cand[kTdPerLane];
 	uint32_t word[kTdPerLane];
 #pragma unroll
@@ -89,23 +119,22 @@ __device__ __forceinline__ void visit_and_append(const bool (&has)[kTdPerLane], 
 		cnt[bucket_of(deg[q], p)]++;
 	}
 	if (!__ballot_sync(kFull, cnt[0] | cnt[1] | cnt[2])) return;
-	const unsigned lane = lane_id();
 	uint32_t pos[3];
 #pragma unroll
 	for (int bk = 0; bk < 3; ++bk) {
 		const uint32_t incl = warp_incl_scan(cnt[bk]);
 		const uint32_t tot = __shfl_sync(kFull, incl, 31);
-		uint32_t base = 0;
-		if (lane == 31 && tot) base = atomicAdd(&tails[bk], tot);
-		base = __shfl_sync(kFull, base, 31);
-		pos[bk] = base + incl - cnt[bk];
+		if (wq.n[bk] + tot > kWqCap) wq_flush(wq, bk);
+		pos[bk] = wq.n[bk] + incl - cnt[bk];
+		wq.n[bk] += tot;
 	}
 #pragma unroll
 	for (int q = 0; q < kTdPerLane; ++q) {
 		if (!claimed[q]) continue;
 		const uint32_t bk = bucket_of(deg[q], p);
-		qn[bk][pos[bk]++] = v[q];
+		wq.buf[bk * kWqCap + pos[bk]++] = v[q];
 	}
+	__syncwarp();
 }
 
 // Vertices of a top-down chunk staged in shared memory.
@@ -134,7 +163,7 @@ __device__ __forceinline__ uint32_t block_incl_scan(uint32_t x) {
 // Top-down step (BFS_kernel_sparse + update_sparse, apps/bfs_simd/bfs.cpp:467-711)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t step,
-		ThreadAcc &acc) {
+		uint32_t *smem, ThreadAcc &acc) {
 	const uint32_t cur = step & 1, nxt = (step + 1) & 1;
 	const StepCounters *in = r.ctr + (step + 2) % 3;
 	StepCounters *out = r.ctr + step % 3;
@@ -143,12 +172,12 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 	const uint32_t nL = ld_volatile(&in->tail[2]);
 	const uint32_t *qS = r.q[cur][0], *qM = r.q[cur][1], *qL = r.q[cur][2];
 	uint32_t *const qn[3] = {r.q[nxt][0], r.q[nxt][1], r.q[nxt][2]};
-	unsigned *tails = out->tail;
 	const int32_t nl = (int32_t) step + 1;
 	const unsigned lane = lane_id(), wid = warp_id();
 	const uint64_t gwarp = (uint64_t) blockIdx.x * kWarps + wid;
 	const uint64_t nwarps = (uint64_t) gridDim.x * kWarps;
 	constexpr uint32_t kSpan = 32 * kTdPerLane;  // edges per warp iteration
+	WarpQ wq{smem + (size_t) wid * 3 * kWqCap, {0, 0, 0}, qn, out->tail};
 	bool has[kTdPerLane];
 	uint32_t uu[kTdPerLane], vv[kTdPerLane];
 
@@ -188,7 +217,7 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 				uu[q] = xsh.u[jj];
 				vv[q] = has[q] ? __ldg(g.col + xsh.beg[jj] + (uint32_t) (f - prev)) : 0u;
 			}
-			visit_and_append(has, uu, vv, nl, g, r, qn, tails, p, acc);
+			visit_and_append(has, uu, vv, nl, g, r, wq, p, acc);
 		}
 		if (blockIdx.x == 0 && threadIdx.x == 0) { acc.td_edges += total; acc.td_vertices += cn; }
 		__syncthreads();
@@ -231,7 +260,7 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 					uu[q] = xsh.u[jj];
 					vv[q] = has[q] ? __ldg(g.col + xsh.beg[jj] + (uint32_t) (f - prev)) : 0u;
 				}
-				visit_and_append(has, uu, vv, nl, g, r, qn, tails, p, acc);
+				visit_and_append(has, uu, vv, nl, g, r, wq, p, acc);
 			}
 			if (threadIdx.x == 0) { acc.td_edges += total; acc.td_vertices += cn; }
 			__syncthreads();
@@ -265,7 +294,7 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 				const uint32_t oe = __shfl_sync(kFull, excl, lo);
 				vv[q] = has[q] ? __ldg(g.col + ob + (f - oe)) : 0u;
 			}
-			visit_and_append(has, uu, vv, nl, g, r, qn, tails, p, acc);
+			visit_and_append(has, uu, vv, nl, g, r, wq, p, acc);
 		}
 		const unsigned nvalid = (unsigned) __popc(__ballot_sync(kFull, valid));
 		if (lane == 0) {
@@ -273,12 +302,13 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 			acc.td_vertices += nvalid;
 		}
 	}
+	wq_flush_all(wq);
 }
 
 // ---------------------------------------------------------------------------
 // Queue -> bitmap (to_dense, apps/bfs_simd/bfs.cpp:54-88)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void phase_to_dense(const DevGraph &g, const RunCtx &r, uint32_t step) {
+__device__ __forceinline__ void phase_to_dense(const DevGraph &g, const RunCtx &r, uint32_t step, bool track_stripes) {
 	const StepCounters *in = r.ctr + (step + 2) % 3;
 	const uint32_t cur = step & 1;
 	uint32_t n0 = ld_volatile(&in->tail[0]), n1 = ld_volatile(&in->tail[1]), n2 = ld_volatile(&in->tail[2]);
@@ -292,7 +322,9 @@ __device__ __forceinline__ void phase_to_dense(const DevGraph &g, const RunCtx &
 		else if (i < (uint64_t) n0 + n1) v = ld_cg(r.q[cur][1] + (i - n0));
 		else v = ld_cg(r.q[cur][2] + (i - n0 - n1));
 		atomicOr(bm + (v >> 5), 1u << (v & 31));
-		sf[v / g.sw] = 1;
+		// stripe flags feed only the streaming bottom-up step; read before
+		// writing, since every CTA hits the same few cache lines
+		if (track_stripes && !ld_cg_u8(sf + v / g.sw)) sf[v / g.sw] = 1;
 	}
 }
 
@@ -369,7 +401,7 @@ __device__ __shared__ alignas(8) uint64_t tma_empty[kTmaStages];  // stage relea
 // into nxt_s, and counts the vertices with an in-edge that are still unvisited.
 // Returns false when no group is left.  Uniform across the CTA.
 __device__ __forceinline__ bool dense_group_begin(const DevGraph &g, const RunCtx &r, StepCounters *out, uint32_t *vis_s,
-		uint32_t *nxt_s, DenseGroup &gr) {
+		uint32_t *nxt_s, DenseGroup &gr, uint32_t *hin_s = nullptr) {
 	__syncthreads();
 	if (threadIdx.x == 0) { dsh.group = atomicAdd(&out->work, 1u); dsh.unsettled = 0; dsh.stop = 0; }
 	__syncthreads();
@@ -385,6 +417,7 @@ __device__ __forceinline__ bool dense_group_begin(const DevGraph &g, const RunCt
 		uint32_t hb = bits_at(g.hasin, gr.v0 + 32ull * j, gr.v1, 0u);
 		vis_s[j] = vb;
 		nxt_s[j] = vb;  // visited bits at the start: the new frontier is vis_s & ~nxt_s
+		if (hin_s) hin_s[j] = hb;
 		uns += __popc(hb & ~vb);
 	}
 	if (threadIdx.x == 0) vis_s[gr.gw] = kFull;  // the slot padding words point at
@@ -482,7 +515,6 @@ __device__ __forceinline__ void dense_group_publish(const DevGraph &g, const Run
 				const uint32_t v = v0 + 32u * j + lane;
 				deg[q] = __ldg(g.row_off + v + 1) - __ldg(g.row_off + v);
 				r.level[v] = nl;
-				sf_nxt[v / sw] = 1;
 			}
 		}
 #pragma unroll
@@ -493,6 +525,14 @@ __device__ __forceinline__ void dense_group_publish(const DevGraph &g, const Run
 				acc.count += __popc(bits[q]);
 				or_bits_at(nxt, vb, bits[q]);
 				or_bits_at(r.vis, vb, bits[q]);
+				if (sf_nxt) {
+					// the stripes of the first and last new vertex of the word
+					// (a word of 32 vertices spans at most two stripes when S*W >= 32)
+					const uint32_t ka = (uint32_t) ((vb + (__ffs(bits[q]) - 1)) / sw);
+					const uint32_t kb = (uint32_t) ((vb + (31 - __clz(bits[q]))) / sw);
+					for (uint32_t k = ka; k <= kb; ++k)
+						if (!ld_cg_u8(sf_nxt + k)) sf_nxt[k] = 1;
+				}
 			}
 		}
 	}
@@ -784,9 +824,145 @@ __device__ __forceinline__ void phase_dense_tma(const DevGraph &g, const RunCtx 
 	}
 }
 
-__device__ __forceinline__ void phase_dense(const DevGraph &g, const RunCtx &r, uint32_t step, uint32_t batch,
-		uint32_t *smem, ThreadAcc &acc) {
-	if (g.tma) phase_dense_tma(g, r, step, smem, acc);
+// Bottom-up step as a pull over in-edge lists (the column's tiles sorted by
+// destination): a CTA owns a column group with its visited bits in shared
+// memory; every unvisited destination that has in-edges scans them in order
+// and stops at the first source in the frontier (Beamer's bottom-up; the
+// reference's dense step tests every edge of the active rows instead,
+// apps/bfs_simd/bfs.cpp:194-217, with the same levels).  Pass 1 gives each
+// destination one lane and its first kPullShort in-edges; destinations not
+// settled by then go to a shared-memory queue that whole warps scan 32 edges
+// at a time with a ballot to stop at the first hit.
+constexpr uint32_t kPullShort = 4;
+
+__device__ __forceinline__ bool frontier_bit(const uint32_t *cur, uint32_t u) {
+	return (ld_cg(cur + (u >> 5)) >> (u & 31)) & 1u;
+}
+
+__device__ __forceinline__ void phase_pull(const DevGraph &g, const RunCtx &r, uint32_t step, uint32_t *smem,
+		ThreadAcc &acc) {
+	const uint32_t *cur = r.bm[(step + 2) % 3];
+	uint32_t *nxt = r.bm[step % 3];
+	StepCounters *out = r.ctr + step % 3;
+	const int32_t nl = (int32_t) step + 1;
+	const unsigned wid = warp_id(), lane = lane_id();
+	const uint32_t mgw = g.max_group_words + 1;
+	uint32_t *vis_s = smem;
+	uint32_t *vis0_s = vis_s + mgw;
+	uint32_t *hin_s = vis0_s + mgw;
+	uint32_t *longq = hin_s + mgw;
+	const uint32_t long_cap = g.pull_long_cap;
+	uint32_t *parent = r.parent;
+	DenseGroup gr;
+	unsigned long long cyc[4] = {0, 0, 0, 0};
+	long long t0 = clock64();
+	while (dense_group_begin(g, r, out, vis_s, vis0_s, gr, hin_s)) {
+		{ long long t1 = clock64(); cyc[0] += t1 - t0; t0 = t1; }
+		if (dsh.unsettled == 0) continue;
+		if (threadIdx.x == 0) { acc.bu_groups++; dsh.nlist = 0; }
+		__syncthreads();
+		const uint32_t v0 = (uint32_t) gr.v0;
+		uint32_t edges = 0, tested = 0;
+		// Pass 1: a warp takes four bitmap words (a lane per destination in
+		// each); the list offsets, the first in-edge and its frontier word of
+		// all four destinations are loaded stage by stage, so a lane waits for
+		// three round trips per four destinations, not per destination.
+		for (uint32_t j0 = wid * 4; j0 < gr.gw; j0 += kWarps * 4) {
+			uint32_t todo_w[4], beg[4], end[4], u[4];
+			bool found[4];
+#pragma unroll
+			for (int q = 0; q < 4; ++q) {
+				const uint32_t j = j0 + q;
+				todo_w[q] = (j < gr.gw) ? (hin_s[j] & ~vis0_s[j]) : 0u;
+				found[q] = false;
+				beg[q] = end[q] = 0;
+				if ((todo_w[q] >> lane) & 1u) {
+					const uint32_t v = v0 + 32u * j + lane;
+					beg[q] = __ldg(g.in_off + v);
+					end[q] = __ldg(g.in_off + v + 1);
+				}
+			}
+#pragma unroll
+			for (int q = 0; q < 4; ++q) u[q] = (beg[q] < end[q]) ? __ldg(g.in_src + beg[q]) : 0u;
+#pragma unroll
+			for (int q = 0; q < 4; ++q) {
+				if (beg[q] < end[q]) {
+					++tested;
+					++edges;
+					found[q] = frontier_bit(cur, u[q]);
+				}
+			}
+#pragma unroll
+			for (int q = 0; q < 4; ++q) {
+				if (beg[q] < end[q] && !found[q]) {
+					// the next few in-edges, then the long queue
+					const uint32_t v = v0 + 32u * (j0 + q) + lane;
+					const uint32_t stop = min(end[q], beg[q] + kPullShort);
+					uint32_t e = beg[q] + 1;
+					for (; e < stop; ++e) {
+						++edges;
+						u[q] = __ldg(g.in_src + e);
+						if (frontier_bit(cur, u[q])) { found[q] = true; break; }
+					}
+					if (!found[q] && e < end[q]) {
+						const uint32_t pos = atomicAdd(&dsh.nlist, 1u);
+						if (pos < long_cap) {
+							longq[pos] = v;
+						} else {
+							// queue full: finish the scan here
+							for (; e < end[q]; ++e) {
+								++edges;
+								u[q] = __ldg(g.in_src + e);
+								if (frontier_bit(cur, u[q])) { found[q] = true; break; }
+							}
+						}
+					}
+				}
+				if (found[q] && parent) parent[v0 + 32u * (j0 + q) + lane] = u[q];
+				const uint32_t fmask = __ballot_sync(kFull, found[q]);
+				if (lane == 0 && fmask) atomicOr(&vis_s[j0 + q], fmask);
+			}
+		}
+		__syncthreads();
+		{ long long t1 = clock64(); cyc[1] += t1 - t0; t0 = t1; }
+		// Pass 2: a warp per remaining destination, 32 in-edges at a time.
+		const uint32_t nlong = min(dsh.nlist, long_cap);
+		for (uint32_t x = wid; x < nlong; x += kWarps) {
+			const uint32_t v = longq[x];
+			const uint32_t end = __ldg(g.in_off + v + 1);
+			for (uint32_t e0 = __ldg(g.in_off + v) + kPullShort; e0 < end; e0 += 32) {
+				const uint32_t e = e0 + lane;
+				uint32_t u = 0;
+				const bool hit = e < end && frontier_bit(cur, u = __ldg(g.in_src + e));
+				const uint32_t hm = __ballot_sync(kFull, hit);
+				if (hm) {
+					const int first = __ffs(hm) - 1;
+					if (lane == (unsigned) first) {
+						if (parent) parent[v] = u;
+						const uint32_t d = v - v0;
+						atomicOr(&vis_s[d >> 5], 1u << (d & 31));
+					}
+					if (lane == 0) edges += (uint32_t) first + 1;
+					break;
+				}
+				if (lane == 0) edges += min(32u, end - e0);
+			}
+		}
+		acc.bu_words += edges;
+		acc.bu_vertices += tested;
+		__syncthreads();
+		{ long long t1 = clock64(); cyc[2] += t1 - t0; t0 = t1; }
+		dense_group_publish(g, r, gr, vis_s, vis0_s, nl, nxt, nullptr, acc);  // the pull reads no stripe flags
+		{ long long t1 = clock64(); cyc[3] += t1 - t0; t0 = t1; }
+	}
+	if (threadIdx.x == 0)
+		for (int i = 0; i < 4; ++i) atomicAdd(&r.stats->bu_cycles[i], cyc[i]);
+}
+
+__device__ __forceinline__ void phase_dense(const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t step,
+		uint32_t batch, uint32_t *smem, ThreadAcc &acc) {
+	if (p.bottom_up == 0) phase_pull(g, r, step, smem, acc);
+	else if (g.tma) phase_dense_tma(g, r, step, smem, acc);
 	else phase_dense_generic(g, r, step, batch, smem, acc);
 }
 
@@ -802,40 +978,82 @@ __device__ __forceinline__ void clear_slot(const DevGraph &g, const RunCtx &r, u
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		StepCounters *c = r.ctr + slot;
 		c->tail[0] = c->tail[1] = c->tail[2] = 0;
-		c->count = 0;
-		c->degsum = 0;
 		c->work = 0;
 	}
 }
 
-// Adds the CTA's accumulated counts to the step slot and the run statistics.
-__device__ __forceinline__ void flush_acc(ThreadAcc &acc, StepCounters *slot, DevStats *stats) {
-	__shared__ unsigned long long red[7][kWarps];
-	unsigned long long v[7] = {acc.count, acc.degsum, acc.td_edges, acc.td_vertices, acc.bu_words, acc.bu_slices, acc.bu_groups};
+// The step totals (vertices discovered, their out-degree sum) are written as
+// one partial per CTA -- plain stores, no atomics on a shared cache line --
+// and every CTA sums the partials after the grid barrier.
+__device__ __forceinline__ unsigned long long *part_at(const RunCtx &r, uint32_t slot, uint32_t which) {
+	return r.part + ((size_t) slot * 2 + which) * kMaxGrid;
+}
+
+__device__ __forceinline__ void flush_step(ThreadAcc &acc, const RunCtx &r, uint32_t slot) {
+	__shared__ unsigned long long red[2][kWarps];
+	const unsigned lane = lane_id(), wid = warp_id();
+	const unsigned long long c = warp_sum(acc.count), d = warp_sum(acc.degsum);
+	if (lane == 0) { red[0][wid] = c; red[1][wid] = d; }
+	__syncthreads();
+	if (threadIdx.x < 2) {
+		unsigned long long t = 0;
+		for (int w = 0; w < kWarps; ++w) t += red[threadIdx.x][w];
+		part_at(r, slot, threadIdx.x)[blockIdx.x] = t;
+	}
+	__syncthreads();
+	acc.count = 0;
+	acc.degsum = 0;
+}
+
+// Sums the partials of `slot` over the grid (all threads call).
+__device__ __forceinline__ void step_totals(const RunCtx &r, uint32_t slot, uint32_t *count,
+		unsigned long long *degsum) {
+	__shared__ unsigned long long tot[2];
+	if (warp_id() == 0) {
+		unsigned long long c = 0, d = 0;
+		const unsigned long long *pc = part_at(r, slot, 0), *pd = part_at(r, slot, 1);
+		for (uint32_t i = lane_id(); i < gridDim.x; i += 32) {
+			c += __ldcg(pc + i);
+			d += __ldcg(pd + i);
+		}
+		c = warp_sum(c);
+		d = warp_sum(d);
+		if (lane_id() == 0) { tot[0] = c; tot[1] = d; }
+	}
+	__syncthreads();
+	*count = (uint32_t) tot[0];
+	*degsum = tot[1];
+	__syncthreads();
+}
+
+// Adds the CTA's counters to the run statistics (once per launch).
+__device__ __forceinline__ void flush_stats(ThreadAcc &acc, DevStats *stats) {
+	__shared__ unsigned long long red[6][kWarps];
+	unsigned long long v[6] = {acc.td_edges, acc.td_vertices, acc.bu_words, acc.bu_slices, acc.bu_groups,
+			acc.bu_vertices};
 	const unsigned lane = lane_id(), wid = warp_id();
 #pragma unroll
-	for (int i = 0; i < 7; ++i) {
+	for (int i = 0; i < 6; ++i) {
 		unsigned long long x = warp_sum(v[i]);
 		if (lane == 0) red[i][wid] = x;
 	}
 	__syncthreads();
-	if (threadIdx.x < 7) {
-		unsigned long long s = 0;
-		for (int wv = 0; wv < kWarps; ++wv) s += red[threadIdx.x][wv];
-		if (s) {
+	if (threadIdx.x < 6) {
+		unsigned long long t = 0;
+		for (int w = 0; w < kWarps; ++w) t += red[threadIdx.x][w];
+		if (t) {
 			switch (threadIdx.x) {
-			case 0: atomicAdd(&slot->count, (unsigned) s); break;
-			case 1: atomicAdd(&slot->degsum, s); break;
-			case 2: atomicAdd(&stats->td_edges, s); break;
-			case 3: atomicAdd(&stats->td_vertices, s); break;
-			case 4: atomicAdd(&stats->bu_words, s); break;
-			case 5: atomicAdd(&stats->bu_slices, s); break;
-			default: atomicAdd(&stats->bu_groups, s); break;
+			case 0: atomicAdd(&stats->td_edges, t); break;
+			case 1: atomicAdd(&stats->td_vertices, t); break;
+			case 2: atomicAdd(&stats->bu_words, t); break;
+			case 3: atomicAdd(&stats->bu_slices, t); break;
+			case 4: atomicAdd(&stats->bu_groups, t); break;
+			default: atomicAdd(&stats->bu_vertices, t); break;
 			}
 		}
 	}
 	__syncthreads();
-	acc = ThreadAcc{0, 0, 0, 0, 0, 0, 0};
+	acc.td_edges = acc.td_vertices = acc.bu_words = acc.bu_slices = acc.bu_groups = acc.bu_vertices = 0;
 }
 
 __device__ void seed_source(const DevGraph &g, const RunCtx &r, const StepParams &p) {
@@ -848,8 +1066,8 @@ __device__ void seed_source(const DevGraph &g, const RunCtx &r, const StepParams
 	r.q[0][bk][0] = s;
 	StepCounters *c = r.ctr + 2;  // the frontier "produced by step -1"
 	c->tail[bk] = 1;
-	c->count = 1;
-	c->degsum = deg;
+	part_at(r, 2, 0)[0] = 1;
+	part_at(r, 2, 1)[0] = deg;
 }
 
 // ---------------------------------------------------------------------------
@@ -870,6 +1088,7 @@ __global__ void __launch_bounds__(kThreads) k_init(DevGraph g, RunCtx r) {
 	}
 	for (uint64_t i = t0; i < g.num_stripes; i += stride) { r.sf[0][i] = 0; r.sf[1][i] = 0; r.sf[2][i] = 0; }
 	if (t0 < 3 * sizeof(StepCounters) / 4) ((uint32_t *) r.ctr)[t0] = 0;
+	for (uint64_t i = t0; i < 6ull * kMaxGrid; i += stride) r.part[i] = 0;
 	if (t0 < sizeof(DevStats) / 4) ((uint32_t *) r.stats)[t0] = 0;
 	if (t0 < 2) r.bar[t0] = 0;
 	if (t0 == 0) *r.err = 0;
@@ -881,7 +1100,7 @@ __global__ void k_seed(DevGraph g, RunCtx r, StepParams p) {
 
 __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunCtx r, StepParams p, uint32_t batch) {
 	extern __shared__ __align__(128) uint32_t smem[];
-	ThreadAcc acc{0, 0, 0, 0, 0, 0, 0};
+	ThreadAcc acc{0, 0, 0, 0, 0, 0, 0, 0};
 	bool ok = true;
 	dense_tma_init();
 	if (blockIdx.x == 0 && threadIdx.x == 0) seed_source(g, r, p);
@@ -889,9 +1108,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 	bool last_dense = false;
 	uint32_t step = 0;
 	for (; ok; ++step) {
-		const StepCounters *in = r.ctr + (step + 2) % 3;
-		const uint32_t fsize = ld_volatile(&in->count);
-		const unsigned long long dsum = ld_volatile_u64(&in->degsum);
+		uint32_t fsize;
+		unsigned long long dsum;
+		step_totals(r, (step + 2) % 3, &fsize, &dsum);
 		if (blockIdx.x == 0 && threadIdx.x == 0) {
 			r.stats->reached += fsize;
 			r.stats->edges_traversed += dsum;
@@ -906,20 +1125,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 		clear_slot(g, r, (step + 1) % 3);
 		if (dense) {
 			if (!last_dense) {
-				phase_to_dense(g, r, step);
+				phase_to_dense(g, r, step, p.bottom_up != 0);
 				if (!(ok = grid_barrier(r.bar, r.err))) break;
 				if (blockIdx.x == 0 && threadIdx.x == 0 && step < 256) r.stats->t_conv[step] = global_timer_ns();
 			}
-			phase_dense(g, r, step, batch, smem, acc);
+			phase_dense(g, r, p, step, batch, smem, acc);
 		} else {
 			if (last_dense) {
 				phase_to_sparse(g, r, p, step);
 				if (!(ok = grid_barrier(r.bar, r.err))) break;
 				if (blockIdx.x == 0 && threadIdx.x == 0 && step < 256) r.stats->t_conv[step] = global_timer_ns();
 			}
-			phase_expand(g, r, p, step, acc);
+			phase_expand(g, r, p, step, smem, acc);
 		}
-		flush_acc(acc, r.ctr + step % 3, r.stats);
+		flush_step(acc, r, step % 3);
 		if (blockIdx.x == 0 && threadIdx.x == 0) {
 			if (step < 256) r.stats->trace[step] = dense ? 1 : 0;
 			if (dense) r.stats->dense_steps++;
@@ -927,6 +1146,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 		last_dense = dense;
 		ok = grid_barrier(r.bar, r.err);
 	}
+	flush_stats(acc, r.stats);
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		r.stats->num_steps = step;
 		r.stats->status = *(volatile int *) r.err;
@@ -937,23 +1157,27 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 __global__ void __launch_bounds__(kThreads) k_step_clear(DevGraph g, RunCtx r, uint32_t step) {
 	clear_slot(g, r, (step + 1) % 3);
 }
-__global__ void __launch_bounds__(kThreads) k_step_to_dense(DevGraph g, RunCtx r, uint32_t step) {
-	phase_to_dense(g, r, step);
+__global__ void __launch_bounds__(kThreads) k_step_to_dense(DevGraph g, RunCtx r, StepParams p, uint32_t step) {
+	phase_to_dense(g, r, step, p.bottom_up != 0);
 }
 __global__ void __launch_bounds__(kThreads) k_step_to_sparse(DevGraph g, RunCtx r, StepParams p, uint32_t step) {
 	phase_to_sparse(g, r, p, step);
 }
 __global__ void __launch_bounds__(kThreads) k_step_expand(DevGraph g, RunCtx r, StepParams p, uint32_t step) {
-	ThreadAcc acc{0, 0, 0, 0, 0, 0, 0};
-	phase_expand(g, r, p, step, acc);
-	flush_acc(acc, r.ctr + step % 3, r.stats);
-}
-__global__ void __launch_bounds__(kThreads, 2) k_step_dense(DevGraph g, RunCtx r, uint32_t step, uint32_t batch) {
 	extern __shared__ __align__(128) uint32_t smem[];
-	ThreadAcc acc{0, 0, 0, 0, 0, 0, 0};
+	ThreadAcc acc{0, 0, 0, 0, 0, 0, 0, 0};
+	phase_expand(g, r, p, step, smem, acc);
+	flush_step(acc, r, step % 3);
+	flush_stats(acc, r.stats);
+}
+__global__ void __launch_bounds__(kThreads, 2) k_step_dense(DevGraph g, RunCtx r, StepParams p, uint32_t step,
+		uint32_t batch) {
+	extern __shared__ __align__(128) uint32_t smem[];
+	ThreadAcc acc{0, 0, 0, 0, 0, 0, 0, 0};
 	dense_tma_init();
-	phase_dense(g, r, step, batch, smem, acc);
-	flush_acc(acc, r.ctr + step % 3, r.stats);
+	phase_dense(g, r, p, step, batch, smem, acc);
+	flush_step(acc, r, step % 3);
+	flush_stats(acc, r.stats);
 }
 
 // ---------------------------------------------------------------------------
@@ -963,7 +1187,11 @@ size_t dense_smem_bytes(const DevGraph &g, uint32_t batch) {
 	size_t words = (size_t) 2 * (g.max_group_words + 1) + 3 * kThreads;
 	if (g.tma) words += (size_t) kTmaStages * (kTmaEdgeWords + (size_t) g.tma_batch * g.slice_words);
 	else words += (size_t) batch * g.slice_words;
-	return sizeof(uint32_t) * words;
+	const size_t pull = (size_t) 3 * (g.max_group_words + 1) + g.pull_long_cap;
+	const size_t expand = (size_t) kWarps * 3 * kWqCap;
+	size_t need = words > pull ? words : pull;
+	need = need > expand ? need : expand;
+	return sizeof(uint32_t) * need;
 }
 
 int persistent_grid(const DevGraph &g, uint32_t batch, int num_sms, int *grid, size_t *smem) {
@@ -971,6 +1199,8 @@ int persistent_grid(const DevGraph &g, uint32_t batch, int num_sms, int *grid, s
 	if (cudaFuncSetAttribute(k_bfs_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) *smem) != cudaSuccess)
 		return BFS_ECUDA;
 	if (cudaFuncSetAttribute(k_step_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) *smem) != cudaSuccess)
+		return BFS_ECUDA;
+	if (cudaFuncSetAttribute(k_step_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) *smem) != cudaSuccess)
 		return BFS_ECUDA;
 	int per_sm = 0;
 	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bfs_persistent, kThreads, *smem) != cudaSuccess)
@@ -1002,10 +1232,10 @@ int launch_step(int kind, const DevGraph &g, const RunCtx &r, const StepParams &
 	switch (kind) {
 	case kStepSeed: k_seed<<<1, 32, 0, st>>>(g, r, p); break;
 	case kStepClear: k_step_clear<<<grid, kThreads, 0, st>>>(g, r, step); break;
-	case kStepToDense: k_step_to_dense<<<grid, kThreads, 0, st>>>(g, r, step); break;
+	case kStepToDense: k_step_to_dense<<<grid, kThreads, 0, st>>>(g, r, p, step); break;
 	case kStepToSparse: k_step_to_sparse<<<grid, kThreads, 0, st>>>(g, r, p, step); break;
-	case kStepExpand: k_step_expand<<<grid, kThreads, 0, st>>>(g, r, p, step); break;
-	case kStepDense: k_step_dense<<<grid, kThreads, smem, st>>>(g, r, step, batch); break;
+	case kStepExpand: k_step_expand<<<grid, kThreads, smem, st>>>(g, r, p, step); break;
+	case kStepDense: k_step_dense<<<grid, kThreads, smem, st>>>(g, r, p, step, batch); break;
 	default: return BFS_EARG;
 	}
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;

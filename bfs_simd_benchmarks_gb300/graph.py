@@ -122,6 +122,8 @@ class Graph:
         for k, v in kw.items():
             if k == "mode" and isinstance(v, str):
                 v = {"persistent": N.BFS_MODE_PERSISTENT, "stepwise": N.BFS_MODE_STEPWISE}[v]
+            if k == "bottom_up" and isinstance(v, str):
+                v = {"pull": N.BFS_BU_PULL, "stream": N.BFS_BU_STREAM}[v]
             setattr(o, k, int(v))
         N.check(lib.bfs_set_options(self._h, C.byref(o)), "bfs_set_options")
 

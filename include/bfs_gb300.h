@@ -123,8 +123,17 @@ typedef struct bfs_options {
 	                              (the reference uses the same ratio for both) */
 	uint32_t warp_max_degree;  /* top-down: degree <= this -> warp-cooperative gather */
 	uint32_t cta_max_degree;   /* top-down: degree <= this -> one CTA per vertex; above -> grid-strided */
-	uint32_t reserved[3];
+	uint32_t bottom_up;        /* BFS_BU_PULL or BFS_BU_STREAM */
+	uint32_t reserved[2];
 } bfs_options;
+
+/* Bottom-up step variants.  PULL: every unvisited destination of a column
+ * group scans its in-edges (the column's tiles sorted by destination) and
+ * stops at the first source in the frontier.  STREAM: the column group's
+ * tiles of every active stripe are streamed into shared memory with bulk
+ * copies and every edge is tested, the reference's dense step. */
+#define BFS_BU_PULL 0u
+#define BFS_BU_STREAM 1u
 
 /* Fills the defaults (reference switch rule, persistent mode). */
 int bfs_options_default(bfs_options *opt);
@@ -142,9 +151,10 @@ typedef struct bfs_stats {
 	uint64_t edges_traversed;  /* m(s): sum of out-degrees of reached vertices (TEPS numerator) */
 	uint64_t td_edges;         /* CSR edges read by top-down steps */
 	uint64_t td_vertices;      /* frontier vertices expanded top-down */
-	uint64_t bu_words;         /* packed tile words streamed by bottom-up steps */
+	uint64_t bu_words;         /* bottom-up: packed tile words streamed (STREAM) or in-edges read (PULL) */
 	uint64_t bu_slices;        /* frontier slices staged by bottom-up steps */
 	uint64_t bu_groups;        /* column groups visited by bottom-up steps */
+	uint64_t bu_vertices;      /* destinations tested by PULL bottom-up steps */
 	double device_ms;          /* device time of the traversal, initialisation included (CUDA events) */
 	double kernel_ms;          /* device time of the traversal kernel(s) alone */
 	int32_t status;            /* device-side status of the run (BFS_OK or BFS_ETIMEOUT) */

@@ -36,14 +36,15 @@ def _check_run(B, oracle, arr, g, src, expect=None, trace=True):
     return lev, st
 
 
+@pytest.mark.parametrize("bottom_up", ["pull", "stream"])
 @pytest.mark.parametrize("mode", ["persistent", "stepwise"])
 @pytest.mark.parametrize("name", CASES)
-def test_golden_levels_from_edges(native, oracle, name, mode):
+def test_golden_levels_from_edges(native, oracle, name, mode, bottom_up):
     import bfs_simd_benchmarks_gb300 as B
     c = load_case(name)
     arr = oracle.arrays_from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"])
     with B.Graph.from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"]) as g:
-        g.set_options(mode=mode)
+        g.set_options(mode=mode, bottom_up=bottom_up)
         for i, src in enumerate(c["sources"]):
             _check_run(B, oracle, arr, g, src, expect=c["levels"][i])
 
@@ -75,16 +76,45 @@ def test_golden_levels_from_arrays(native, oracle, name):
             _check_run(B, oracle, arr, g, src, expect=c["levels"][i], trace=False)
 
 
+@pytest.mark.parametrize("bottom_up", ["pull", "stream"])
 @pytest.mark.parametrize("w,s", [(512, 8), (1024, 16), (2048, 32), (4096, 8), (96, 7)])
-def test_tile_shapes_scale14(native, oracle, w, s):
+def test_tile_shapes_scale14(native, oracle, w, s, bottom_up):
     import bfs_simd_benchmarks_gb300 as B
     n = 1 << 14
     src, dst = B.gen_rmat(n, 16 * n, seed=1400 + w + s, permute=True)
     arr = oracle.arrays_from_edges(n, src, dst, w, s)
     srcs = B.pick_sources(arr["degrees"], 4, seed=w * 7 + s)
     with B.Graph.from_edges(n, src, dst, w, s) as g:
+        g.set_options(bottom_up=bottom_up)
         for sv in srcs:
             _check_run(B, oracle, arr, g, sv)
+
+
+def test_pull_long_scans_and_queue_overflow(native, oracle):
+    """A graph where many destinations need long in-edge scans (hubs of in-edges
+    reached late) exercises pass 2 and the full-queue fallback of the pull step."""
+    import bfs_simd_benchmarks_gb300 as B
+    rng = np.random.default_rng(5)
+    n = 20000
+    # a chain 0->1->...->199 feeding a fan-out, plus 600 high in-degree vertices whose
+    # in-edges mostly come from vertices reached only at the end of the chain
+    chain = np.arange(199)
+    src = [chain, np.full(2000, 199)]
+    dst = [chain + 1, rng.choice(np.arange(200, n), 2000, replace=False)]
+    hubs = rng.choice(np.arange(200, n), 600, replace=False)
+    for h in hubs:
+        ins = rng.choice(np.arange(200, n), 60, replace=False)
+        src.append(ins)
+        dst.append(np.full(60, h))
+    src = np.concatenate(src).astype(np.uint32)
+    dst = np.concatenate(dst).astype(np.uint32)
+    arr = oracle.arrays_from_edges(n, src, dst, 256, 4)
+    with B.Graph.from_edges(n, src, dst, 256, 4) as g:
+        g.set_options(to_dense_ratio=1000000, to_sparse_ratio=1000000)  # every later step bottom-up
+        lev, par, st = g.run(0)
+        np.testing.assert_array_equal(lev, oracle.bfs_levels(arr, 0))
+        assert oracle.check_parents(arr, 0, lev, par) == 0
+        assert st["dense_steps"] > 0
 
 
 def test_direction_thresholds_do_not_change_levels(native, oracle):
