@@ -47,6 +47,9 @@ __device__ __forceinline__ uint32_t bucket_of(uint32_t deg, const StepParams &p)
 }
 
 constexpr int kTdPerLane = 4;  // candidate edges a lane handles per top-down iteration
+// Medium-degree buckets up to this size join the grid-flat expansion of the
+// large ones (a few chunks); larger ones are spread over CTAs in chunks.
+constexpr uint32_t kFlatMediumMax = 4 * kThreads;
 
 // Next-frontier appends of one warp are staged in a shared-memory buffer per
 // degree bucket and moved to the global queue in blocks, so the queue tails
@@ -79,33 +82,29 @@ __device__ __forceinline__ void wq_flush_all(WarpQ &wq) {
 }
 
 // All 32 lanes of the warp call this with up to kTdPerLane candidate edges
-// u[q] -> v[q] each (has[q] false for an empty slot).  The visited checks,
-// the claiming atomicOr's and the degree loads of the claimed vertices are
-// each issued for all candidates before any result is used, so a lane waits
-// for one round trip per stage rather than one per edge.  Claimed vertices
-// get their level and parent and are staged for the next queue bucket of
-// their out-degree.
+// u[q] -> v[q] each (has[q] false for an empty slot).  Each stage -- the
+// visited pre-load (it keeps already-visited hub destinations off the atomic
+// unit), the claiming atomicOr, the degree load of the claimed -- is issued
+// for all candidates before any result is used, so a lane waits for three
+// round trips per batch of edges, not per edge.
+// Claimed vertices get their level and parent and are staged for the next
+// queue bucket of their out-degree.
 __device__ __forceinline__ void visit_and_append(const bool (&has)[kTdPerLane], const uint32_t (&u)[kTdPerLane],
 		const uint32_t (&v)[kTdPerLane], int32_t next_level, const DevGraph &g, const RunCtx &r, WarpQ &wq,
 		const StepParams &p, ThreadAcc &acc) {
-	bool cand[kTdPerLane];
 	uint32_t word[kTdPerLane];
 #pragma unroll
-	for (int q = 0; q < kTdPerLane; ++q) {
-		cand[q] = has[q];
-		word[q] = cand[q] ? ld_cg(r.vis + (v[q] >> 5)) : 0u;
-	}
+	for (int q = 0; q < kTdPerLane; ++q) word[q] = has[q] ? ld_cg(r.vis + (v[q] >> 5)) : ~0u;
 #pragma unroll
 	for (int q = 0; q < kTdPerLane; ++q) {
 		const uint32_t bit = 1u << (v[q] & 31);
-		if (cand[q] && (word[q] & bit)) cand[q] = false;
-		if (cand[q]) word[q] = atomicOr(r.vis + (v[q] >> 5), bit);
+		if (!(word[q] & bit)) word[q] = atomicOr(r.vis + (v[q] >> 5), bit);
 	}
 	uint32_t deg[kTdPerLane];
 	bool claimed[kTdPerLane];
 #pragma unroll
 	for (int q = 0; q < kTdPerLane; ++q) {
-		claimed[q] = cand[q] && !(word[q] & (1u << (v[q] & 31)));
+		claimed[q] = !(word[q] & (1u << (v[q] & 31)));
 		deg[q] = claimed[q] ? __ldg(g.row_off + v[q] + 1) - __ldg(g.row_off + v[q]) : 0u;
 	}
 	uint32_t cnt[3] = {0, 0, 0};
@@ -181,15 +180,19 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 	bool has[kTdPerLane];
 	uint32_t uu[kTdPerLane], vv[kTdPerLane];
 
-	// Large out-degree: the edges of all large vertices form one flat range
-	// that every warp of the grid shares evenly.  Each CTA stages a chunk of
-	// up to kThreads large vertices with the inclusive prefix of their degrees
-	// in shared memory; a lane finds the owner of its edge by binary search.
-	for (uint32_t c0 = 0; c0 < nL; c0 += kThreads) {
-		const uint32_t cn = min((uint32_t) kThreads, nL - c0);
+	// Large out-degree vertices -- and medium ones when there are few of them
+	// -- are expanded as one flat edge range that every warp of the grid
+	// shares evenly.  Each CTA stages a chunk of up to kThreads such vertices
+	// with the inclusive prefix of their degrees in shared memory; a lane
+	// finds the owner of its edge by binary search.
+	const bool flat_medium = nM <= kFlatMediumMax;
+	const uint32_t nflat = nL + (flat_medium ? nM : 0u);
+	for (uint32_t c0 = 0; c0 < nflat; c0 += kThreads) {
+		const uint32_t cn = min((uint32_t) kThreads, nflat - c0);
 		uint32_t deg = 0, u = 0, beg = 0;
 		if (threadIdx.x < cn) {
-			u = ld_cg(qL + c0 + threadIdx.x);
+			const uint32_t x = c0 + threadIdx.x;
+			u = ld_cg(x < nL ? qL + x : qM + (x - nL));
 			beg = __ldg(g.row_off + u);
 			deg = __ldg(g.row_off + u + 1) - beg;
 		}
@@ -222,10 +225,9 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 		if (blockIdx.x == 0 && threadIdx.x == 0) { acc.td_edges += total; acc.td_vertices += cn; }
 		__syncthreads();
 	}
-	// Medium out-degree: a CTA expands a chunk of up to 32 vertices as one
-	// flat edge list (one vertex per chunk when there are fewer vertices than
-	// CTAs, so every CTA gets work).
-	{
+	// Medium out-degree, many vertices: a CTA expands a chunk of up to 32
+	// vertices as one flat edge list.
+	if (!flat_medium) {
 		const uint32_t chunk = max(1u, min(32u, nM / gridDim.x));
 		const uint32_t nchunks = (nM + chunk - 1) / chunk;
 		for (uint32_t ci = blockIdx.x; ci < nchunks; ci += gridDim.x) {
