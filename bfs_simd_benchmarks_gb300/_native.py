@@ -68,8 +68,30 @@ class Options(C.Structure):
         ("warp_max_degree", C.c_uint32),
         ("cta_max_degree", C.c_uint32),
         ("bottom_up", C.c_uint32),
-        ("reserved", C.c_uint32 * 2),
+        ("batch_planes", C.c_uint32),
+        ("batch_budget_mb", C.c_uint32),
     ]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [
+        ("num_sources", C.c_uint32),
+        ("depth", C.c_uint32),
+        ("push_levels", C.c_uint32),
+        ("status", C.c_int32),
+        ("edges_traversed", C.c_uint64),
+        ("rows_gathered", C.c_uint64),
+        ("planes", C.c_uint32),
+        ("spills", C.c_uint32),
+        ("words_per_vertex", C.c_uint32),
+        ("grid_ctas", C.c_uint32),
+        ("device_ms", C.c_double),
+        ("levels_ms", C.c_double),
+        ("device_bytes", C.c_uint64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Stats(C.Structure):
@@ -138,6 +160,8 @@ _SIGNATURES = [
     ("bfs_run", C.c_int, [C.c_void_p, C.c_uint32, _i32p, _u32p, C.POINTER(Stats)]),
     ("bfs_run_device", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("bfs_last_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    ("bfs_run_batch", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(BatchStats)]),
+    ("bfs_last_batch_stats", C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
     ("bfs_run_noalloc", C.c_int, [C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("bfs_write_level_dump", C.c_int, [C.c_char_p, C.c_uint32, _i32p]),
     ("bfs_tool_csr_tiling", C.c_int, [C.c_char_p, C.c_uint32]),

@@ -10,6 +10,7 @@
 
 #include "internal.h"
 #include "kernels_api.h"
+#include "msbfs.h"
 
 using namespace bfsg;
 
@@ -17,6 +18,8 @@ namespace {
 
 constexpr uint32_t kMaxGroupVertices = 32768;  // shared-memory bitmaps of one column group
 constexpr uint32_t kGroupsPerCta = 1;
+constexpr uint32_t kBatchPushDiv = 16;       // batched levels push while frontier edges < E / 16
+constexpr uint32_t kBatchDefaultPlanes = 32; // level planes when sized from the budget
 
 struct DevBuf {
 	void *p = nullptr;
@@ -58,6 +61,22 @@ struct bfs_graph {
 	bfs_options opt{};
 	uint32_t num_groups = 0;
 	uint64_t packed_words = 0;
+	// batched traversal state, allocated by the first bfs_run_batch
+	struct Batch {
+		uint32_t k_alloc = 0;        // words per vertex the buffers hold
+		uint32_t wanted_alloc = 0;   // planes asked for when they were allocated
+		size_t hist_bytes = 0;
+		MsArgs args{};
+		uint32_t *d_sources = nullptr;
+		MsControl *h_ctl = nullptr;  // pinned
+		cudaEvent_t e0 = nullptr, e1 = nullptr;
+		cudaStream_t stream = nullptr;
+		uint32_t num_sources = 0;
+		int grid = 0;
+		bool have_run = false, fresh = false;
+		size_t bytes = 0;
+		std::vector<DevBuf> bufs;
+	} mb;
 	std::mutex mu;
 };
 
@@ -88,7 +107,21 @@ template <class T> int dev_upload(bfs_graph *g, const T **out, const std::vector
 	return BFS_OK;
 }
 
+void release_batch(bfs_graph *g) {
+	for (auto &b : g->mb.bufs) cudaFree(b.p);
+	g->mb.bufs.clear();
+	g->mb.bytes = 0;
+	g->mb.k_alloc = 0;
+	g->mb.hist_bytes = 0;
+}
+
 void release(bfs_graph *g) {
+	release_batch(g);
+	if (g->mb.h_ctl) cudaFreeHost(g->mb.h_ctl);
+	if (g->mb.e0) cudaEventDestroy(g->mb.e0);
+	if (g->mb.e1) cudaEventDestroy(g->mb.e1);
+	g->mb.h_ctl = nullptr;
+	g->mb.e0 = g->mb.e1 = nullptr;
 	for (auto &b : g->bufs) cudaFree(b.p);
 	g->bufs.clear();
 	if (g->h_stats) cudaFreeHost(g->h_stats);
@@ -109,6 +142,8 @@ void default_options(bfs_options *o) {
 	o->warp_max_degree = 32;
 	o->cta_max_degree = 4096;
 	o->bottom_up = BFS_BU_PULL;
+	o->batch_planes = 0;
+	o->batch_budget_mb = 40960;
 }
 
 // Builds the device copy of a validated host graph.
@@ -380,6 +415,143 @@ int collect_stats(bfs_graph *g, bfs_stats *out) {
 	return s.status;
 }
 
+template <class T> int batch_alloc(bfs_graph *g, T **out, size_t count) {
+	size_t bytes = std::max<size_t>(sizeof(T) * count, 16);
+	void *p = nullptr;
+	if (cudaMalloc(&p, bytes) != cudaSuccess) {
+		cudaGetLastError();
+		return BFS_ENOMEM;
+	}
+	g->mb.bufs.push_back({p, bytes});
+	g->mb.bytes += bytes;
+	*out = (T *) p;
+	return BFS_OK;
+}
+
+// Level planes a batch of K words per vertex asks for.
+uint32_t batch_planes_wanted(const bfs_graph *g, uint32_t K) {
+	if (g->opt.batch_planes) return g->opt.batch_planes;
+	const size_t plane = (size_t) g->n * K * 8;
+	const size_t budget = (size_t) g->opt.batch_budget_mb << 20;
+	return (uint32_t) std::max<size_t>(2, std::min<size_t>(kBatchDefaultPlanes, budget / std::max<size_t>(plane, 1)));
+}
+
+// Makes the batch buffers hold K words per vertex and `planes` level planes;
+// returns the planes the call will use.
+int batch_prepare(bfs_graph *g, uint32_t K, uint32_t *planes_out) {
+	auto &b = g->mb;
+	const size_t plane = (size_t) g->n * K * 8;
+	uint32_t planes = batch_planes_wanted(g, K);
+	if (!b.h_ctl) {
+		if (cudaMallocHost(&b.h_ctl, sizeof(MsControl)) != cudaSuccess) return BFS_ENOMEM;
+		if (cudaEventCreate(&b.e0) != cudaSuccess || cudaEventCreate(&b.e1) != cudaSuccess) return BFS_ECUDA;
+	}
+	const uint32_t have = b.k_alloc >= K ? (uint32_t) std::min<size_t>(kMsMaxLevel + 1, b.hist_bytes / plane) : 0;
+	// reuse when the planes fit, or when this is the shape the buffers were
+	// sized for and memory capped them
+	if (have >= planes || (have >= 2 && b.k_alloc == K && b.wanted_alloc == planes)) {
+		*planes_out = std::min(planes, have);
+		return BFS_OK;
+	}
+	// (re)allocate: wait for earlier batches that still use the buffers
+	if (b.have_run && cudaEventSynchronize(b.e1) != cudaSuccess) return BFS_ECUDA;
+	release_batch(g);
+	const size_t fixed = plane + (size_t) g->n * (3 + 4 + 8) + sizeof(MsControl) + 4 * BFS_BATCH_MAX_SOURCES;
+	size_t free_b = 0, total_b = 0;
+	if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return BFS_ECUDA;
+	const size_t usable = free_b > (size_t) 1 << 30 ? free_b - ((size_t) 1 << 30) : 0;  // leave 1 GiB
+	if (usable < fixed + 2 * plane) return BFS_ENOMEM;
+	if (fixed + planes * plane > usable) {
+		if (g->opt.batch_planes) return BFS_ENOMEM;  // an explicit plane count that does not fit
+		planes = (uint32_t) ((usable - fixed) / plane);
+	}
+	MsArgs &a = b.args;
+	int st;
+	if ((st = batch_alloc(g, &a.vis, (size_t) g->n * K))) return st;
+	if ((st = batch_alloc(g, &a.hist, (size_t) planes * g->n * K))) return st;
+	if ((st = batch_alloc(g, &a.act[0], g->n))) return st;
+	if ((st = batch_alloc(g, &a.act[1], g->n))) return st;
+	if ((st = batch_alloc(g, &a.touched, g->n))) return st;
+	if ((st = batch_alloc(g, &a.seed_flag, g->n))) return st;
+	if ((st = batch_alloc(g, &a.queue[0], g->n))) return st;
+	if ((st = batch_alloc(g, &a.queue[1], g->n))) return st;
+	if ((st = batch_alloc(g, &a.ctl, 1))) return st;
+	if ((st = batch_alloc(g, &b.d_sources, BFS_BATCH_MAX_SOURCES))) return st;
+	b.k_alloc = K;
+	b.wanted_alloc = batch_planes_wanted(g, K);
+	b.hist_bytes = (size_t) planes * plane;
+	*planes_out = planes;
+	return BFS_OK;
+}
+
+int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *levels, cudaStream_t st) {
+	if (g->host_only) return BFS_EUNSUPPORTED;
+	if (!sources || !levels || ns == 0 || ns > BFS_BATCH_MAX_SOURCES) return BFS_EARG;
+	for (uint32_t i = 0; i < ns; ++i)
+		if (sources[i] >= g->n) return BFS_EARG;
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	const uint32_t K = (ns + 63) / 64;
+	uint32_t planes = 0;
+	int rc = batch_prepare(g, K, &planes);
+	if (rc) return rc;
+	auto &b = g->mb;
+	MsArgs a = b.args;
+	a.n = g->n;
+	a.m = (uint32_t) g->m;
+	a.K = K;
+	a.last_bits = ns - 64 * (K - 1);
+	a.planes = planes;
+	a.push_div = kBatchPushDiv;
+	a.vec_out = (g->n % 16 == 0 && ((uintptr_t) levels % 16) == 0) ? 1u : 0u;
+	a.row_off = g->dg.row_off;
+	a.col = g->dg.col;
+	a.in_off = g->dg.in_off;
+	a.in_src = g->dg.in_src;
+	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
+	// pageable source: the copy has left `sources` when the call returns
+	if (cudaMemcpyAsync(b.d_sources, sources, sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, st) != cudaSuccess)
+		return BFS_ECUDA;
+	if ((rc = ms_launch(a, b.d_sources, ns, levels, g->num_sms, st, &b.grid))) return rc;
+	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
+	b.args.planes = planes;
+	b.args.K = K;
+	b.num_sources = ns;
+	b.stream = st;
+	b.have_run = true;
+	b.fresh = false;
+	return BFS_OK;
+}
+
+int collect_batch_stats(bfs_graph *g, bfs_batch_stats *out) {
+	auto &b = g->mb;
+	if (!b.have_run) return BFS_EARG;
+	if (!b.fresh) {
+		if (cudaMemcpyAsync(b.h_ctl, b.args.ctl, sizeof(MsControl), cudaMemcpyDeviceToHost, b.stream) != cudaSuccess ||
+				cudaStreamSynchronize(b.stream) != cudaSuccess)
+			return BFS_ECUDA;
+		b.fresh = true;
+	}
+	const MsControl &c = *b.h_ctl;
+	bfs_batch_stats s{};
+	s.num_sources = b.num_sources;
+	s.depth = c.stats.depth;
+	s.push_levels = c.stats.push_levels;
+	s.status = c.err;
+	s.edges_traversed = c.stats.traversed;
+	s.rows_gathered = c.stats.edges;
+	s.planes = b.args.planes;
+	s.spills = c.stats.spills;
+	s.words_per_vertex = b.args.K;
+	s.grid_ctas = (uint32_t) b.grid;
+	float ms = 0;
+	cudaEventElapsedTime(&ms, b.e0, b.e1);
+	s.device_ms = ms;
+	s.levels_ms = c.stats.t_levels1 > c.stats.t_levels0 ? (c.stats.t_levels1 - c.stats.t_levels0) * 1e-6 : 0.0;
+	s.device_bytes = b.bytes;
+	if (out) *out = s;
+	return s.status;
+}
+
 } // namespace
 
 extern "C" {
@@ -517,7 +689,8 @@ int bfs_options_default(bfs_options *opt) {
 int bfs_set_options(bfs_graph *g, const bfs_options *opt) {
 	if (!g || !opt) return BFS_EARG;
 	if (opt->mode > BFS_MODE_STEPWISE || opt->bottom_up > BFS_BU_STREAM || opt->to_dense_ratio == 0 || opt->to_sparse_ratio == 0 ||
-			opt->warp_max_degree == 0 || opt->cta_max_degree < opt->warp_max_degree)
+			opt->warp_max_degree == 0 || opt->cta_max_degree < opt->warp_max_degree || opt->batch_planes == 1 ||
+			opt->batch_planes > kMsMaxLevel + 1 || (opt->batch_planes == 0 && opt->batch_budget_mb == 0))
 		return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);
 	g->opt = *opt;
@@ -554,6 +727,21 @@ int bfs_last_stats(bfs_graph *g, bfs_stats *stats) {
 	if (!g) return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);
 	return collect_stats(g, stats);
+}
+
+int bfs_run_batch(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, uint8_t *levels, void *stream,
+		bfs_batch_stats *stats) {
+	if (!g) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	int st = run_batch_impl(g, sources, num_sources, levels, (cudaStream_t) stream);
+	if (st || !stats) return st;
+	return collect_batch_stats(g, stats);
+}
+
+int bfs_last_batch_stats(bfs_graph *g, bfs_batch_stats *stats) {
+	if (!g) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	return collect_batch_stats(g, stats);
 }
 
 } // extern "C"

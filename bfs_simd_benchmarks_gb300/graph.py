@@ -113,7 +113,7 @@ class Graph:
     def options(self) -> dict:
         o = N.Options()
         N.check(N.load().bfs_get_options(self._h, C.byref(o)), "bfs_get_options")
-        return {k: getattr(o, k) for k, _ in N.Options._fields_ if k != "reserved"}
+        return {k: getattr(o, k) for k, _ in N.Options._fields_}
 
     def set_options(self, **kw) -> None:
         o = N.Options()
@@ -148,6 +148,29 @@ class Graph:
     def last_stats(self) -> dict:
         st = N.Stats()
         N.check(N.load().bfs_last_stats(self._h, C.byref(st)), "bfs_last_stats")
+        return st.as_dict()
+
+    def run_batch_device(self, sources, levels_ptr: int, stream: int = 0, stats: bool = False):
+        """Enqueues a batched traversal writing uint8 levels [len(sources)][N] at a device pointer."""
+        src = _u32(sources)
+        st = N.BatchStats() if stats else None
+        N.check(N.load().bfs_run_batch(self._h, _ptr(src, C.c_uint32), src.size, C.c_void_p(levels_ptr),
+                                       C.c_void_p(stream) if stream else None,
+                                       C.byref(st) if st is not None else None), "bfs_run_batch")
+        return st.as_dict() if st is not None else None
+
+    def run_batch(self, sources):
+        """Levels of every source at once: a torch uint8 CUDA tensor [len(sources), N]
+        (255 = unreached) and the batch stats."""
+        import torch
+        src = _u32(sources)
+        out = torch.empty((src.size, self.num_vertices), dtype=torch.uint8, device="cuda")
+        stats = self.run_batch_device(src, out.data_ptr(), torch.cuda.current_stream().cuda_stream, stats=True)
+        return out, stats
+
+    def last_batch_stats(self) -> dict:
+        st = N.BatchStats()
+        N.check(N.load().bfs_last_batch_stats(self._h, C.byref(st)), "bfs_last_batch_stats")
         return st.as_dict()
 
 

@@ -38,7 +38,7 @@ enum bfs_status {
 	BFS_EBUDGET = 5,      /* admission refused: over the device-memory budget */
 	BFS_ETIMEOUT = 6,     /* a device-side wait hit its bound and returned */
 	BFS_ECUDA = 7,        /* a CUDA runtime call failed */
-	BFS_EUNSUPPORTED = 8, /* the tile width / stripe length cannot be packed */
+	BFS_EUNSUPPORTED = 8, /* tile shape that cannot be packed; batched level above 254 */
 	BFS_ENODEV = 9        /* no CUDA device is available */
 };
 
@@ -124,7 +124,8 @@ typedef struct bfs_options {
 	uint32_t warp_max_degree;  /* top-down: degree <= this -> warp-cooperative gather */
 	uint32_t cta_max_degree;   /* top-down: degree <= this -> one CTA per vertex; above -> grid-strided */
 	uint32_t bottom_up;        /* BFS_BU_PULL or BFS_BU_STREAM */
-	uint32_t reserved[2];
+	uint32_t batch_planes;     /* bfs_run_batch: level planes (2..255); 0 = from batch_budget_mb, at most 32 */
+	uint32_t batch_budget_mb;  /* bfs_run_batch: HBM budget of the level planes in MiB (default 40960) */
 } bfs_options;
 
 /* Bottom-up step variants.  PULL: every unvisited destination of a column
@@ -186,6 +187,42 @@ int bfs_run(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, b
  */
 int bfs_run_device(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, void *stream);
 int bfs_last_stats(bfs_graph *g, bfs_stats *stats);
+
+/* ---- batched traversal (no counterpart in the reference) --------------- */
+#define BFS_BATCH_MAX_SOURCES 4096
+
+typedef struct bfs_batch_stats {
+	uint32_t num_sources;
+	uint32_t depth;            /* the deepest source's max level + 1 */
+	uint32_t push_levels;      /* levels expanded top-down (the others pulled bottom-up) */
+	int32_t status;            /* BFS_OK, BFS_ETIMEOUT, or BFS_EUNSUPPORTED (a level above 254) */
+	uint64_t edges_traversed;  /* sum over the sources of the out-degrees of the vertices each reached */
+	uint64_t rows_gathered;    /* in-neighbour frontier rows read by pull levels */
+	uint32_t planes;           /* level planes held (levels kept before an early output pass) */
+	uint32_t spills;           /* early output passes (traversal deeper than the planes) */
+	uint32_t words_per_vertex; /* 64-bit words per vertex, ceil(num_sources / 64) */
+	uint32_t grid_ctas;
+	double device_ms;          /* the whole launch (CUDA events) */
+	double levels_ms;          /* the levels alone (device clock) */
+	uint64_t device_bytes;     /* HBM held by the batch state */
+} bfs_batch_stats;
+
+/*
+ * Traverses from num_sources (1..BFS_BATCH_MAX_SOURCES) sources at once and
+ * writes uint8 levels[num_sources][N] (caller-owned device memory, source-major,
+ * 255 = unreached) on `stream`.  Row i equals bfs_run(g, sources[i])'s levels
+ * (graph_prepare's h_cost, apps/bfs_simd/bfs.cpp:753-963) wherever those are
+ * at most 254; a traversal with a level above 254 reports BFS_EUNSUPPORTED.
+ * Sources may repeat.  `sources` is host memory.  With stats NULL the call
+ * only enqueues work; bfs_last_batch_stats waits for it and reads them.  The
+ * batch state -- about (planes + 1) * N * ceil(num_sources / 64) * 8 bytes,
+ * planes from bfs_options.batch_planes / batch_budget_mb -- is allocated by
+ * the first call that needs it and kept with the graph; calls on one graph
+ * must not overlap on the GPU.
+ */
+int bfs_run_batch(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, uint8_t *levels, void *stream,
+		bfs_batch_stats *stats);
+int bfs_last_batch_stats(bfs_graph *g, bfs_batch_stats *stats);
 
 /* ---- allocation-free traversal (no counterpart in the reference) -------- */
 #define BFS_NOALLOC_MAX_VERTICES (1u << 20)
