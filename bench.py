@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sources", type=int, default=0, help="use only the first K sources (profiling runs)")
+    ap.add_argument("--batch-workload", default="rmat22", help="graph of the batched measurement ('none' skips it)")
+    ap.add_argument("--batch-sources", type=int, default=4096)
+    ap.add_argument("--batch-steps", type=int, default=5)
     return ap.parse_args()
 
 
@@ -215,6 +218,87 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def bench_batched(args, torch, dev):
+    """Batched multi-source BFS (bfs_run_batch): every step traverses all the
+    sources at once and writes uint8 levels [sources][N] into HBM.  Compared
+    with the single-source kernel on the same graph (the plain GPU BFS)."""
+    import bfs_simd_benchmarks_gb300 as B
+    from bfs_simd_benchmarks_gb300 import workloads
+    wl = workloads.get(args.batch_workload)
+    t0 = time.perf_counter()
+    src, dst = wl.edges()
+    g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s)
+    build_s = time.perf_counter() - t0
+    del src, dst
+    deg = g.degrees()
+    sources = wl.sources(deg, args.batch_sources)
+    out = torch.empty((len(sources), wl.n), dtype=torch.uint8, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    runs = []
+    for i in range(max(3, args.warmup) + args.batch_steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.run_batch_device(sources, out.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+        st = g.last_batch_stats()
+        if st["status"] != 0:
+            raise RuntimeError(f"batched traversal status {st['status']}")
+        if i >= max(3, args.warmup):
+            runs.append((e0.elapsed_time(e1), st))
+    ms = [r[0] for r in runs]
+    edges = runs[0][1]["edges_traversed"]
+    gteps = edges * len(ms) / (sum(ms) / 1e3) / 1e9
+    # the single-source kernel on the same graph, a sample of the same sources
+    lev = torch.empty(wl.n, dtype=torch.int32, device=dev)
+    single_ms, single_edges, rows_ok = [], 0, 0
+    check = list(range(0, len(sources), max(1, len(sources) // 8)))[:8]
+    host = out.cpu() if len(sources) * wl.n <= (1 << 31) else None
+    for j, s in enumerate(sources[:64]):
+        with torch.cuda.stream(stream):
+            flush.fill_(j & 0xFF)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.run_device(int(s), lev.data_ptr(), 0, stream.cuda_stream)
+            e1.record(stream)
+        st = g.last_stats()
+        single_ms.append(e0.elapsed_time(e1))
+        single_edges += st["edges_traversed"]
+    for i in check:
+        with torch.cuda.stream(stream):
+            g.run_device(int(sources[i]), lev.data_ptr(), 0, stream.cuda_stream)
+        g.last_stats()
+        ref = lev.cpu().numpy()
+        ref = np.where(ref < 0, 255, ref).astype(np.uint8)
+        row = host[i].numpy() if host is not None else out[i].cpu().numpy()
+        rows_ok += int(np.array_equal(row, ref))
+    single_gteps = single_edges / (sum(single_ms) / 1e3) / 1e9
+    st = runs[-1][1]
+    res = {
+        "workload": wl.describe() | {"sources": len(sources)}, "graph_build_s": round(build_s, 2),
+        "gteps": gteps, "ms_per_batch_mean": statistics.mean(ms), "ms_per_batch_p50": statistics.median(ms),
+        "levels_ms_mean": statistics.mean(r[1]["levels_ms"] for r in runs),
+        "edges_traversed_per_batch": edges, "depth": st["depth"], "push_levels": st["push_levels"],
+        "planes": st["planes"], "spills": st["spills"], "rows_gathered": st["rows_gathered"],
+        "level_ms": st["level_ms"], "level_frontier": st["level_frontier"], "level_push": st["level_push"],
+        "grid_ctas": st["grid_ctas"], "batch_state_bytes": st["device_bytes"],
+        "output_bytes": len(sources) * wl.n,
+        "plain_gpu_bfs": {"gteps": single_gteps, "ms_per_traversal_mean": statistics.mean(single_ms),
+                          "sources": len(single_ms), "kernel": "k_bfs_persistent (single source)"},
+        "speedup_vs_plain_gpu_bfs": gteps / single_gteps,
+        "parity": f"batched rows equal single-source levels on {rows_ok}/{len(check)} sources checked",
+        "steps": len(ms), "l2": "flushed (256 MiB write) before every batch; batch state far above L2",
+    }
+    g.close()
+    del out
+    torch.cuda.empty_cache()
+    return res
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -316,6 +400,10 @@ def main():
     e2e_s = time.perf_counter() - t0
     e2e_value = e2e_edges / e2e_s / 1e9
 
+    batched = None
+    if args.batch_workload != "none" and world == 1:
+        batched = bench_batched(args, torch, dev)
+
     cpu = None
     parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -362,6 +450,7 @@ def main():
             "clocks": clocks,
             "cpu_baseline": cpu,
             "parity": parity,
+            "batched": batched,
         }
         print(json.dumps(line))
     if world > 1:

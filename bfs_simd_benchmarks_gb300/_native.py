@@ -36,6 +36,7 @@ BFS_RMAT_NO_SELF_LOOPS = 0x1
 BFS_RMAT_DEDUP = 0x2
 BFS_RMAT_PERMUTE = 0x4
 
+BFS_BATCH_TRACE_LEVELS = 64
 BFS_TRACE_MAX = 256
 
 _u32p = C.POINTER(C.c_uint32)
@@ -88,10 +89,18 @@ class BatchStats(C.Structure):
         ("device_ms", C.c_double),
         ("levels_ms", C.c_double),
         ("device_bytes", C.c_uint64),
+        ("level_ms", C.c_float * BFS_BATCH_TRACE_LEVELS),
+        ("level_frontier", C.c_uint32 * BFS_BATCH_TRACE_LEVELS),
+        ("level_push", C.c_uint8 * BFS_BATCH_TRACE_LEVELS),
     ]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("level_")}
+        k = min(self.depth, BFS_BATCH_TRACE_LEVELS)
+        d["level_ms"] = [round(x, 4) for x in self.level_ms[:k]]
+        d["level_frontier"] = list(self.level_frontier[:k])
+        d["level_push"] = list(self.level_push[:k])
+        return d
 
 
 class Stats(C.Structure):

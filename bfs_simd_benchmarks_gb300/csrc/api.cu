@@ -61,6 +61,9 @@ struct bfs_graph {
 	bfs_options opt{};
 	uint32_t num_groups = 0;
 	uint64_t packed_words = 0;
+	// batched pull: destinations with many in-edges, cut into chunks
+	const uint32_t *ms_in_big = nullptr, *ms_chunk_v = nullptr, *ms_chunk_beg = nullptr;
+	uint32_t ms_nbig_in = 0, ms_nchunks = 0;
 	// batched traversal state, allocated by the first bfs_run_batch
 	struct Batch {
 		uint32_t k_alloc = 0;        // words per vertex the buffers hold
@@ -216,6 +219,21 @@ int upload(bfs_graph *g, HostGraph &h) {
 			for (uint32_t e = h.row_off[u]; e < h.row_off[u + 1]; ++e) in_src[fill[h.csr_dst[e]]++] = u;
 		if ((st = dev_upload(g, &d.in_off, in_off))) return st;
 		if ((st = dev_upload(g, &d.in_src, in_src))) return st;
+		// batched pull: destinations with many in-edges and their chunks
+		std::vector<uint32_t> in_big, chunk_v, chunk_beg;
+		for (uint32_t v = 0; v < h.n; ++v) {
+			if (in_off[v + 1] - in_off[v] <= kMsPullBig) continue;
+			in_big.push_back(v);
+			for (uint32_t b = in_off[v]; b < in_off[v + 1]; b += kMsChunk) {
+				chunk_v.push_back(v);
+				chunk_beg.push_back(b);
+			}
+		}
+		g->ms_nbig_in = (uint32_t) in_big.size();
+		g->ms_nchunks = (uint32_t) chunk_v.size();
+		if ((st = dev_upload(g, &g->ms_in_big, in_big))) return st;
+		if ((st = dev_upload(g, &g->ms_chunk_v, chunk_v))) return st;
+		if ((st = dev_upload(g, &g->ms_chunk_beg, chunk_beg))) return st;
 	}
 
 	// Run context.
@@ -456,7 +474,7 @@ int batch_prepare(bfs_graph *g, uint32_t K, uint32_t *planes_out) {
 	// (re)allocate: wait for earlier batches that still use the buffers
 	if (b.have_run && cudaEventSynchronize(b.e1) != cudaSuccess) return BFS_ECUDA;
 	release_batch(g);
-	const size_t fixed = plane + (size_t) g->n * (3 + 4 + 8) + sizeof(MsControl) + 4 * BFS_BATCH_MAX_SOURCES;
+	const size_t fixed = plane + (size_t) g->n * (16 + 1 + 4 + 8) + sizeof(MsControl) + 4 * BFS_BATCH_MAX_SOURCES;
 	size_t free_b = 0, total_b = 0;
 	if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return BFS_ECUDA;
 	const size_t usable = free_b > (size_t) 1 << 30 ? free_b - ((size_t) 1 << 30) : 0;  // leave 1 GiB
@@ -507,6 +525,11 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 	a.col = g->dg.col;
 	a.in_off = g->dg.in_off;
 	a.in_src = g->dg.in_src;
+	a.in_big = g->ms_in_big;
+	a.chunk_v = g->ms_chunk_v;
+	a.chunk_beg = g->ms_chunk_beg;
+	a.nbig_in = g->ms_nbig_in;
+	a.nchunks = g->ms_nchunks;
 	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
 	// pageable source: the copy has left `sources` when the call returns
 	if (cudaMemcpyAsync(b.d_sources, sources, sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, st) != cudaSuccess)
@@ -548,6 +571,13 @@ int collect_batch_stats(bfs_graph *g, bfs_batch_stats *out) {
 	s.device_ms = ms;
 	s.levels_ms = c.stats.t_levels1 > c.stats.t_levels0 ? (c.stats.t_levels1 - c.stats.t_levels0) * 1e-6 : 0.0;
 	s.device_bytes = b.bytes;
+	const uint32_t nl = std::min<uint32_t>(c.stats.depth, kMsTraceLevels);
+	for (uint32_t l = 0; l < nl; ++l) {
+		const unsigned long long t0 = c.stats.t_level[l], t1 = c.stats.t_level[l + 1];
+		s.level_ms[l] = (t0 && t1 > t0) ? (float) ((t1 - t0) * 1e-6) : 0.f;
+		s.level_frontier[l] = c.stats.frontier[l];
+		s.level_push[l] = c.stats.push[l];
+	}
 	if (out) *out = s;
 	return s.status;
 }

@@ -8,7 +8,8 @@
 //   vis[v][K]          sources that have reached v
 //   hist[p][v][K]      sources that reached v first at level base + p; the
 //                      plane of level L is the frontier that level L expands
-//   act[L&1][v]        v has any bit in the plane of level L
+//   act[L&1][v]        bit k: word k of v's row in the plane of level L is
+//                      non-zero (the frontier's vertex set and which rows to read)
 //   queue[L&1]         the frontier's vertices: degree <= kMsBig from the
 //                      front, higher degree from the back
 // A level is expanded either
@@ -17,8 +18,10 @@
 //     every out-neighbour's next words (64-bit atomics); a high-degree vertex
 //     has its edges spread over every warp of the grid; or
 //   - pull (bottom-up) once it holds many: a warp owns a destination, gathers
-//     the words of its active in-neighbours and stops as soon as every source
-//     has reached it (per-destination early exit).
+//     the non-zero words of its frontier in-neighbours that the destination
+//     still lacks and stops as soon as every source has reached it
+//     (per-destination early exit); destinations with many in-edges are cut
+//     into chunks that warps all over the grid gather and OR together.
 // Everything -- clearing, seeding, all levels, the output and the edge count
 // -- runs in one cooperative launch, levels separated by a bounded-spin grid
 // barrier.  The output pass turns planes into uint8 levels [source][vertex]
@@ -39,6 +42,7 @@ constexpr int kMsThreads = 512;
 constexpr int kMsWarps = kMsThreads / 32;
 constexpr uint32_t kMsWq = 64;          // per-warp staged queue appends (pull)
 constexpr uint32_t kMsBig = 1024;       // push: higher-degree vertices are spread over the grid
+constexpr int kMsGather = 4;            // pull: frontier rows gathered per round
 constexpr uint32_t kEmitWords = 8;      // output tile: 8 words (512 sources) ...
 constexpr uint32_t kEmitRows = kEmitWords * 64;
 constexpr uint32_t kEmitV = 64;         // ... x 64 vertices
@@ -74,13 +78,14 @@ __device__ __forceinline__ void ms_append(const MsArgs &a, MsCounters *cn, uint3
 
 // Push: ORs u's non-zero frontier words into the next words of its out-edges
 // [beg + first, end), taking 32 edges per warp step of `step`.  Warp-uniform.
-__device__ __forceinline__ void ms_push_edges(const MsArgs &a, const uint64_t *cur, uint64_t *nxt, uint32_t u,
-		uint32_t beg, uint32_t end, uint32_t first, uint32_t step) {
+__device__ __forceinline__ void ms_push_edges(const MsArgs &a, const uint64_t *cur, const uint64_t *actc,
+		uint64_t *nxt, uint32_t u, uint32_t beg, uint32_t end, uint32_t first, uint32_t step) {
 	const uint32_t K = a.K;
 	const unsigned lane = lane_id();
-	const uint64_t w0 = lane < K ? ld_cg64(cur + (size_t) u * K + lane) : 0ull;
-	const uint64_t w1 = lane + 32 < K ? ld_cg64(cur + (size_t) u * K + lane + 32) : 0ull;
-	const uint32_t nz0 = __ballot_sync(kFull, w0 != 0ull), nz1 = __ballot_sync(kFull, w1 != 0ull);
+	const uint64_t um = ld_cg64(actc + u);  // which of u's words are non-zero
+	const uint32_t nz0 = (uint32_t) um, nz1 = (uint32_t) (um >> 32);
+	const uint64_t w0 = (nz0 >> lane) & 1u ? ld_cg64(cur + (size_t) u * K + lane) : 0ull;
+	const uint64_t w1 = (nz1 >> lane) & 1u ? ld_cg64(cur + (size_t) u * K + lane + 32) : 0ull;
 	for (uint32_t e0 = beg + first; e0 < end; e0 += step) {
 		const uint32_t e = e0 + lane;
 		const bool ok = e < end;
@@ -102,16 +107,22 @@ __device__ __forceinline__ void ms_push_edges(const MsArgs &a, const uint64_t *c
 
 __device__ void ms_push(const MsArgs &a, uint32_t lvl, const uint64_t *cur, uint64_t *nxt, uint32_t nq, uint32_t nb) {
 	const uint32_t *q = a.queue[lvl & 1];
+	const uint64_t *actc = a.act[lvl & 1];
 	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
 	const uint32_t nwarps = gridDim.x * kMsWarps;
 	for (uint32_t i = gwarp; i < nq; i += nwarps) {
 		const uint32_t u = ld_cg(q + i);
-		ms_push_edges(a, cur, nxt, u, __ldg(a.row_off + u), __ldg(a.row_off + u + 1), 0, 32);
+		ms_push_edges(a, cur, actc, nxt, u, __ldg(a.row_off + u), __ldg(a.row_off + u + 1), 0, 32);
 	}
 	for (uint32_t i = 0; i < nb; ++i) {
 		const uint32_t u = ld_cg(q + a.n - 1 - i);
-		ms_push_edges(a, cur, nxt, u, __ldg(a.row_off + u), __ldg(a.row_off + u + 1), gwarp * 32, nwarps * 32);
+		ms_push_edges(a, cur, actc, nxt, u, __ldg(a.row_off + u), __ldg(a.row_off + u + 1), gwarp * 32, nwarps * 32);
 	}
+}
+
+// The next-frontier mask of a row whose new words lanes hold (word l, l + 32).
+__device__ __forceinline__ uint64_t row_mask(uint64_t n0, uint64_t n1) {
+	return (uint64_t) __ballot_sync(kFull, n0 != 0ull) | ((uint64_t) __ballot_sync(kFull, n1 != 0ull) << 32);
 }
 
 // After a push level: the OR'ed words lose the bits already visited, the rest
@@ -121,7 +132,7 @@ __device__ void ms_push_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, uns
 	const uint32_t K = a.K;
 	const unsigned lane = lane_id();
 	uint32_t *qn = a.queue[(lvl + 1) & 1];
-	uint8_t *actn = a.act[(lvl + 1) & 1];
+	uint64_t *actn = a.act[(lvl + 1) & 1];
 	MsCounters *cn = &a.ctl->ctr[(lvl + 1) % 3];
 	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
 	const uint32_t nwarps = gridDim.x * kMsWarps;
@@ -132,24 +143,26 @@ __device__ void ms_push_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, uns
 		for (uint32_t tm = __ballot_sync(kFull, t); tm; tm &= tm - 1) {
 			const int j = __ffs(tm) - 1;
 			const size_t row = (size_t) (vb + j) * K;
-			bool any = false;
-			for (uint32_t k = lane; k < K; k += 32) {
+			uint64_t nw[2] = {0ull, 0ull};
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const uint32_t k = lane + 32 * h;
+				if (k >= K) continue;
 				const uint64_t w = ld_cg64(nxt + row + k);
 				if (!w) continue;
 				const uint64_t vv = ld_cg64(a.vis + row + k);
-				const uint64_t nw = w & ~vv;
-				if (nw != w) nxt[row + k] = nw;
-				if (nw) { a.vis[row + k] = vv | nw; any = true; }
+				nw[h] = w & ~vv;
+				if (nw[h] != w) nxt[row + k] = nw[h];
+				if (nw[h]) a.vis[row + k] = vv | nw[h];
 			}
-			if (__any_sync(kFull, any)) anym |= 1u << j;
+			const uint64_t mask = row_mask(nw[0], nw[1]);
+			if (lane == 0) actn[vb + j] = mask;
+			if (mask) anym |= 1u << j;
 		}
 		if (t) a.touched[v] = 0;
+		else if (v < a.n) actn[v] = 0;
 		const bool any = (anym >> lane) & 1u;
-		uint32_t d = 0;
-		if (v < a.n) {
-			actn[v] = any ? 1 : 0;
-			if (any) d = deg_of(a, v);
-		}
+		const uint32_t d = any ? deg_of(a, v) : 0u;
 		ms_append(a, cn, qn, v, any && d <= kMsBig, any && d > kMsBig);
 		actdeg += d;
 	}
@@ -169,72 +182,98 @@ __device__ __forceinline__ void ms_wq_flush(MsCounters *cn, uint32_t *qn, uint32
 	wn = 0;
 }
 
-// Pull: a warp per destination, lane l owns words l and l + 32.
+// The bits a complete word of lane's word (lane + 32 * h) holds.
+struct FullMask {
+	uint64_t f0, f1;
+	__device__ __forceinline__ FullMask(const MsArgs &a, unsigned lane) {
+		const uint64_t last = a.last_bits == 64 ? ~0ull : ((1ull << a.last_bits) - 1);
+		f0 = lane < a.K ? (lane == a.K - 1 ? last : ~0ull) : 0ull;
+		f1 = lane + 32 < a.K ? (lane + 32 == a.K - 1 ? last : ~0ull) : 0ull;
+	}
+	__device__ __forceinline__ bool complete(uint64_t x0, uint64_t x1) const {
+		return __all_sync(kFull, (x0 & f0) == f0 && (x1 & f1) == f1);
+	}
+};
+
+// ORs into acc the frontier words of the in-neighbours in [beg, end) until
+// every source has reached the destination.  Only words that are non-zero in
+// the neighbour's row and still incomplete in the destination's are read.
+// Returns true when it stopped early.  Warp-uniform.
+__device__ __forceinline__ bool ms_gather(const MsArgs &a, const uint64_t *cur, const uint64_t *actc, uint32_t beg,
+		uint32_t end, const FullMask &fm, uint64_t vis0, uint64_t vis1, uint64_t &acc0, uint64_t &acc1,
+		unsigned long long &gathered) {
+	const uint32_t K = a.K;
+	const unsigned lane = lane_id();
+	bool done = false;
+	for (uint32_t e0 = beg; e0 < end && !done; e0 += 32) {
+		const uint32_t e = e0 + lane;
+		const uint32_t u = e < end ? __ldg(a.in_src + e) : 0u;
+		const uint64_t um = e < end ? ld_cg64(actc + u) : 0ull;
+		uint32_t lm = __ballot_sync(kFull, um != 0ull);
+		while (lm && !done) {
+			const bool need0 = ((acc0 | vis0) & fm.f0) != fm.f0;
+			const bool need1 = ((acc1 | vis1) & fm.f1) != fm.f1;
+			uint64_t g0[kMsGather], g1[kMsGather];
+			int cnt = 0;
+#pragma unroll
+			for (int t = 0; t < kMsGather; ++t) {
+				uint32_t ut = 0;
+				uint64_t mt = 0;
+				if (lm) {
+					const int src_lane = __ffs(lm) - 1;
+					lm &= lm - 1;
+					ut = __shfl_sync(kFull, u, src_lane);
+					mt = shfl64(um, src_lane);
+					++cnt;
+				}
+				const uint64_t *r = cur + (size_t) ut * K;
+				g0[t] = (need0 && ((mt >> lane) & 1ull)) ? ld_cg64(r + lane) : 0ull;
+				g1[t] = (need1 && ((mt >> (lane + 32)) & 1ull)) ? ld_cg64(r + lane + 32) : 0ull;
+			}
+#pragma unroll
+			for (int t = 0; t < kMsGather; ++t) { acc0 |= g0[t]; acc1 |= g1[t]; }
+			if (lane == 0) gathered += cnt;
+			done = fm.complete(acc0 | vis0, acc1 | vis1);
+		}
+	}
+	return done;
+}
+
+// Pull, destinations with at most kMsPullBig in-edges: a warp per
+// destination, lane l owns words l and l + 32.  The rows of the others are
+// cleared here and filled by ms_pull_chunks.
 __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, uint64_t *nxt, unsigned long long &actdeg,
 		unsigned long long &gathered, uint32_t *wq_base) {
 	const uint32_t K = a.K;
-	const uint8_t *act = a.act[lvl & 1];
-	uint8_t *actn = a.act[(lvl + 1) & 1];
+	const uint64_t *actc = a.act[lvl & 1];
+	uint64_t *actn = a.act[(lvl + 1) & 1];
 	uint32_t *qn = a.queue[(lvl + 1) & 1];
 	MsCounters *cn = &a.ctl->ctr[(lvl + 1) % 3];
 	const unsigned lane = lane_id();
 	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
 	const uint32_t nwarps = gridDim.x * kMsWarps;
 	const bool w0 = lane < K, w1 = lane + 32 < K;
+	const FullMask fm(a, lane);
 	uint32_t *wbuf = wq_base + warp_id() * kMsWq;
 	uint32_t wn = 0;
-	// the bits a complete word holds (the last word may be partial)
-	const uint64_t last = a.last_bits == 64 ? ~0ull : ((1ull << a.last_bits) - 1);
-	const uint64_t full0 = w0 ? (lane == K - 1 ? last : ~0ull) : 0ull;
-	const uint64_t full1 = w1 ? (lane + 32 == K - 1 ? last : ~0ull) : 0ull;
 	for (uint32_t v = gwarp; v < a.n; v += nwarps) {
 		const size_t row = (size_t) v * K;
+		const uint32_t beg = __ldg(a.in_off + v), end = __ldg(a.in_off + v + 1);
 		const uint64_t vis0 = w0 ? ld_cg64(a.vis + row + lane) : 0ull;
 		const uint64_t vis1 = w1 ? ld_cg64(a.vis + row + lane + 32) : 0ull;
-		uint64_t acc0 = 0, acc1 = 0;
-		bool done = __all_sync(kFull, (vis0 | ~full0) == ~0ull && (vis1 | ~full1) == ~0ull);
-		if (!done) {
-			const uint32_t beg = __ldg(a.in_off + v), end = __ldg(a.in_off + v + 1);
-			for (uint32_t e0 = beg; e0 < end && !done; e0 += 32) {
-				const uint32_t e = e0 + lane;
-				const uint32_t u = e < end ? __ldg(a.in_src + e) : 0u;
-				const bool live = e < end && ld_cg_u8(act + u);
-				uint32_t lm = __ballot_sync(kFull, live);
-				// gather the live in-neighbours' words four at a time
-				while (lm && !done) {
-					uint32_t us[4];
-					int cnt = 0;
-#pragma unroll
-					for (int t = 0; t < 4; ++t) {
-						if (lm) {
-							const int src_lane = __ffs(lm) - 1;
-							lm &= lm - 1;
-							us[t] = __shfl_sync(kFull, u, src_lane);
-							++cnt;
-						} else {
-							us[t] = 0xFFFFFFFFu;
-						}
-					}
-					uint64_t g0[4], g1[4];
-#pragma unroll
-					for (int t = 0; t < 4; ++t) {
-						const bool ok = us[t] != 0xFFFFFFFFu;
-						g0[t] = (ok && w0) ? ld_cg64(cur + (size_t) us[t] * K + lane) : 0ull;
-						g1[t] = (ok && w1) ? ld_cg64(cur + (size_t) us[t] * K + lane + 32) : 0ull;
-					}
-#pragma unroll
-					for (int t = 0; t < 4; ++t) { acc0 |= g0[t]; acc1 |= g1[t]; }
-					if (lane == 0) gathered += cnt;
-					done = __all_sync(kFull, ((acc0 | vis0) | ~full0) == ~0ull && ((acc1 | vis1) | ~full1) == ~0ull);
-				}
-			}
+		if (end - beg > kMsPullBig) {
+			if (w0) nxt[row + lane] = 0;
+			if (w1) nxt[row + lane + 32] = 0;
+			continue;
 		}
-		const uint64_t n0 = acc0 & ~vis0 & full0, n1 = acc1 & ~vis1 & full1;
+		uint64_t acc0 = 0, acc1 = 0;
+		if (!fm.complete(vis0, vis1)) ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
+		const uint64_t n0 = acc0 & ~vis0 & fm.f0, n1 = acc1 & ~vis1 & fm.f1;
 		if (w0) { nxt[row + lane] = n0; if (n0) a.vis[row + lane] = vis0 | n0; }
 		if (w1) { nxt[row + lane + 32] = n1; if (n1) a.vis[row + lane + 32] = vis1 | n1; }
-		const bool any = __any_sync(kFull, (n0 | n1) != 0ull);
-		if (lane == 0) actn[v] = any ? 1 : 0;
-		if (any) {
+		const uint64_t mask = row_mask(n0, n1);
+		if (lane == 0) actn[v] = mask;
+		if (mask) {
 			const uint32_t d = deg_of(a, v);
 			if (lane == 0) actdeg += d;
 			if (d > kMsBig) {
@@ -246,6 +285,68 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, uint
 		}
 	}
 	ms_wq_flush(cn, qn, wbuf, wn);
+}
+
+// Pull, destinations with many in-edges: warps take chunks of kMsChunk
+// in-edges over the whole grid and OR what they gather into the row.
+__device__ void ms_pull_chunks(const MsArgs &a, uint32_t lvl, const uint64_t *cur, uint64_t *nxt,
+		unsigned long long &gathered) {
+	const uint32_t K = a.K;
+	const uint64_t *actc = a.act[lvl & 1];
+	const unsigned lane = lane_id();
+	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
+	const uint32_t nwarps = gridDim.x * kMsWarps;
+	const bool w0 = lane < K, w1 = lane + 32 < K;
+	const FullMask fm(a, lane);
+	for (uint32_t c = gwarp; c < a.nchunks; c += nwarps) {
+		const uint32_t v = __ldg(a.chunk_v + c), beg = __ldg(a.chunk_beg + c);
+		const uint32_t end = min(beg + kMsChunk, __ldg(a.in_off + v + 1));
+		const size_t row = (size_t) v * K;
+		const uint64_t vis0 = w0 ? ld_cg64(a.vis + row + lane) : 0ull;
+		const uint64_t vis1 = w1 ? ld_cg64(a.vis + row + lane + 32) : 0ull;
+		if (fm.complete(vis0, vis1)) continue;
+		uint64_t acc0 = 0, acc1 = 0;
+		ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
+		const uint64_t n0 = acc0 & ~vis0 & fm.f0, n1 = acc1 & ~vis1 & fm.f1;
+		if (n0) atomicOr((unsigned long long *) (nxt + row + lane), (unsigned long long) n0);
+		if (n1) atomicOr((unsigned long long *) (nxt + row + lane + 32), (unsigned long long) n1);
+	}
+}
+
+// After ms_pull_chunks: the many-in-edge destinations' rows hold their new
+// bits; update vis, the frontier mask and the queue.
+__device__ void ms_pull_chunks_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, unsigned long long &actdeg) {
+	const uint32_t K = a.K;
+	uint64_t *actn = a.act[(lvl + 1) & 1];
+	uint32_t *qn = a.queue[(lvl + 1) & 1];
+	MsCounters *cn = &a.ctl->ctr[(lvl + 1) % 3];
+	const unsigned lane = lane_id();
+	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
+	const uint32_t nwarps = gridDim.x * kMsWarps;
+	const bool w0 = lane < K, w1 = lane + 32 < K;
+	for (uint32_t j = gwarp; j < a.nbig_in; j += nwarps) {
+		const uint32_t v = __ldg(a.in_big + j);
+		const size_t row = (size_t) v * K;
+		uint64_t n0 = 0, n1 = 0;
+		if (w0) {
+			n0 = ld_cg64(nxt + row + lane);
+			if (n0) a.vis[row + lane] = ld_cg64(a.vis + row + lane) | n0;
+		}
+		if (w1) {
+			n1 = ld_cg64(nxt + row + lane + 32);
+			if (n1) a.vis[row + lane + 32] = ld_cg64(a.vis + row + lane + 32) | n1;
+		}
+		const uint64_t mask = row_mask(n0, n1);
+		if (lane == 0) {
+			actn[v] = mask;
+			if (mask) {
+				const uint32_t d = deg_of(a, v);
+				actdeg += d;
+				if (d > kMsBig) qn[a.n - 1 - atomicAdd(&cn->nbig, 1u)] = v;
+				else qn[atomicAdd(&cn->nact, 1u)] = v;
+			}
+		}
+	}
 }
 
 // Planes [first, last] (levels base + p) -> uint8 levels [source][vertex].
@@ -346,8 +447,8 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 			const unsigned long long bit = 1ull << (i % 64);
 			atomicOr((unsigned long long *) (a.hist + x), bit);
 			atomicOr((unsigned long long *) (a.vis + x), bit);
+			atomicOr((unsigned long long *) (a.act[0] + v), 1ull << (i / 64));
 			if (atomicExch(a.seed_flag + v, 1u) == 0u) {
-				a.act[0][v] = 1;
 				const uint32_t d = deg_of(a, v);
 				if (d > kMsBig) a.queue[0][a.n - 1 - atomicAdd(&ctl->ctr[0].nbig, 1u)] = v;
 				else a.queue[0][atomicAdd(&ctl->ctr[0].nact, 1u)] = v;
@@ -381,6 +482,11 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 		}
 		// the counters of the level after next are free again
 		if (leader) {
+			if (lvl < kMsTraceLevels) {
+				ctl->stats.t_level[lvl] = global_timer_ns();
+				ctl->stats.frontier[lvl] = nq + nb;
+				ctl->stats.push[lvl] = qdeg * (unsigned long long) a.push_div < (unsigned long long) a.m;
+			}
 			MsCounters *c2 = &ctl->ctr[(lvl + 2) % 3];
 			c2->nact = 0;
 			c2->nbig = 0;
@@ -398,6 +504,12 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 			ms_push_finish(a, lvl, nxt, actdeg);
 		} else {
 			ms_pull(a, lvl, cur, nxt, actdeg, gathered, wq);
+			if (a.nbig_in) {
+				if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
+				ms_pull_chunks(a, lvl, cur, nxt, gathered);
+				if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
+				ms_pull_chunks_finish(a, lvl, nxt, actdeg);
+			}
 		}
 		// the next frontier's out-degree: per-CTA sum, one atomic per CTA
 		const unsigned long long d = warp_sum(actdeg);
@@ -415,7 +527,10 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 		__syncthreads();
 		ok = grid_barrier(ctl->bar, &ctl->err);
 	}
-	if (leader) ctl->stats.t_levels1 = global_timer_ns();
+	if (leader) {
+		ctl->stats.t_levels1 = global_timer_ns();
+		if (lvl < kMsTraceLevels) ctl->stats.t_level[lvl] = ctl->stats.t_levels1;
+	}
 	if (complete) {
 		// plane lvl - base is the empty frontier; a later segment's plane 0 was written already
 		const uint32_t first = base == 0 ? 0 : 1;

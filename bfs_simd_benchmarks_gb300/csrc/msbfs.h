@@ -8,6 +8,9 @@
 namespace bfsg {
 
 constexpr uint32_t kMsMaxLevel = 254;  // uint8 levels; 255 = unreached
+constexpr uint32_t kMsTraceLevels = 64; // levels with per-level statistics
+constexpr uint32_t kMsPullBig = 256;    // pull: destinations with more in-edges are split ...
+constexpr uint32_t kMsChunk = 256;      // ... into chunks of this many in-edges
 
 struct MsCounters {
 	unsigned int nact;            // frontier vertices of degree <= kMsBig (queue front)
@@ -24,6 +27,9 @@ struct MsStats {
 	unsigned long long traversed;  // sum over (source, reached vertex) of out-degree
 	unsigned long long t_levels0;  // device clock (ns) when the first level starts
 	unsigned long long t_levels1;  // ... and when the last one has ended
+	unsigned long long t_level[kMsTraceLevels + 1];  // device clock at the start of each level
+	unsigned int frontier[kMsTraceLevels];           // frontier vertices of each level
+	unsigned char push[kMsTraceLevels];              // 1: the level was pushed
 };
 
 // Everything the launch needs zeroed; the host clears it with one memset.
@@ -42,10 +48,14 @@ struct MsArgs {
 	uint32_t planes;      // level planes allocated (>= 2)
 	uint32_t push_div;    // a level pushes while its frontier's edges < m / push_div
 	uint32_t vec_out;     // levels rows start 16-byte aligned (16-byte stores)
+	uint32_t nbig_in;     // destinations with more than kMsPullBig in-edges
+	uint32_t nchunks;     // their in-edge chunks
 	const uint32_t *row_off, *col, *in_off, *in_src;
+	const uint32_t *in_big;              // [nbig_in] those destinations
+	const uint32_t *chunk_v, *chunk_beg; // [nchunks] destination and first in-edge of each chunk
 	uint64_t *vis;        // [n][K] sources that reached v
 	uint64_t *hist;       // [planes][n][K] sources that reached v first at level base + plane
-	uint8_t *act[2];      // [n] frontier vertex flags by level parity
+	uint64_t *act[2];     // [n] by level parity: bit k = word k of v's frontier row is non-zero
 	uint8_t *touched;     // [n] push: destination received a word
 	uint32_t *seed_flag;  // [n]
 	uint32_t *queue[2];   // [n] frontier vertices by level parity (small front, big back)

@@ -190,6 +190,7 @@ int bfs_last_stats(bfs_graph *g, bfs_stats *stats);
 
 /* ---- batched traversal (no counterpart in the reference) --------------- */
 #define BFS_BATCH_MAX_SOURCES 4096
+#define BFS_BATCH_TRACE_LEVELS 64
 
 typedef struct bfs_batch_stats {
 	uint32_t num_sources;
@@ -205,6 +206,9 @@ typedef struct bfs_batch_stats {
 	double device_ms;          /* the whole launch (CUDA events) */
 	double levels_ms;          /* the levels alone (device clock) */
 	uint64_t device_bytes;     /* HBM held by the batch state */
+	float level_ms[BFS_BATCH_TRACE_LEVELS];          /* time of each of the first 64 levels */
+	uint32_t level_frontier[BFS_BATCH_TRACE_LEVELS]; /* frontier vertices of each level */
+	uint8_t level_push[BFS_BATCH_TRACE_LEVELS];      /* 1: the level was expanded top-down */
 } bfs_batch_stats;
 
 /*

@@ -162,3 +162,22 @@ def test_argument_errors(native, oracle):
             g.run_batch(np.zeros(4097, np.uint32))  # too many sources
         with pytest.raises(B.BfsError):
             g.set_options(batch_planes=1)
+
+
+def test_many_in_edge_destinations(native, oracle):
+    """Destinations with thousands of in-edges: their in-edges are cut into
+    chunks that warps across the grid gather and combine."""
+    import bfs_simd_benchmarks_gb300 as B
+    rng = np.random.default_rng(17)
+    n = 20000
+    s1, d1 = B.gen_rmat(1 << 14, 8 * (1 << 14), seed=171, permute=True)
+    sinks = np.array([19990, 19991, 19992, 5, 77], np.uint32)
+    src = [s1, rng.integers(0, n, 5 * 3000).astype(np.uint32), np.repeat(sinks[:3], 40)]
+    dst = [d1, np.repeat(sinks, 3000), rng.integers(0, n, 120).astype(np.uint32)]
+    src = np.concatenate(src).astype(np.uint32)
+    dst = np.concatenate(dst).astype(np.uint32)
+    arr = oracle.arrays_from_edges(n, src, dst, 512, 8)
+    srcs = B.pick_sources(arr["degrees"], 500, seed=9)
+    with B.Graph.from_edges(n, src, dst, 512, 8) as g:
+        _, st = _check(oracle, arr, g, srcs)
+        assert 0 in st["level_push"], "expected pull levels"
