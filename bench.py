@@ -285,6 +285,7 @@ def bench_batched(args, torch, dev):
         "edges_traversed_per_batch": edges, "depth": st["depth"], "push_levels": st["push_levels"],
         "planes": st["planes"], "spills": st["spills"], "rows_gathered": st["rows_gathered"],
         "level_ms": st["level_ms"], "level_frontier": st["level_frontier"], "level_push": st["level_push"],
+        "level_phase_ms": st["level_phase_ms"], "setup_ms": st["setup_ms"], "output_ms": st["output_ms"],
         "grid_ctas": st["grid_ctas"], "batch_state_bytes": st["device_bytes"],
         "output_bytes": len(sources) * wl.n,
         "plain_gpu_bfs": {"gteps": single_gteps, "ms_per_traversal_mean": statistics.mean(single_ms),

@@ -92,6 +92,9 @@ class BatchStats(C.Structure):
         ("level_ms", C.c_float * BFS_BATCH_TRACE_LEVELS),
         ("level_frontier", C.c_uint32 * BFS_BATCH_TRACE_LEVELS),
         ("level_push", C.c_uint8 * BFS_BATCH_TRACE_LEVELS),
+        ("level_phase_ms", (C.c_float * 3) * BFS_BATCH_TRACE_LEVELS),
+        ("setup_ms", C.c_double),
+        ("output_ms", C.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -100,6 +103,7 @@ class BatchStats(C.Structure):
         d["level_ms"] = [round(x, 4) for x in self.level_ms[:k]]
         d["level_frontier"] = list(self.level_frontier[:k])
         d["level_push"] = list(self.level_push[:k])
+        d["level_phase_ms"] = [[round(x, 4) for x in self.level_phase_ms[i]] for i in range(k)]
         return d
 
 

@@ -67,12 +67,11 @@ struct bfs_graph {
 	// batched traversal state, allocated by the first bfs_run_batch
 	struct Batch {
 		uint32_t k_alloc = 0;        // words per vertex the buffers hold
-		uint32_t wanted_alloc = 0;   // planes asked for when they were allocated
-		size_t hist_bytes = 0;
+		uint32_t planes_alloc = 0;   // level planes they hold
 		MsArgs args{};
 		uint32_t *d_sources = nullptr;
 		MsControl *h_ctl = nullptr;  // pinned
-		cudaEvent_t e0 = nullptr, e1 = nullptr;
+		cudaEvent_t e0 = nullptr, e1 = nullptr, em = nullptr;
 		cudaStream_t stream = nullptr;
 		uint32_t num_sources = 0;
 		int grid = 0;
@@ -115,7 +114,7 @@ void release_batch(bfs_graph *g) {
 	g->mb.bufs.clear();
 	g->mb.bytes = 0;
 	g->mb.k_alloc = 0;
-	g->mb.hist_bytes = 0;
+	g->mb.planes_alloc = 0;
 }
 
 void release(bfs_graph *g) {
@@ -123,8 +122,9 @@ void release(bfs_graph *g) {
 	if (g->mb.h_ctl) cudaFreeHost(g->mb.h_ctl);
 	if (g->mb.e0) cudaEventDestroy(g->mb.e0);
 	if (g->mb.e1) cudaEventDestroy(g->mb.e1);
+	if (g->mb.em) cudaEventDestroy(g->mb.em);
 	g->mb.h_ctl = nullptr;
-	g->mb.e0 = g->mb.e1 = nullptr;
+	g->mb.e0 = g->mb.e1 = g->mb.em = nullptr;
 	for (auto &b : g->bufs) cudaFree(b.p);
 	g->bufs.clear();
 	if (g->h_stats) cudaFreeHost(g->h_stats);
@@ -454,27 +454,31 @@ uint32_t batch_planes_wanted(const bfs_graph *g, uint32_t K) {
 	return (uint32_t) std::max<size_t>(2, std::min<size_t>(kBatchDefaultPlanes, budget / std::max<size_t>(plane, 1)));
 }
 
-// Makes the batch buffers hold K words per vertex and `planes` level planes;
-// returns the planes the call will use.
+// Makes the batch buffers hold K words per vertex and enough level planes;
+// returns the planes the call will use.  Buffers that hold at least K words
+// are reused; with the planes sized from the budget any plane count will do
+// (a deeper traversal writes its output early), an explicit batch_planes must
+// fit.
 int batch_prepare(bfs_graph *g, uint32_t K, uint32_t *planes_out) {
 	auto &b = g->mb;
-	const size_t plane = (size_t) g->n * K * 8;
+	const size_t plane = (size_t) g->n * K * 8 + (size_t) g->n * 8;  // rows + word masks
 	uint32_t planes = batch_planes_wanted(g, K);
 	if (!b.h_ctl) {
 		if (cudaMallocHost(&b.h_ctl, sizeof(MsControl)) != cudaSuccess) return BFS_ENOMEM;
-		if (cudaEventCreate(&b.e0) != cudaSuccess || cudaEventCreate(&b.e1) != cudaSuccess) return BFS_ECUDA;
+		if (cudaEventCreate(&b.e0) != cudaSuccess || cudaEventCreate(&b.e1) != cudaSuccess ||
+				cudaEventCreate(&b.em) != cudaSuccess)
+			return BFS_ECUDA;
 	}
-	const uint32_t have = b.k_alloc >= K ? (uint32_t) std::min<size_t>(kMsMaxLevel + 1, b.hist_bytes / plane) : 0;
-	// reuse when the planes fit, or when this is the shape the buffers were
-	// sized for and memory capped them
-	if (have >= planes || (have >= 2 && b.k_alloc == K && b.wanted_alloc == planes)) {
-		*planes_out = std::min(planes, have);
+	const uint32_t have = b.k_alloc >= K ? b.planes_alloc : 0;
+	if (have >= 2 && (have >= planes || !g->opt.batch_planes)) {
+		*planes_out = g->opt.batch_planes ? planes : have;
 		return BFS_OK;
 	}
 	// (re)allocate: wait for earlier batches that still use the buffers
 	if (b.have_run && cudaEventSynchronize(b.e1) != cudaSuccess) return BFS_ECUDA;
 	release_batch(g);
-	const size_t fixed = plane + (size_t) g->n * (16 + 1 + 4 + 8) + sizeof(MsControl) + 4 * BFS_BATCH_MAX_SOURCES;
+	const size_t fixed = (size_t) g->n * K * 8 + (size_t) g->n * (2 + 4 + 8) + sizeof(MsControl) +
+			4 * BFS_BATCH_MAX_SOURCES;
 	size_t free_b = 0, total_b = 0;
 	if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return BFS_ECUDA;
 	const size_t usable = free_b > (size_t) 1 << 30 ? free_b - ((size_t) 1 << 30) : 0;  // leave 1 GiB
@@ -487,17 +491,16 @@ int batch_prepare(bfs_graph *g, uint32_t K, uint32_t *planes_out) {
 	int st;
 	if ((st = batch_alloc(g, &a.vis, (size_t) g->n * K))) return st;
 	if ((st = batch_alloc(g, &a.hist, (size_t) planes * g->n * K))) return st;
-	if ((st = batch_alloc(g, &a.act[0], g->n))) return st;
-	if ((st = batch_alloc(g, &a.act[1], g->n))) return st;
+	if ((st = batch_alloc(g, &a.pmask, (size_t) planes * g->n))) return st;
 	if ((st = batch_alloc(g, &a.touched, g->n))) return st;
+	if ((st = batch_alloc(g, &a.done, g->n))) return st;
 	if ((st = batch_alloc(g, &a.seed_flag, g->n))) return st;
 	if ((st = batch_alloc(g, &a.queue[0], g->n))) return st;
 	if ((st = batch_alloc(g, &a.queue[1], g->n))) return st;
 	if ((st = batch_alloc(g, &a.ctl, 1))) return st;
 	if ((st = batch_alloc(g, &b.d_sources, BFS_BATCH_MAX_SOURCES))) return st;
 	b.k_alloc = K;
-	b.wanted_alloc = batch_planes_wanted(g, K);
-	b.hist_bytes = (size_t) planes * plane;
+	b.planes_alloc = planes;
 	*planes_out = planes;
 	return BFS_OK;
 }
@@ -534,7 +537,7 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 	// pageable source: the copy has left `sources` when the call returns
 	if (cudaMemcpyAsync(b.d_sources, sources, sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, st) != cudaSuccess)
 		return BFS_ECUDA;
-	if ((rc = ms_launch(a, b.d_sources, ns, levels, g->num_sms, st, &b.grid))) return rc;
+	if ((rc = ms_launch(a, b.d_sources, ns, levels, g->num_sms, st, &b.grid, b.em))) return rc;
 	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
 	b.args.planes = planes;
 	b.args.K = K;
@@ -566,15 +569,26 @@ int collect_batch_stats(bfs_graph *g, bfs_batch_stats *out) {
 	s.spills = c.stats.spills;
 	s.words_per_vertex = b.args.K;
 	s.grid_ctas = (uint32_t) b.grid;
-	float ms = 0;
+	float ms = 0, ems = 0;
 	cudaEventElapsedTime(&ms, b.e0, b.e1);
+	cudaEventElapsedTime(&ems, b.em, b.e1);
 	s.device_ms = ms;
+	s.output_ms = ems;
+	s.setup_ms = c.stats.t_levels0 > c.stats.t_start ? (c.stats.t_levels0 - c.stats.t_start) * 1e-6 : 0.0;
 	s.levels_ms = c.stats.t_levels1 > c.stats.t_levels0 ? (c.stats.t_levels1 - c.stats.t_levels0) * 1e-6 : 0.0;
 	s.device_bytes = b.bytes;
 	const uint32_t nl = std::min<uint32_t>(c.stats.depth, kMsTraceLevels);
 	for (uint32_t l = 0; l < nl; ++l) {
 		const unsigned long long t0 = c.stats.t_level[l], t1 = c.stats.t_level[l + 1];
 		s.level_ms[l] = (t0 && t1 > t0) ? (float) ((t1 - t0) * 1e-6) : 0.f;
+		const unsigned long long p0 = c.stats.t_phase[l][0], p1 = c.stats.t_phase[l][1];
+		if (t0 && p0 >= t0 && p1 >= p0 && t1 >= p1) {
+			s.level_phase_ms[l][0] = (float) ((p0 - t0) * 1e-6);
+			s.level_phase_ms[l][1] = (float) ((p1 - p0) * 1e-6);
+			s.level_phase_ms[l][2] = (float) ((t1 - p1) * 1e-6);
+		} else if (t0 && t1 > t0) {
+			s.level_phase_ms[l][0] = s.level_ms[l];
+		}
 		s.level_frontier[l] = c.stats.frontier[l];
 		s.level_push[l] = c.stats.push[l];
 	}

@@ -8,8 +8,8 @@
 //   vis[v][K]          sources that have reached v
 //   hist[p][v][K]      sources that reached v first at level base + p; the
 //                      plane of level L is the frontier that level L expands
-//   act[L&1][v]        bit k: word k of v's row in the plane of level L is
-//                      non-zero (the frontier's vertex set and which rows to read)
+//   pmask[p][v]        bit k: word k of v's row in plane p is non-zero (the
+//                      frontier's vertex set, and which words to read)
 //   queue[L&1]         the frontier's vertices: degree <= kMsBig from the
 //                      front, higher degree from the back
 // A level is expanded either
@@ -22,10 +22,10 @@
 //     still lacks and stops as soon as every source has reached it
 //     (per-destination early exit); destinations with many in-edges are cut
 //     into chunks that warps all over the grid gather and OR together.
-// Everything -- clearing, seeding, all levels, the output and the edge count
-// -- runs in one cooperative launch, levels separated by a bounded-spin grid
-// barrier.  The output pass turns planes into uint8 levels [source][vertex]
-// (255 = unreached) through a shared-memory transpose.  When a traversal is
+// Clearing, seeding, all levels and the edge count run in one cooperative
+// launch, levels separated by a bounded-spin grid barrier; the output pass,
+// its own launch, turns planes into uint8 levels [source][vertex] (255 =
+// unreached) through a shared-memory transpose.  When a traversal is
 // deeper than the planes allocated, the planes so far are written out, the
 // current frontier plane becomes plane 0 and the traversal goes on; the later
 // output passes merge into the bytes already written.
@@ -43,10 +43,10 @@ constexpr int kMsWarps = kMsThreads / 32;
 constexpr uint32_t kMsWq = 64;          // per-warp staged queue appends (pull)
 constexpr uint32_t kMsBig = 1024;       // push: higher-degree vertices are spread over the grid
 constexpr int kMsGather = 4;            // pull: frontier rows gathered per round
-constexpr uint32_t kEmitWords = 8;      // output tile: 8 words (512 sources) ...
-constexpr uint32_t kEmitRows = kEmitWords * 64;
-constexpr uint32_t kEmitV = 64;         // ... x 64 vertices
-constexpr uint32_t kEmitStride = 68;    // shared row stride in bytes (17 words: column writes spread over banks)
+constexpr uint32_t kEmitV = 128;        // output tile: 128 vertices x 4 words (256 sources)
+constexpr uint32_t kEmitW = 4;
+constexpr uint32_t kEmitStride = 132;   // shared row stride in bytes (33 words: column writes spread over banks)
+constexpr uint32_t kEmitBytes = kEmitW * 64 * kEmitStride;
 
 __device__ __forceinline__ uint64_t ld_cg64(const uint64_t *p) { return __ldcg((const unsigned long long *) p); }
 __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
@@ -105,9 +105,9 @@ __device__ __forceinline__ void ms_push_edges(const MsArgs &a, const uint64_t *c
 	}
 }
 
-__device__ void ms_push(const MsArgs &a, uint32_t lvl, const uint64_t *cur, uint64_t *nxt, uint32_t nq, uint32_t nb) {
+__device__ void ms_push(const MsArgs &a, uint32_t lvl, const uint64_t *cur, const uint64_t *actc, uint64_t *nxt, uint32_t nq,
+		uint32_t nb) {
 	const uint32_t *q = a.queue[lvl & 1];
-	const uint64_t *actc = a.act[lvl & 1];
 	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
 	const uint32_t nwarps = gridDim.x * kMsWarps;
 	for (uint32_t i = gwarp; i < nq; i += nwarps) {
@@ -128,11 +128,10 @@ __device__ __forceinline__ uint64_t row_mask(uint64_t n0, uint64_t n1) {
 // After a push level: the OR'ed words lose the bits already visited, the rest
 // are new, go into vis and put v into the next frontier.  A warp takes 32
 // vertices, then works through the touched ones together (K words each).
-__device__ void ms_push_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, unsigned long long &actdeg) {
+__device__ void ms_push_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, uint64_t *actn, unsigned long long &actdeg) {
 	const uint32_t K = a.K;
 	const unsigned lane = lane_id();
 	uint32_t *qn = a.queue[(lvl + 1) & 1];
-	uint64_t *actn = a.act[(lvl + 1) & 1];
 	MsCounters *cn = &a.ctl->ctr[(lvl + 1) % 3];
 	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
 	const uint32_t nwarps = gridDim.x * kMsWarps;
@@ -239,14 +238,15 @@ __device__ __forceinline__ bool ms_gather(const MsArgs &a, const uint64_t *cur, 
 	return done;
 }
 
-// Pull, destinations with at most kMsPullBig in-edges: a warp per
-// destination, lane l owns words l and l + 32.  The rows of the others are
-// cleared here and filled by ms_pull_chunks.
-__device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, uint64_t *nxt, unsigned long long &actdeg,
-		unsigned long long &gathered, uint32_t *wq_base) {
+// Pull, destinations with at most kMsPullBig in-edges.  A warp screens 32
+// consecutive destinations at once (their in-edge ranges and "every source
+// has arrived" flags, lane-parallel), clears the rows of those with nothing
+// to do as one contiguous block, then works through the others one at a
+// time: lane l owns words l and l + 32.  The rows of many-in-edge
+// destinations are cleared here and filled by ms_pull_chunks.
+__device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, const uint64_t *actc, uint64_t *nxt,
+		uint64_t *actn, unsigned long long &actdeg, unsigned long long &gathered, uint32_t *wq_base) {
 	const uint32_t K = a.K;
-	const uint64_t *actc = a.act[lvl & 1];
-	uint64_t *actn = a.act[(lvl + 1) & 1];
 	uint32_t *qn = a.queue[(lvl + 1) & 1];
 	MsCounters *cn = &a.ctl->ctr[(lvl + 1) % 3];
 	const unsigned lane = lane_id();
@@ -256,31 +256,46 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, uint
 	const FullMask fm(a, lane);
 	uint32_t *wbuf = wq_base + warp_id() * kMsWq;
 	uint32_t wn = 0;
-	for (uint32_t v = gwarp; v < a.n; v += nwarps) {
-		const size_t row = (size_t) v * K;
-		const uint32_t beg = __ldg(a.in_off + v), end = __ldg(a.in_off + v + 1);
-		const uint64_t vis0 = w0 ? ld_cg64(a.vis + row + lane) : 0ull;
-		const uint64_t vis1 = w1 ? ld_cg64(a.vis + row + lane + 32) : 0ull;
-		if (end - beg > kMsPullBig) {
-			if (w0) nxt[row + lane] = 0;
-			if (w1) nxt[row + lane + 32] = 0;
-			continue;
-		}
-		uint64_t acc0 = 0, acc1 = 0;
-		if (!fm.complete(vis0, vis1)) ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
-		const uint64_t n0 = acc0 & ~vis0 & fm.f0, n1 = acc1 & ~vis1 & fm.f1;
-		if (w0) { nxt[row + lane] = n0; if (n0) a.vis[row + lane] = vis0 | n0; }
-		if (w1) { nxt[row + lane + 32] = n1; if (n1) a.vis[row + lane + 32] = vis1 | n1; }
-		const uint64_t mask = row_mask(n0, n1);
-		if (lane == 0) actn[v] = mask;
-		if (mask) {
-			const uint32_t d = deg_of(a, v);
-			if (lane == 0) actdeg += d;
-			if (d > kMsBig) {
-				if (lane == 0) qn[a.n - 1 - atomicAdd(&cn->nbig, 1u)] = v;
-			} else {
-				if (lane == 0) wbuf[wn] = v;
-				if (++wn == kMsWq) ms_wq_flush(cn, qn, wbuf, wn);
+	for (uint32_t vb = gwarp * 32; vb < a.n; vb += nwarps * 32) {
+		const uint32_t vl = vb + lane;
+		const bool valid = vl < a.n;
+		const uint32_t lbeg = valid ? __ldg(a.in_off + vl) : 0u, lend = valid ? __ldg(a.in_off + vl + 1) : 0u;
+		const bool big = lend - lbeg > kMsPullBig;
+		const bool needy = valid && !big && lend > lbeg && !ld_cg_u8(a.done + vl);
+		const uint32_t needm = __ballot_sync(kFull, needy);
+		if (valid && !needy && !big) actn[vl] = 0;
+		// rows of the block with nothing to do (and of big destinations) are zero
+		const uint32_t nb = min(32u, a.n - vb);
+		uint64_t *blk = nxt + (size_t) vb * K;
+		for (uint32_t x = lane; x < nb * K; x += 32)
+			if (!((needm >> (x / K)) & 1u)) blk[x] = 0ull;
+		for (uint32_t m = needm; m; m &= m - 1) {
+			const int jj = __ffs(m) - 1;
+			const uint32_t v = vb + jj;
+			const uint32_t beg = __shfl_sync(kFull, lbeg, jj), end = __shfl_sync(kFull, lend, jj);
+			const size_t row = (size_t) v * K;
+			const uint64_t vis0 = w0 ? ld_cg64(a.vis + row + lane) : 0ull;
+			const uint64_t vis1 = w1 ? ld_cg64(a.vis + row + lane + 32) : 0ull;
+			uint64_t acc0 = 0, acc1 = 0;
+			if (!fm.complete(vis0, vis1)) ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
+			const uint64_t n0 = acc0 & ~vis0 & fm.f0, n1 = acc1 & ~vis1 & fm.f1;
+			if (w0) { nxt[row + lane] = n0; if (n0) a.vis[row + lane] = vis0 | n0; }
+			if (w1) { nxt[row + lane + 32] = n1; if (n1) a.vis[row + lane + 32] = vis1 | n1; }
+			const uint64_t mask = row_mask(n0, n1);
+			const bool full = fm.complete(vis0 | n0, vis1 | n1);
+			if (lane == 0) {
+				actn[v] = mask;
+				if (full) a.done[v] = 1;
+			}
+			if (mask) {
+				const uint32_t d = deg_of(a, v);
+				if (lane == 0) actdeg += d;
+				if (d > kMsBig) {
+					if (lane == 0) qn[a.n - 1 - atomicAdd(&cn->nbig, 1u)] = v;
+				} else {
+					if (lane == 0) wbuf[wn] = v;
+					if (++wn == kMsWq) ms_wq_flush(cn, qn, wbuf, wn);
+				}
 			}
 		}
 	}
@@ -289,10 +304,9 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, uint
 
 // Pull, destinations with many in-edges: warps take chunks of kMsChunk
 // in-edges over the whole grid and OR what they gather into the row.
-__device__ void ms_pull_chunks(const MsArgs &a, uint32_t lvl, const uint64_t *cur, uint64_t *nxt,
+__device__ void ms_pull_chunks(const MsArgs &a, const uint64_t *cur, const uint64_t *actc, uint64_t *nxt,
 		unsigned long long &gathered) {
 	const uint32_t K = a.K;
-	const uint64_t *actc = a.act[lvl & 1];
 	const unsigned lane = lane_id();
 	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
 	const uint32_t nwarps = gridDim.x * kMsWarps;
@@ -315,9 +329,9 @@ __device__ void ms_pull_chunks(const MsArgs &a, uint32_t lvl, const uint64_t *cu
 
 // After ms_pull_chunks: the many-in-edge destinations' rows hold their new
 // bits; update vis, the frontier mask and the queue.
-__device__ void ms_pull_chunks_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, unsigned long long &actdeg) {
+__device__ void ms_pull_chunks_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, uint64_t *actn,
+		unsigned long long &actdeg) {
 	const uint32_t K = a.K;
-	uint64_t *actn = a.act[(lvl + 1) & 1];
 	uint32_t *qn = a.queue[(lvl + 1) & 1];
 	MsCounters *cn = &a.ctl->ctr[(lvl + 1) % 3];
 	const unsigned lane = lane_id();
@@ -350,70 +364,93 @@ __device__ void ms_pull_chunks_finish(const MsArgs &a, uint32_t lvl, uint64_t *n
 }
 
 // Planes [first, last] (levels base + p) -> uint8 levels [source][vertex].
-// A CTA takes tiles of 64 vertices x 8 words: each thread loads one word per
-// plane (a warp reads 4 vertices x 64 contiguous bytes), writes the level of
-// each set bit into the shared tile, then the tile leaves as 64-byte rows.
-// `merge` starts each tile from the bytes already in `levels` (a later
-// segment of a traversal deeper than the planes) instead of 255.
+// A CTA of 512 threads takes tiles of 128 vertices x 4 words (256 sources);
+// thread (vertex, word) -- a warp holds 32 consecutive vertices of one word
+// -- builds the 64 level bytes of its word's sources in 16 registers: for
+// every plane whose word mask says the word is non-zero it loads the word and,
+// four sources at a time, spreads the 4 bits into a byte mask (two integer
+// multiplies) and writes the plane's level under it.  A byte starts at 255
+// and is written at most once (a source reaches a vertex at one level), so
+// "write" is an XOR with 255 ^ level.  The bytes go to a shared tile
+// [source][vertex] (lanes store consecutive bytes) and leave as 128-byte
+// rows.  `merge` combines with the bytes already in `levels` (a later
+// segment of a traversal deeper than the planes) by a byte-wise minimum:
+// every byte is below 255 in at most one segment.
+__device__ __forceinline__ uint32_t nibble_bytes(uint32_t nib) {
+	return ((nib * 0x00204081u) & 0x01010101u) * 0xFFu;  // bit i -> byte i all ones
+}
+
 __device__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t ns, uint32_t base, uint32_t first, uint32_t last,
 		bool merge, uint8_t *lev) {
+	constexpr uint32_t kRows = kEmitW * 64;
 	const uint32_t K = a.K, n = a.n;
-	const uint32_t vtiles = (n + kEmitV - 1) / kEmitV, wtiles = (K + kEmitWords - 1) / kEmitWords;
-	const uint32_t vi = threadIdx.x / kEmitWords, wi = threadIdx.x % kEmitWords;
+	const uint32_t vtiles = (n + kEmitV - 1) / kEmitV, wtiles = (K + kEmitW - 1) / kEmitW;
+	const uint32_t vi = threadIdx.x % kEmitV, wi = threadIdx.x / kEmitV;
+	const size_t pstride = (size_t) n * K;
 	for (uint32_t tile = blockIdx.x; tile < vtiles * wtiles; tile += gridDim.x) {
-		const uint32_t v0 = (tile % vtiles) * kEmitV, k0 = (tile / vtiles) * kEmitWords;
+		const uint32_t v0 = (tile % vtiles) * kEmitV, k0 = (tile / vtiles) * kEmitW;
 		const uint32_t nv = min(kEmitV, n - v0);
-		const uint32_t nrows = min(kEmitRows, ns - k0 * 64);
+		const uint32_t nrows = min(kRows, ns - k0 * 64);
 		const bool vec = a.vec_out && nv == kEmitV;
-		// 1. start values
-		for (uint32_t idx = threadIdx.x; idx < kEmitRows * (kEmitV / 4); idx += blockDim.x) {
-			const uint32_t r = idx / (kEmitV / 4), c = (idx % (kEmitV / 4)) * 4;
-			uint32_t val = 0xFFFFFFFFu;
-			if (merge && r < nrows) {
-				const uint8_t *src = levels + (size_t) (k0 * 64 + r) * n + v0 + c;
-				if (vec) {
-					val = __ldcg((const unsigned int *) src);
-				} else {
-					for (uint32_t b = 0; b < 4; ++b)
-						if (c + b < nv) val = (val & ~(0xFFu << (8 * b))) | ((uint32_t) ld_cg_u8(src + b) << (8 * b));
-				}
-			}
-			*(uint32_t *) (lev + r * kEmitStride + c) = val;
-		}
-		__syncthreads();
-		// 2. the level of every set bit
+		// 1. this thread's 64 level bytes
 		if (vi < nv && k0 + wi < K) {
-			const uint64_t *p = a.hist + ((size_t) first * n + v0 + vi) * K + k0 + wi;
-			const size_t pstride = (size_t) n * K;
-			uint8_t *col = lev + wi * 64 * kEmitStride + vi;
+			const uint32_t v = v0 + vi, k = k0 + wi;
+			const uint64_t *pw = a.hist + ((size_t) first * n + v) * K + k;
+			const uint64_t *pm = a.pmask + (size_t) first * n + v;
+			uint32_t o[16];
+#pragma unroll
+			for (int q = 0; q < 16; ++q) o[q] = 0xFFFFFFFFu;
 			for (uint32_t l = first; l <= last; l += 4) {
 				uint64_t w[4];
 #pragma unroll
-				for (int t = 0; t < 4; ++t) w[t] = l + t <= last ? ld_cg64(p + (size_t) (l - first + t) * pstride) : 0ull;
+				for (int t = 0; t < 4; ++t) {
+					const uint64_t m = l + t <= last ? ld_cg64(pm + (size_t) (l - first + t) * n) : 0ull;
+					w[t] = ((m >> k) & 1ull) ? ld_cg64(pw + (size_t) (l - first + t) * pstride) : 0ull;
+				}
 #pragma unroll
 				for (int t = 0; t < 4; ++t) {
-					const uint8_t val = (uint8_t) (base + l + t);
-					for (uint64_t x = w[t]; x; x &= x - 1) col[(__ffsll((long long) x) - 1) * kEmitStride] = val;
+					if (!w[t]) continue;
+					const uint32_t inv = ~((uint32_t) (base + l + t) * 0x01010101u);
+					const uint32_t lo = (uint32_t) w[t], hi = (uint32_t) (w[t] >> 32);
+#pragma unroll
+					for (int q = 0; q < 8; ++q) o[q] ^= nibble_bytes((lo >> (4 * q)) & 0xFu) & inv;
+#pragma unroll
+					for (int q = 0; q < 8; ++q) o[8 + q] ^= nibble_bytes((hi >> (4 * q)) & 0xFu) & inv;
 				}
 			}
+			uint8_t *col = lev + wi * 64 * kEmitStride + vi;
+#pragma unroll
+			for (int q = 0; q < 16; ++q)
+#pragma unroll
+				for (int b = 0; b < 4; ++b) col[(4 * q + b) * kEmitStride] = (uint8_t) (o[q] >> (8 * b));
 		}
 		__syncthreads();
-		// 3. rows out
-		for (uint32_t idx = threadIdx.x; idx < kEmitRows * (kEmitV / 16); idx += blockDim.x) {
+		// 2. rows out
+		for (uint32_t idx = threadIdx.x; idx < kRows * (kEmitV / 16); idx += blockDim.x) {
 			const uint32_t r = idx / (kEmitV / 16), c = (idx % (kEmitV / 16)) * 16;
 			if (r >= nrows) continue;
 			uint8_t *dst = levels + (size_t) (k0 * 64 + r) * n + v0 + c;
-			const uint8_t *s = lev + r * kEmitStride + c;
+			const uint8_t *sp = lev + r * kEmitStride + c;
 			if (vec) {
 				uint4 x;
-				x.x = *(const uint32_t *) (s + 0);
-				x.y = *(const uint32_t *) (s + 4);
-				x.z = *(const uint32_t *) (s + 8);
-				x.w = *(const uint32_t *) (s + 12);
+				x.x = *(const uint32_t *) (sp + 0);
+				x.y = *(const uint32_t *) (sp + 4);
+				x.z = *(const uint32_t *) (sp + 8);
+				x.w = *(const uint32_t *) (sp + 12);
+				if (merge) {
+					const uint4 old = __ldcg((const uint4 *) dst);
+					x.x = __vminu4(x.x, old.x);
+					x.y = __vminu4(x.y, old.y);
+					x.z = __vminu4(x.z, old.z);
+					x.w = __vminu4(x.w, old.w);
+				}
 				*(uint4 *) dst = x;
 			} else {
-				for (uint32_t b = 0; b < 16; ++b)
-					if (c + b < nv) dst[b] = s[b];
+				for (uint32_t b = 0; b < 16; ++b) {
+					if (c + b >= nv) break;
+					const uint8_t x = sp[b];
+					dst[b] = merge ? min(x, ld_cg_u8(dst + b)) : x;
+				}
 			}
 		}
 		__syncthreads();
@@ -424,17 +461,18 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 		uint8_t *levels) {
 	__shared__ unsigned long long red[kMsWarps];
 	__shared__ uint32_t wq[kMsWarps * kMsWq];
-	__shared__ __align__(16) uint8_t lev[kEmitRows * kEmitStride];
+	__shared__ __align__(16) uint8_t lev[kEmitBytes];
 	MsControl *ctl = a.ctl;
 	const uint32_t stride = gridDim.x * blockDim.x;
 	const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
 	const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
 	const size_t nK = (size_t) a.n * a.K;
+	if (leader) ctl->stats.t_start = global_timer_ns();
 	// clear (the control block was zeroed by the host)
 	for (size_t i = t0; i < nK; i += stride) { a.vis[i] = 0; a.hist[i] = 0; }
 	for (uint32_t i = t0; i < a.n; i += stride) {
-		a.act[0][i] = 0;
-		a.act[1][i] = 0;
+		a.pmask[i] = 0;
+		a.done[i] = 0;
 		a.touched[i] = 0;
 		a.seed_flag[i] = 0;
 	}
@@ -447,7 +485,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 			const unsigned long long bit = 1ull << (i % 64);
 			atomicOr((unsigned long long *) (a.hist + x), bit);
 			atomicOr((unsigned long long *) (a.vis + x), bit);
-			atomicOr((unsigned long long *) (a.act[0] + v), 1ull << (i / 64));
+			atomicOr((unsigned long long *) (a.pmask + v), 1ull << (i / 64));
 			if (atomicExch(a.seed_flag + v, 1u) == 0u) {
 				const uint32_t d = deg_of(a, v);
 				if (d > kMsBig) a.queue[0][a.n - 1 - atomicAdd(&ctl->ctr[0].nbig, 1u)] = v;
@@ -476,6 +514,8 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 			if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
 			const uint64_t *src = a.hist + (size_t) (lvl - base) * nK;
 			for (size_t i = t0; i < nK; i += stride) a.hist[i] = ld_cg64(src + i);
+			const uint64_t *msrc = a.pmask + (size_t) (lvl - base) * a.n;
+			for (uint32_t i = t0; i < a.n; i += stride) a.pmask[i] = ld_cg64(msrc + i);
 			base = lvl;
 			if (leader) ctl->stats.spills++;
 			if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
@@ -494,21 +534,28 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 		}
 		const uint64_t *cur = a.hist + (size_t) (lvl - base) * nK;
 		uint64_t *nxt = a.hist + (size_t) (lvl + 1 - base) * nK;
+		const uint64_t *actc = a.pmask + (size_t) (lvl - base) * a.n;
+		uint64_t *actn = a.pmask + (size_t) (lvl + 1 - base) * a.n;
+		unsigned long long *tph = lvl < kMsTraceLevels ? ctl->stats.t_phase[lvl] : nullptr;
 		unsigned long long actdeg = 0;
 		const bool push = qdeg * (unsigned long long) a.push_div < (unsigned long long) a.m;
 		if (push) {
 			for (size_t i = t0; i < nK; i += stride) nxt[i] = 0;
 			if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
-			ms_push(a, lvl, cur, nxt, nq, nb);
+			if (leader && tph) tph[0] = global_timer_ns();
+			ms_push(a, lvl, cur, actc, nxt, nq, nb);
 			if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
-			ms_push_finish(a, lvl, nxt, actdeg);
+			if (leader && tph) tph[1] = global_timer_ns();
+			ms_push_finish(a, lvl, nxt, actn, actdeg);
 		} else {
-			ms_pull(a, lvl, cur, nxt, actdeg, gathered, wq);
+			ms_pull(a, lvl, cur, actc, nxt, actn, actdeg, gathered, wq);
 			if (a.nbig_in) {
 				if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
-				ms_pull_chunks(a, lvl, cur, nxt, gathered);
+				if (leader && tph) tph[0] = global_timer_ns();
+				ms_pull_chunks(a, cur, actc, nxt, gathered);
 				if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
-				ms_pull_chunks_finish(a, lvl, nxt, actdeg);
+				if (leader && tph) tph[1] = global_timer_ns();
+				ms_pull_chunks_finish(a, lvl, nxt, actn, actdeg);
 			}
 		}
 		// the next frontier's out-degree: per-CTA sum, one atomic per CTA
@@ -530,11 +577,10 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 	if (leader) {
 		ctl->stats.t_levels1 = global_timer_ns();
 		if (lvl < kMsTraceLevels) ctl->stats.t_level[lvl] = ctl->stats.t_levels1;
+		ctl->stats.base = base;
+		ctl->stats.complete = complete ? 1u : 0u;
 	}
 	if (complete) {
-		// plane lvl - base is the empty frontier; a later segment's plane 0 was written already
-		const uint32_t first = base == 0 ? 0 : 1;
-		if (lvl - 1 >= base + first) ms_emit(a, levels, ns, base, first, lvl - 1 - base, base != 0, lev);
 		// TEPS numerator: sum over (source, reached vertex) of out-degree
 		unsigned long long tr = 0;
 		for (uint32_t v = t0; v < a.n; v += stride) {
@@ -557,8 +603,21 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 	if (leader) ctl->stats.depth = lvl;
 }
 
+// The final output pass, its own launch after k_ms_bfs (more CTAs per SM than
+// the cooperative kernel, so more plane loads in flight).  Plane depth - base
+// is the empty frontier; after an early output pass, plane 0 was written too.
+__global__ void __launch_bounds__(kMsThreads, 2) k_ms_emit(MsArgs a, uint32_t ns, uint8_t *levels) {
+	__shared__ __align__(16) uint8_t lev[kEmitBytes];
+	const MsStats &st = a.ctl->stats;
+	if (!st.complete) return;
+	const uint32_t base = st.base, depth = st.depth;
+	const uint32_t first = base == 0 ? 0 : 1;
+	if (depth < base + first + 1) return;
+	ms_emit(a, levels, ns, base, first, depth - 1 - base, base != 0, lev);
+}
+
 int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *levels, int num_sms, cudaStream_t st,
-		int *grid) {
+		int *grid, cudaEvent_t between) {
 	int per_sm = 0;
 	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ms_bfs, kMsThreads, 0) != cudaSuccess || per_sm < 1)
 		return BFS_ECUDA;
@@ -573,7 +632,9 @@ int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *
 	if (cudaLaunchCooperativeKernel((const void *) k_ms_bfs, dim3(num_sms * per_sm), dim3(kMsThreads), args, 0, st) !=
 			cudaSuccess)
 		return BFS_ECUDA;
-	return BFS_OK;
+	if (between && cudaEventRecord(between, st) != cudaSuccess) return BFS_ECUDA;
+	k_ms_emit<<<num_sms * 2, kMsThreads, 0, st>>>(a, ns, levels);
+	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }
 
 } // namespace bfsg

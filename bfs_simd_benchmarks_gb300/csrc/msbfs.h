@@ -23,11 +23,15 @@ struct MsStats {
 	unsigned int push_levels;      // of which top-down
 	unsigned int depth;            // level whose frontier came out empty
 	unsigned int spills;           // times the level planes filled up and were written out early
+	unsigned int base;             // level of plane 0 when the traversal ended
+	unsigned int complete;         // 1: every level ran (the output pass may go)
 	unsigned long long edges;      // in-neighbour frontier rows gathered by pull levels
 	unsigned long long traversed;  // sum over (source, reached vertex) of out-degree
 	unsigned long long t_levels0;  // device clock (ns) when the first level starts
 	unsigned long long t_levels1;  // ... and when the last one has ended
+	unsigned long long t_start;    // device clock when the launch starts
 	unsigned long long t_level[kMsTraceLevels + 1];  // device clock at the start of each level
+	unsigned long long t_phase[kMsTraceLevels][2];   // ... after its first and second grid barrier
 	unsigned int frontier[kMsTraceLevels];           // frontier vertices of each level
 	unsigned char push[kMsTraceLevels];              // 1: the level was pushed
 };
@@ -55,16 +59,18 @@ struct MsArgs {
 	const uint32_t *chunk_v, *chunk_beg; // [nchunks] destination and first in-edge of each chunk
 	uint64_t *vis;        // [n][K] sources that reached v
 	uint64_t *hist;       // [planes][n][K] sources that reached v first at level base + plane
-	uint64_t *act[2];     // [n] by level parity: bit k = word k of v's frontier row is non-zero
+	uint64_t *pmask;      // [planes][n] bit k: word k of v's row in that plane is non-zero
 	uint8_t *touched;     // [n] push: destination received a word
+	uint8_t *done;        // [n] pull: every source has reached v (set by pulls; a hint)
 	uint32_t *seed_flag;  // [n]
 	uint32_t *queue[2];   // [n] frontier vertices by level parity (small front, big back)
 	MsControl *ctl;
 };
 
-// Enqueues the whole batched traversal (one cooperative launch) on `st`;
+// Enqueues the whole batched traversal (one cooperative launch and the
+// output pass) on `st`; `between` (may be null) is recorded between the two;
 // *grid receives the launch's CTA count.
 int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *levels, int num_sms, cudaStream_t st,
-		int *grid);
+		int *grid, cudaEvent_t between);
 
 } // namespace bfsg

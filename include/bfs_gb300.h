@@ -209,6 +209,10 @@ typedef struct bfs_batch_stats {
 	float level_ms[BFS_BATCH_TRACE_LEVELS];          /* time of each of the first 64 levels */
 	uint32_t level_frontier[BFS_BATCH_TRACE_LEVELS]; /* frontier vertices of each level */
 	uint8_t level_push[BFS_BATCH_TRACE_LEVELS];      /* 1: the level was expanded top-down */
+	float level_phase_ms[BFS_BATCH_TRACE_LEVELS][3]; /* pull: small destinations, chunks, finish;
+	                                                    push: clear, expand, finish */
+	double setup_ms;           /* clearing and seeding (device clock) */
+	double output_ms;          /* the output pass (CUDA events) */
 } bfs_batch_stats;
 
 /*
