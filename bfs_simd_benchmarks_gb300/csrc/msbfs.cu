@@ -238,6 +238,16 @@ __device__ __forceinline__ bool ms_gather(const MsArgs &a, const uint64_t *cur, 
 	return done;
 }
 
+// A bijection of [0, 2^bits): xor-shift, multiply by an odd constant, xor-shift.
+__device__ __forceinline__ uint32_t block_perm(uint32_t x, uint32_t bits) {
+	const uint32_t mask = bits >= 32 ? 0xFFFFFFFFu : (1u << bits) - 1u;
+	const uint32_t h = (bits + 1) / 2;
+	x ^= x >> h;
+	x = (x * 0x9E3779B1u) & mask;
+	x ^= x >> h;
+	return x;
+}
+
 // Pull, destinations with at most kMsPullBig in-edges.  A warp screens 32
 // consecutive destinations at once (their in-edge ranges and "every source
 // has arrived" flags, lane-parallel), clears the rows of those with nothing
@@ -256,7 +266,15 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, cons
 	const FullMask fm(a, lane);
 	uint32_t *wbuf = wq_base + warp_id() * kMsWq;
 	uint32_t wn = 0;
-	for (uint32_t vb = gwarp * 32; vb < a.n; vb += nwarps * 32) {
+	// blocks of 32 destinations in a hashed order: in-degree follows the id
+	// bits of R-MAT-like graphs, so a plain stride gives some warps the heavy
+	// blocks every time
+	const uint32_t nblk = (a.n + 31) / 32;
+	const uint32_t pbits = 32 - __clz(max(nblk - 1, 1u));
+	for (uint32_t i = gwarp; i < (1u << pbits); i += nwarps) {
+		const uint32_t bi = block_perm(i, pbits);
+		if (bi >= nblk) continue;
+		const uint32_t vb = bi * 32;
 		const uint32_t vl = vb + lane;
 		const bool valid = vl < a.n;
 		const uint32_t lbeg = valid ? __ldg(a.in_off + vl) : 0u, lend = valid ? __ldg(a.in_off + vl + 1) : 0u;
