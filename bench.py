@@ -278,6 +278,11 @@ def bench_batched(args, torch, dev):
         rows_ok += int(np.array_equal(row, ref))
     single_gteps = single_edges / (sum(single_ms) / 1e3) / 1e9
     st = runs[-1][1]
+    # algorithmic bytes of a batch: every level writes its N x K-word plane, each
+    # gathered frontier row costs at least one word, the output is N bytes per source
+    alg = st["depth"] * 8 * st["words_per_vertex"] * wl.n + 8 * st["rows_gathered"] + len(sources) * wl.n
+    peak, peak_kind = peaks()
+    achieved = alg / (statistics.mean(ms) / 1e3) / 1e9
     res = {
         "workload": wl.describe() | {"sources": len(sources)}, "graph_build_s": round(build_s, 2),
         "gteps": gteps, "ms_per_batch_mean": statistics.mean(ms), "ms_per_batch_p50": statistics.median(ms),
@@ -291,6 +296,8 @@ def bench_batched(args, torch, dev):
         "plain_gpu_bfs": {"gteps": single_gteps, "ms_per_traversal_mean": statistics.mean(single_ms),
                           "sources": len(single_ms), "kernel": "k_bfs_persistent (single source)"},
         "speedup_vs_plain_gpu_bfs": gteps / single_gteps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "kernels": "k_ms_bfs + k_ms_emit", "peak_kind": peak_kind, "algorithmic_bytes_per_batch": alg},
         "parity": f"batched rows equal single-source levels on {rows_ok}/{len(check)} sources checked",
         "steps": len(ms), "l2": "flushed (256 MiB write) before every batch; batch state far above L2",
     }

@@ -8,6 +8,7 @@ are drawn until exactly E edges survive self-loop and duplicate removal.
   rmat16  : scale 16, 1,048,576 edges, W=1024, S=16 (the reference's CPU case)
   pokec   : 1,632,803 vertices, 30,622,564 edges, permuted ids, W=1024, S=16,
             64 seeded sources (the Pokec shape, tools/galois_data/rmat24.sh:7)
+  rmat18  : scale 18, 4,194,304 edges, 4096 sources (batched; profiling size)
   rmat22  : scale 22, 67,108,864 edges, 4096 sources (batched)
   twitter : 41,652,230 vertices, 1,468,365,182 edges, permuted ids, W=1024, S=16
             (the Twitter shape, tools/galois_data/rmat24.sh:19)
@@ -55,6 +56,7 @@ class Workload:
 _WORKLOADS = {
     "rmat16": Workload("rmat16", 1 << 16, 1 << 20, 1024, 16, 1, False, 16),
     "pokec": Workload("pokec", 1_632_803, 30_622_564, 1024, 16, 64, True, 2),
+    "rmat18": Workload("rmat18", 1 << 18, 1 << 22, 1024, 16, 4096, False, 18),
     "rmat22": Workload("rmat22", 1 << 22, 1 << 26, 1024, 16, 4096, False, 22),
     "twitter": Workload("twitter", 41_652_230, 1_468_365_182, 1024, 16, 16, True, 5),
 }
