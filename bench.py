@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--batch-workload", default="rmat22", help="graph of the batched measurement ('none' skips it)")
     ap.add_argument("--batch-sources", type=int, default=4096)
     ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--serve", default="c4", help="serving measurement: 'c4' (8 graphs, Poisson load) or 'none'")
+    ap.add_argument("--serve-rates", default="2000,10000,50000", help="query arrival rates (queries/s)")
+    ap.add_argument("--serve-seconds", type=float, default=1.5, help="arrival window per rate")
     return ap.parse_args()
 
 
@@ -307,6 +310,62 @@ def bench_batched(args, torch, dev):
     return res
 
 
+def bench_serving(args, torch, dev):
+    """The serving loop: 8 resident R-MAT graphs (scales 14, 16, 18-23, edge
+    factor 16) under a 40 GB HBM admission budget; open-loop Poisson arrivals
+    of (graph, source) queries drawn uniformly, coalesced per graph into
+    batches of up to 1024 sources; levels are computed and left on the device
+    (BFS_DST_NONE) so that latency measures the traversal path."""
+    import bfs_simd_benchmarks_gb300 as B
+    from bfs_simd_benchmarks_gb300 import workloads
+    t0 = time.perf_counter()
+    graphs = []
+    for wl in workloads.serve_graphs():
+        src, dst = wl.edges()
+        graphs.append((wl, B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s)))
+        del src, dst
+    build_s = time.perf_counter() - t0
+    srv = B.Server(budget_bytes=40 * 10**9)
+    for _, g in graphs:
+        srv.add_graph(g)
+    pools = [wl.sources(g.degrees(), 4096) for wl, g in graphs]
+    rng = np.random.default_rng(2024)
+
+    def trace(rate, seconds):
+        count = max(1, int(rate * seconds))
+        gids = rng.integers(0, len(graphs), count).astype(np.uint32)
+        picks = rng.integers(0, 4096, count)
+        srcs = np.array([pools[gi][k] for gi, k in zip(gids, picks)], dtype=np.uint32)
+        arr = np.cumsum(rng.exponential(1e9 / rate, count)).astype(np.uint64)
+        return gids, srcs, arr
+
+    srv.replay(*trace(5000, 0.4))  # warm-up
+    rates = []
+    with ClockSampler(dev.index or 0) as clk:
+        for rate in [float(x) for x in args.serve_rates.split(",") if x]:
+            gids, srcs, arr = trace(rate, args.serve_seconds)
+            srv.reset_stats()
+            t1 = time.perf_counter()
+            srv.replay(gids, srcs, arr)
+            wall = time.perf_counter() - t1
+            st = srv.stats()
+            rates.append({"offered_qps": rate, "queries": int(st["completed"]), "achieved_qps": st["completed"] / wall,
+                          "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+                          "max_ms": st["max_ms"], "mean_batch": st["mean_batch"], "batches": int(st["batches"]),
+                          "gteps": st["edges_traversed"] / wall / 1e9, "wall_s": wall,
+                          "slots_in_flight_mean": st["device_ms"] / 1e3 / wall})
+    res = {"graphs": [{"workload": wl.name, "vertices": wl.n, "edges": wl.m} for wl, _ in graphs],
+           "budget_bytes": 40 * 10**9, "admitted_bytes": srv.stats()["device_bytes"], "graph_build_s": round(build_s, 1),
+           "max_batch": 1024, "slots": 3, "results": "left on the device (BFS_DST_NONE)",
+           "latency": "submit -> traversal and output pass complete, host clock", "rates": rates,
+           "clocks": clk.summary()}
+    srv.close()
+    for _, g in graphs:
+        g.close()
+    torch.cuda.empty_cache()
+    return res
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -411,6 +470,9 @@ def main():
     batched = None
     if args.batch_workload != "none" and world == 1:
         batched = bench_batched(args, torch, dev)
+    serving = None
+    if args.serve != "none" and world == 1:
+        serving = bench_serving(args, torch, dev)
 
     cpu = None
     parity = None
@@ -459,6 +521,7 @@ def main():
             "cpu_baseline": cpu,
             "parity": parity,
             "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line))
     if world > 1:

@@ -6,6 +6,7 @@ csrc/; this package holds the ctypes mirror of that ABI.
 from ._native import BfsError, load as load_library  # noqa: F401
 from .graph import (  # noqa: F401
     Graph,
+    Server,
     gen_rmat,
     pick_sources,
     tool_column_major,
@@ -17,6 +18,6 @@ from .graph import (  # noqa: F401
 )
 
 __all__ = [
-    "BfsError", "Graph", "gen_rmat", "load_library", "pick_sources", "tool_column_major",
+    "BfsError", "Graph", "Server", "gen_rmat", "load_library", "pick_sources", "tool_column_major",
     "tool_coo_tiling", "tool_csr_tiling", "tool_vertex_remap", "write_edge_list", "write_level_dump",
 ]

@@ -142,6 +142,55 @@ class Stats(C.Structure):
         return d
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [
+        ("budget_bytes", C.c_uint64),
+        ("slot_bytes", C.c_uint64),
+        ("max_batch", C.c_uint32),
+        ("num_slots", C.c_uint32),
+        ("planes", C.c_uint32),
+        ("max_pending", C.c_uint32),
+    ]
+
+
+class QueryResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32),
+        ("batch_size", C.c_uint32),
+        ("batch_id", C.c_uint64),
+        ("latency_ms", C.c_double),
+        ("queue_ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_uint64),
+        ("completed", C.c_uint64),
+        ("refused", C.c_uint64),
+        ("batches", C.c_uint64),
+        ("edges_traversed", C.c_uint64),
+        ("p50_ms", C.c_double),
+        ("p99_ms", C.c_double),
+        ("mean_ms", C.c_double),
+        ("max_ms", C.c_double),
+        ("mean_batch", C.c_double),
+        ("device_ms", C.c_double),
+        ("device_bytes", C.c_uint64),
+        ("graphs", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+BFS_DST_NONE, BFS_DST_HOST, BFS_DST_DEVICE = 0, 1, 2
+
+
 class RmatParams(C.Structure):
     _fields_ = [
         ("num_vertices", C.c_uint32),
@@ -175,6 +224,17 @@ _SIGNATURES = [
     ("bfs_last_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     ("bfs_run_batch", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(BatchStats)]),
     ("bfs_last_batch_stats", C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
+    ("bfs_server_options_default", C.c_int, [C.POINTER(ServerOptions)]),
+    ("bfs_server_create", C.c_int, [C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
+    ("bfs_server_add_graph", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32)]),
+    ("bfs_server_submit", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32,
+                                    C.POINTER(C.c_uint64)]),
+    ("bfs_server_wait", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(QueryResult)]),
+    ("bfs_server_drain", C.c_int, [C.c_void_p]),
+    ("bfs_server_replay", C.c_int, [C.c_void_p, C.c_uint32, _u32p, _u32p, C.POINTER(C.c_uint64)]),
+    ("bfs_server_get_stats", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    ("bfs_server_reset_stats", C.c_int, [C.c_void_p]),
+    ("bfs_server_destroy", C.c_int, [C.c_void_p]),
     ("bfs_run_noalloc", C.c_int, [C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("bfs_write_level_dump", C.c_int, [C.c_char_p, C.c_uint32, _i32p]),
     ("bfs_tool_csr_tiling", C.c_int, [C.c_char_p, C.c_uint32]),

@@ -505,7 +505,8 @@ int batch_prepare(bfs_graph *g, uint32_t K, uint32_t *planes_out) {
 	return BFS_OK;
 }
 
-int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *levels, cudaStream_t st) {
+int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *levels, cudaStream_t st,
+		cudaEvent_t wait_before = nullptr, cudaEvent_t between = nullptr) {
 	if (g->host_only) return BFS_EUNSUPPORTED;
 	if (!sources || !levels || ns == 0 || ns > BFS_BATCH_MAX_SOURCES) return BFS_EARG;
 	for (uint32_t i = 0; i < ns; ++i)
@@ -537,7 +538,8 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 	// pageable source: the copy has left `sources` when the call returns
 	if (cudaMemcpyAsync(b.d_sources, sources, sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, st) != cudaSuccess)
 		return BFS_ECUDA;
-	if ((rc = ms_launch(a, b.d_sources, ns, levels, g->num_sms, st, &b.grid, b.em))) return rc;
+	if (wait_before && cudaStreamWaitEvent(st, wait_before, 0) != cudaSuccess) return BFS_ECUDA;
+	if ((rc = ms_launch(a, b.d_sources, ns, levels, g->num_sms, st, &b.grid, b.em, between))) return rc;
 	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
 	b.args.planes = planes;
 	b.args.K = K;
@@ -597,6 +599,35 @@ int collect_batch_stats(bfs_graph *g, bfs_batch_stats *out) {
 }
 
 } // namespace
+
+// ---- hooks of the serving loop (server.cpp) ---------------------------------
+namespace bfsg {
+
+int batch_reserve(bfs_graph *g, uint32_t K, uint32_t planes, size_t *batch_bytes) {
+	if (!g || g->host_only) return BFS_EUNSUPPORTED;
+	if (K == 0 || K > BFS_BATCH_MAX_SOURCES / 64 || planes < 2 || planes > kMsMaxLevel + 1) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	g->opt.batch_planes = planes;
+	uint32_t p = 0;
+	int st = batch_prepare(g, K, &p);
+	if (batch_bytes) *batch_bytes = g->mb.bytes;
+	return st;
+}
+
+int run_batch_ex(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *levels, cudaStream_t st,
+		cudaEvent_t wait_before, cudaEvent_t between) {
+	if (!g) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	return run_batch_impl(g, sources, ns, levels, st, wait_before, between);
+}
+
+size_t graph_device_bytes(const bfs_graph *g) { return g ? g->device_bytes : 0; }
+uint32_t graph_num_vertices(const bfs_graph *g) { return g ? g->n : 0; }
+int graph_device(const bfs_graph *g) { return g ? g->device : -1; }
+bool graph_on_device(const bfs_graph *g) { return g && !g->host_only; }
+
+} // namespace bfsg
 
 extern "C" {
 

@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_emit(MsArgs a, uint32_t ns
 }
 
 int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *levels, int num_sms, cudaStream_t st,
-		int *grid, cudaEvent_t between) {
+		int *grid, cudaEvent_t between, cudaEvent_t between2) {
 	int per_sm = 0;
 	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ms_bfs, kMsThreads, 0) != cudaSuccess || per_sm < 1)
 		return BFS_ECUDA;
@@ -651,6 +651,7 @@ int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *
 			cudaSuccess)
 		return BFS_ECUDA;
 	if (between && cudaEventRecord(between, st) != cudaSuccess) return BFS_ECUDA;
+	if (between2 && cudaEventRecord(between2, st) != cudaSuccess) return BFS_ECUDA;
 	k_ms_emit<<<num_sms * 2, kMsThreads, 0, st>>>(a, ns, levels);
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }

@@ -68,9 +68,10 @@ struct MsArgs {
 };
 
 // Enqueues the whole batched traversal (one cooperative launch and the
-// output pass) on `st`; `between` (may be null) is recorded between the two;
+// output pass) on `st`; `between` and `between2` (either may be null) are
+// recorded between the two;
 // *grid receives the launch's CTA count.
 int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *levels, int num_sms, cudaStream_t st,
-		int *grid, cudaEvent_t between);
+		int *grid, cudaEvent_t between, cudaEvent_t between2);
 
 } // namespace bfsg

@@ -174,6 +174,84 @@ class Graph:
         return st.as_dict()
 
 
+class Server:
+    """The serving loop (bfs_server_*): resident graphs, queries coalesced per
+    graph into batched traversals under a device-memory budget."""
+
+    def __init__(self, budget_bytes: int | None = None, slot_bytes: int | None = None, max_batch: int | None = None,
+                 num_slots: int | None = None, planes: int | None = None, max_pending: int | None = None):
+        lib = N.load()
+        o = N.ServerOptions()
+        N.check(lib.bfs_server_options_default(C.byref(o)), "bfs_server_options_default")
+        for k, v in dict(budget_bytes=budget_bytes, slot_bytes=slot_bytes, max_batch=max_batch,
+                         num_slots=num_slots, planes=planes, max_pending=max_pending).items():
+            if v is not None:
+                setattr(o, k, int(v))
+        h = C.c_void_p()
+        N.check(lib.bfs_server_create(C.byref(o), C.byref(h)), "bfs_server_create")
+        self._h = h
+        self._graphs = []  # keep the graphs alive as long as the server
+
+    def add_graph(self, g: Graph) -> int:
+        gid = C.c_uint32()
+        N.check(N.load().bfs_server_add_graph(self._h, g.handle, C.byref(gid)), "bfs_server_add_graph")
+        self._graphs.append(g)
+        return gid.value
+
+    def submit(self, graph_id: int, source: int, dst_ptr: int = 0, kind: int = N.BFS_DST_NONE) -> int:
+        t = C.c_uint64()
+        N.check(N.load().bfs_server_submit(self._h, graph_id, int(source), C.c_void_p(dst_ptr) if dst_ptr else None,
+                                           kind, C.byref(t)), "bfs_server_submit")
+        return t.value
+
+    def submit_host(self, graph_id: int, source: int, out: np.ndarray) -> int:
+        """Queues a query whose uint8 levels land in `out` (host, N bytes; keep it alive until wait)."""
+        assert out.dtype == np.uint8 and out.flags["C_CONTIGUOUS"]
+        return self.submit(graph_id, source, out.ctypes.data, N.BFS_DST_HOST)
+
+    def wait(self, ticket: int) -> dict:
+        r = N.QueryResult()
+        st = N.load().bfs_server_wait(self._h, ticket, C.byref(r))
+        N.check(st, f"bfs_server_wait({ticket})")
+        return r.as_dict()
+
+    def drain(self) -> None:
+        N.check(N.load().bfs_server_drain(self._h), "bfs_server_drain")
+
+    def replay(self, graph_ids, sources, arrival_ns) -> None:
+        g = _u32(graph_ids)
+        s = _u32(sources)
+        a = np.ascontiguousarray(arrival_ns, dtype=np.uint64)
+        N.check(N.load().bfs_server_replay(self._h, g.size, _ptr(g, C.c_uint32), _ptr(s, C.c_uint32),
+                                           a.ctypes.data_as(C.POINTER(C.c_uint64))), "bfs_server_replay")
+
+    def stats(self) -> dict:
+        st = N.ServerStats()
+        N.check(N.load().bfs_server_get_stats(self._h, C.byref(st)), "bfs_server_get_stats")
+        return st.as_dict()
+
+    def reset_stats(self) -> None:
+        N.check(N.load().bfs_server_reset_stats(self._h), "bfs_server_reset_stats")
+
+    def close(self) -> None:
+        if self._h:
+            N.load().bfs_server_destroy(self._h)
+            self._h = None
+            self._graphs = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ---- tools (the reference's tools/ CLIs) ------------------------------
 def tool_csr_tiling(edge_list: str, weighted: bool = False) -> None:
     N.check(N.load().bfs_tool_csr_tiling(edge_list.encode(), N.BFS_LOAD_WEIGHTED if weighted else 0),

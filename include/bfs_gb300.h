@@ -232,6 +232,79 @@ int bfs_run_batch(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, u
 		bfs_batch_stats *stats);
 int bfs_last_batch_stats(bfs_graph *g, bfs_batch_stats *stats);
 
+/* ---- serving loop (no counterpart in the reference) ---------------------
+ * A server keeps several graphs resident in HBM and answers single-source
+ * queries (graph, source) by coalescing the queries waiting on one graph into
+ * one bfs_run_batch traversal.  Admission is by a device-memory budget: a
+ * graph is admitted with its batch state (reserved up front) only if graphs +
+ * batch states + result slots fit; a batch takes as many waiting queries as
+ * its result slot holds.  Batches of different graphs are in flight at once
+ * on their own streams (their traversals run one after another on the GPU;
+ * output passes and result copies overlap the next traversal); queries that
+ * arrive meanwhile join the next batch of their graph as soon as a slot is
+ * free (continuous batching).  A query's levels are the same as bfs_run's for
+ * that source (as uint8, 255 = unreached) whatever else is in the mix.  The
+ * server starts its own threads; all entry points are thread-safe.  Graphs
+ * stay owned by the caller and must outlive the server.
+ */
+typedef struct bfs_server bfs_server;
+
+typedef struct bfs_server_options {
+	uint64_t budget_bytes;  /* HBM admission budget: graphs + batch states + result slots (default 40 GiB) */
+	uint64_t slot_bytes;    /* device result buffer of one batch (default 2 GiB): at most slot_bytes / N queries
+	                           of an N-vertex graph share a traversal */
+	uint32_t max_batch;     /* queries per traversal (1..BFS_BATCH_MAX_SOURCES, default 1024) */
+	uint32_t num_slots;     /* batches in flight (1..16, default 3) */
+	uint32_t planes;        /* level planes of each graph's batch state (2..255, default 8) */
+	uint32_t max_pending;   /* waiting queries before submit answers BFS_EBUDGET (default 1 << 20) */
+} bfs_server_options;
+
+#define BFS_DST_NONE 0u   /* keep no levels (load generation) */
+#define BFS_DST_HOST 1u   /* dst is host memory of N bytes */
+#define BFS_DST_DEVICE 2u /* dst is device memory of N bytes */
+
+typedef struct bfs_query_result {
+	int32_t status;        /* BFS_OK or the traversal's error */
+	uint32_t batch_size;   /* queries in the traversal that served this one */
+	uint64_t batch_id;
+	double latency_ms;     /* submit -> levels written (or the traversal done, BFS_DST_NONE) */
+	double queue_ms;       /* submit -> its traversal was launched */
+} bfs_query_result;
+
+typedef struct bfs_server_stats {
+	uint64_t submitted;
+	uint64_t completed;
+	uint64_t refused;          /* submits answered BFS_EBUDGET */
+	uint64_t batches;
+	uint64_t edges_traversed;  /* sum over completed queries of m(s) */
+	double p50_ms, p99_ms, mean_ms, max_ms;  /* query latency since the last reset */
+	double mean_batch;         /* queries per traversal */
+	double device_ms;          /* sum of the traversals' device time */
+	uint64_t device_bytes;     /* admitted: graphs + batch states + result slots */
+	uint32_t graphs;
+	uint32_t reserved;
+} bfs_server_stats;
+
+int bfs_server_options_default(bfs_server_options *opt);
+int bfs_server_create(const bfs_server_options *opt, bfs_server **out);
+/* Admits a resident graph (BFS_EBUDGET when it does not fit; the graph is then
+ * left as it was apart from its batch options). */
+int bfs_server_add_graph(bfs_server *s, bfs_graph *g, uint32_t *graph_id);
+int bfs_server_submit(bfs_server *s, uint32_t graph_id, uint32_t source, void *dst, uint32_t dst_kind,
+		uint64_t *ticket);
+/* Waits for a query (each ticket is waited for once). */
+int bfs_server_wait(bfs_server *s, uint64_t ticket, bfs_query_result *result);
+/* Waits until every query submitted so far has completed. */
+int bfs_server_drain(bfs_server *s);
+/* Open-loop load: submits query i (graph_ids[i], sources[i], levels discarded)
+ * arrival_ns[i] nanoseconds after the call starts (non-decreasing), then
+ * drains.  Returns the first error, if any. */
+int bfs_server_replay(bfs_server *s, uint32_t count, const uint32_t *graph_ids, const uint32_t *sources,
+		const uint64_t *arrival_ns);
+int bfs_server_get_stats(bfs_server *s, bfs_server_stats *stats);
+int bfs_server_reset_stats(bfs_server *s);
+int bfs_server_destroy(bfs_server *s);
+
 /* ---- allocation-free traversal (no counterpart in the reference) -------- */
 #define BFS_NOALLOC_MAX_VERTICES (1u << 20)
 

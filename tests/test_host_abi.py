@@ -270,3 +270,23 @@ def test_cli_usage_and_missing_files(native, tmp_path):
     assert r.returncode == 1 and r.stdout.startswith("Usage: ./bfs <data> <tile_width> <stripe_length>")
     r = subprocess.run([build.CLI, str(tmp_path / "none"), "1024", "16"], capture_output=True, text=True)
     assert r.returncode == 1 and "cannot open file" in r.stderr
+
+
+def test_server_option_errors_without_device(native):
+    """Invalid server options are refused before any device work; with no GPU
+    the server reports BFS_ENODEV instead of failing later."""
+    import bfs_simd_benchmarks_gb300 as B
+    from conftest import gpu_available
+    with pytest.raises(B.BfsError) as ei:
+        B.Server(max_batch=0)
+    assert ei.value.status == 4
+    with pytest.raises(B.BfsError) as ei:
+        B.Server(num_slots=17)
+    assert ei.value.status == 4
+    with pytest.raises(B.BfsError) as ei:
+        B.Server(budget_bytes=1 << 20, slot_bytes=1 << 20, num_slots=2)
+    assert ei.value.status == 5
+    if not gpu_available():
+        with pytest.raises(B.BfsError) as ei:
+            B.Server()
+        assert ei.value.status == 9
