@@ -71,6 +71,8 @@ class Options(C.Structure):
         ("bottom_up", C.c_uint32),
         ("batch_planes", C.c_uint32),
         ("batch_budget_mb", C.c_uint32),
+        ("batch_single_max", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 
@@ -95,10 +97,12 @@ class BatchStats(C.Structure):
         ("level_phase_ms", (C.c_float * 3) * BFS_BATCH_TRACE_LEVELS),
         ("setup_ms", C.c_double),
         ("output_ms", C.c_double),
+        ("single_source_runs", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("level_")}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("level_") and k != "reserved"}
         k = min(self.depth, BFS_BATCH_TRACE_LEVELS)
         d["level_ms"] = [round(x, 4) for x in self.level_ms[:k]]
         d["level_frontier"] = list(self.level_frontier[:k])

@@ -76,6 +76,7 @@ struct bfs_graph {
 		uint32_t num_sources = 0;
 		int grid = 0;
 		bool have_run = false, fresh = false;
+		bool singles = false;        // the last batch ran as single-source traversals
 		size_t bytes = 0;
 		std::vector<DevBuf> bufs;
 	} mb;
@@ -147,6 +148,7 @@ void default_options(bfs_options *o) {
 	o->bottom_up = BFS_BU_PULL;
 	o->batch_planes = 0;
 	o->batch_budget_mb = 40960;
+	o->batch_single_max = 4;
 }
 
 // Builds the device copy of a validated host graph.
@@ -499,10 +501,42 @@ int batch_prepare(bfs_graph *g, uint32_t K, uint32_t *planes_out) {
 	if ((st = batch_alloc(g, &a.queue[1], g->n))) return st;
 	if ((st = batch_alloc(g, &a.ctl, 1))) return st;
 	if ((st = batch_alloc(g, &b.d_sources, BFS_BATCH_MAX_SOURCES))) return st;
+	// push chunk list: a vertex above the grid-spread degree has > 1024 edges, so
+	// its chunks number at most E / 1024 + the vertices, at most 2 E / 1024
+	a.push_cap = (uint32_t) std::min<uint64_t>(0xFFFFFFFFull, 2 * g->m / kMsPushChunk + 1);
+	if ((st = batch_alloc(g, &a.push_u, a.push_cap))) return st;
+	if ((st = batch_alloc(g, &a.push_beg, a.push_cap))) return st;
 	b.k_alloc = K;
 	b.planes_alloc = planes;
 	*planes_out = planes;
 	return BFS_OK;
+}
+
+// One single-source traversal's int32 levels -> a uint8 row (255 = unreached);
+// adds the traversal's edge count, depth and status to the batch statistics.
+__global__ void __launch_bounds__(512) k_levels_u8(const int32_t *lev, uint8_t *out, uint32_t n, const DevStats *ds,
+		MsControl *ctl) {
+	const uint32_t stride = gridDim.x * blockDim.x;
+	uint32_t mx = 0;
+	bool over = false;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+		const int32_t l = lev[i];
+		uint8_t x = 255;
+		if (l >= 0) {
+			over |= l > (int32_t) kMsMaxLevel;
+			x = (uint8_t) min(l, (int32_t) kMsMaxLevel);
+			mx = max(mx, (uint32_t) l + 1);
+		}
+		out[i] = x;
+	}
+	for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, d));
+	if ((threadIdx.x & 31) == 0 && mx) atomicMax(&ctl->stats.depth, mx);
+	if (over) atomicExch(&ctl->err, BFS_EUNSUPPORTED);
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		atomicAdd(&ctl->stats.traversed, ds->edges_traversed);
+		if (ds->status) atomicExch(&ctl->err, ds->status);
+		ctl->stats.complete = 1;
+	}
 }
 
 int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *levels, cudaStream_t st,
@@ -535,12 +569,42 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 	a.nbig_in = g->ms_nbig_in;
 	a.nchunks = g->ms_nchunks;
 	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
-	// pageable source: the copy has left `sources` when the call returns
-	if (cudaMemcpyAsync(b.d_sources, sources, sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, st) != cudaSuccess)
-		return BFS_ECUDA;
-	if (wait_before && cudaStreamWaitEvent(st, wait_before, 0) != cudaSuccess) return BFS_ECUDA;
-	if ((rc = ms_launch(a, b.d_sources, ns, levels, g->num_sms, st, &b.grid, b.em, between))) return rc;
+	const bool singles = ns <= g->opt.batch_single_max && g->opt.mode == BFS_MODE_PERSISTENT;
+	if (singles) {
+		// a few sources: one single-source traversal each (queue-driven, no
+		// sweeps over all vertices), rows converted to uint8 on the device
+		if (wait_before && cudaStreamWaitEvent(st, wait_before, 0) != cudaSuccess) return BFS_ECUDA;
+		if (cudaMemsetAsync(a.ctl, 0, sizeof(MsControl), st) != cudaSuccess) return BFS_ECUDA;
+		RunCtx r = g->rc;
+		r.level = g->level_buf;
+		r.parent = g->parent_buf;
+		StepParams p{};
+		p.warp_max_degree = g->opt.warp_max_degree;
+		p.cta_max_degree = g->opt.cta_max_degree;
+		p.bottom_up = g->opt.bottom_up;
+		p.to_dense_threshold = g->m / std::max<uint32_t>(1, g->opt.to_dense_ratio);
+		p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
+		for (uint32_t i = 0; i < ns; ++i) {
+			p.source = sources[i];
+			if ((rc = launch_init(g->dg, r, st, g->num_sms))) return rc;
+			if ((rc = launch_persistent(g->dg, r, p, g->batch, g->grid, g->smem, st))) return rc;
+			k_levels_u8<<<g->num_sms * 4, 512, 0, st>>>(g->level_buf, levels + (size_t) i * g->n, g->n, r.stats, a.ctl);
+		}
+		if (cudaGetLastError() != cudaSuccess) return BFS_ECUDA;
+		if (cudaEventRecord(b.em, st) != cudaSuccess) return BFS_ECUDA;
+		if (between && cudaEventRecord(between, st) != cudaSuccess) return BFS_ECUDA;
+		b.grid = g->grid;
+		// the single-source statistics now describe the last of these runs
+		g->have_run = false;
+	} else {
+		// pageable source: the copy has left `sources` when the call returns
+		if (cudaMemcpyAsync(b.d_sources, sources, sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, st) != cudaSuccess)
+			return BFS_ECUDA;
+		if (wait_before && cudaStreamWaitEvent(st, wait_before, 0) != cudaSuccess) return BFS_ECUDA;
+		if ((rc = ms_launch(a, b.d_sources, ns, levels, g->num_sms, st, &b.grid, b.em, between))) return rc;
+	}
 	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
+	b.singles = singles;
 	b.args.planes = planes;
 	b.args.K = K;
 	b.num_sources = ns;
@@ -579,6 +643,7 @@ int collect_batch_stats(bfs_graph *g, bfs_batch_stats *out) {
 	s.setup_ms = c.stats.t_levels0 > c.stats.t_start ? (c.stats.t_levels0 - c.stats.t_start) * 1e-6 : 0.0;
 	s.levels_ms = c.stats.t_levels1 > c.stats.t_levels0 ? (c.stats.t_levels1 - c.stats.t_levels0) * 1e-6 : 0.0;
 	s.device_bytes = b.bytes;
+	s.single_source_runs = b.singles ? b.num_sources : 0;
 	const uint32_t nl = std::min<uint32_t>(c.stats.depth, kMsTraceLevels);
 	for (uint32_t l = 0; l < nl; ++l) {
 		const unsigned long long t0 = c.stats.t_level[l], t1 = c.stats.t_level[l + 1];

@@ -105,6 +105,42 @@ __device__ __forceinline__ void ms_push_edges(const MsArgs &a, const uint64_t *c
 	}
 }
 
+// Push level, CTA 0: cuts the high-degree frontier vertices (the queue's back)
+// into kMsPushChunk-edge chunks, listed in push_u / push_beg, so that warps
+// all over the grid take them like small vertices.  A block-wide scan of the
+// chunk counts, 512 vertices at a time.
+__device__ void ms_push_chunk_list(const MsArgs &a, uint32_t lvl, uint32_t nb, uint32_t *scan_s) {
+	const uint32_t *q = a.queue[lvl & 1];
+	uint32_t running = 0;
+	for (uint32_t base = 0; base < nb; base += blockDim.x) {
+		const uint32_t i = base + threadIdx.x;
+		uint32_t u = 0, c = 0, beg = 0, end = 0;
+		if (i < nb) {
+			u = ld_cg(q + a.n - 1 - i);
+			beg = __ldg(a.row_off + u);
+			end = __ldg(a.row_off + u + 1);
+			c = (end - beg + kMsPushChunk - 1) / kMsPushChunk;
+		}
+		const uint32_t incl = warp_incl_scan(c);
+		if (lane_id() == 31) scan_s[warp_id()] = incl;
+		__syncthreads();
+		uint32_t before = 0, total = 0;
+		for (int w = 0; w < kMsWarps; ++w) {
+			const uint32_t t = scan_s[w];
+			if (w < (int) warp_id()) before += t;
+			total += t;
+		}
+		uint32_t pos = running + before + incl - c;
+		for (uint32_t k = 0; k < c && pos < a.push_cap; ++k, ++pos) {
+			a.push_u[pos] = u;
+			a.push_beg[pos] = beg + k * kMsPushChunk;
+		}
+		running += total;
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) a.ctl->push_chunks = min(running, a.push_cap);
+}
+
 __device__ void ms_push(const MsArgs &a, uint32_t lvl, const uint64_t *cur, const uint64_t *actc, uint64_t *nxt, uint32_t nq,
 		uint32_t nb) {
 	const uint32_t *q = a.queue[lvl & 1];
@@ -114,9 +150,12 @@ __device__ void ms_push(const MsArgs &a, uint32_t lvl, const uint64_t *cur, cons
 		const uint32_t u = ld_cg(q + i);
 		ms_push_edges(a, cur, actc, nxt, u, __ldg(a.row_off + u), __ldg(a.row_off + u + 1), 0, 32);
 	}
-	for (uint32_t i = 0; i < nb; ++i) {
-		const uint32_t u = ld_cg(q + a.n - 1 - i);
-		ms_push_edges(a, cur, actc, nxt, u, __ldg(a.row_off + u), __ldg(a.row_off + u + 1), gwarp * 32, nwarps * 32);
+	if (!nb) return;
+	const uint32_t nc = ld_volatile(&a.ctl->push_chunks);
+	for (uint32_t c = gwarp; c < nc; c += nwarps) {
+		const uint32_t u = ld_cg(a.push_u + c), beg = ld_cg(a.push_beg + c);
+		const uint32_t end = min(beg + kMsPushChunk, __ldg(a.row_off + u + 1));
+		ms_push_edges(a, cur, actc, nxt, u, beg, end, 0, 32);
 	}
 }
 
@@ -558,6 +597,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 		unsigned long long actdeg = 0;
 		const bool push = qdeg * (unsigned long long) a.push_div < (unsigned long long) a.m;
 		if (push) {
+			if (blockIdx.x == 0 && nb) ms_push_chunk_list(a, lvl, nb, wq);
 			for (size_t i = t0; i < nK; i += stride) nxt[i] = 0;
 			if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
 			if (leader && tph) tph[0] = global_timer_ns();

@@ -11,6 +11,7 @@ constexpr uint32_t kMsMaxLevel = 254;  // uint8 levels; 255 = unreached
 constexpr uint32_t kMsTraceLevels = 64; // levels with per-level statistics
 constexpr uint32_t kMsPullBig = 256;    // pull: destinations with more in-edges are split ...
 constexpr uint32_t kMsChunk = 256;      // ... into chunks of this many in-edges
+constexpr uint32_t kMsPushChunk = 1024; // push: high-degree vertices' edges go out in chunks of this many
 
 struct MsCounters {
 	unsigned int nact;            // frontier vertices of degree <= kMsBig (queue front)
@@ -40,7 +41,7 @@ struct MsStats {
 struct MsControl {
 	unsigned bar[2];
 	int err;
-	int pad;
+	unsigned push_chunks;  // push level: 1024-edge chunks of its high-degree frontier vertices
 	MsCounters ctr[3];
 	MsStats stats;
 };
@@ -57,6 +58,8 @@ struct MsArgs {
 	const uint32_t *row_off, *col, *in_off, *in_src;
 	const uint32_t *in_big;              // [nbig_in] those destinations
 	const uint32_t *chunk_v, *chunk_beg; // [nchunks] destination and first in-edge of each chunk
+	uint32_t *push_u, *push_beg;         // [push_cap] push: vertex and first edge of each 1024-edge chunk
+	uint32_t push_cap;
 	uint64_t *vis;        // [n][K] sources that reached v
 	uint64_t *hist;       // [planes][n][K] sources that reached v first at level base + plane
 	uint64_t *pmask;      // [planes][n] bit k: word k of v's row in that plane is non-zero

@@ -113,7 +113,7 @@ class Graph:
     def options(self) -> dict:
         o = N.Options()
         N.check(N.load().bfs_get_options(self._h, C.byref(o)), "bfs_get_options")
-        return {k: getattr(o, k) for k, _ in N.Options._fields_}
+        return {k: getattr(o, k) for k, _ in N.Options._fields_ if k != "reserved"}
 
     def set_options(self, **kw) -> None:
         o = N.Options()

@@ -126,6 +126,9 @@ typedef struct bfs_options {
 	uint32_t bottom_up;        /* BFS_BU_PULL or BFS_BU_STREAM */
 	uint32_t batch_planes;     /* bfs_run_batch: level planes (2..255); 0 = from batch_budget_mb, at most 32 */
 	uint32_t batch_budget_mb;  /* bfs_run_batch: HBM budget of the level planes in MiB (default 40960) */
+	uint32_t batch_single_max; /* bfs_run_batch: batches of at most this many sources run as back-to-back
+	                              single-source traversals (default 4; 0 = always bit-sliced) */
+	uint32_t reserved;
 } bfs_options;
 
 /* Bottom-up step variants.  PULL: every unvisited destination of a column
@@ -213,6 +216,9 @@ typedef struct bfs_batch_stats {
 	                                                    push: clear, expand, finish */
 	double setup_ms;           /* clearing and seeding (device clock) */
 	double output_ms;          /* the output pass (CUDA events) */
+	uint32_t single_source_runs; /* > 0: the batch ran as that many single-source traversals
+	                                (batch_single_max); the per-level fields are then empty */
+	uint32_t reserved;
 } bfs_batch_stats;
 
 /*

@@ -41,14 +41,19 @@ def _check(oracle, arr, g, sources, expect=None):
     return got, st
 
 
+@pytest.mark.parametrize("single_max", [0, 4])
 @pytest.mark.parametrize("name", [c for c in golden_case_names() if not c.startswith("chain")])
-def test_golden_sources_batched(native, oracle, name):
+def test_golden_sources_batched(native, oracle, name, single_max):
+    """single_max 0: the bit-sliced kernel even for 4 sources; 4: the
+    back-to-back single-source path that small batches take."""
     import bfs_simd_benchmarks_gb300 as B
     c = load_case(name)
     arr = oracle.arrays_from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"])
     exp = np.where(c["levels"] < 0, 255, c["levels"]).astype(np.uint8)
     with B.Graph.from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"]) as g:
-        _check(oracle, arr, g, [int(x) for x in c["sources"]], exp)
+        g.set_options(batch_single_max=single_max)
+        _, st = _check(oracle, arr, g, [int(x) for x in c["sources"]], exp)
+        assert st["single_source_runs"] == (len(c["sources"]) if len(c["sources"]) <= single_max else 0)
 
 
 def test_partial_word_and_repeated_sources(native, oracle):
@@ -137,11 +142,13 @@ def test_aligned_rows_vector_path_and_offset_output(native, oracle):
         np.testing.assert_array_equal(got[1:].reshape(len(srcs), n), exp)
 
 
-def test_levels_above_254_are_refused(native, oracle):
+@pytest.mark.parametrize("single_max", [0, 4])
+def test_levels_above_254_are_refused(native, oracle, single_max):
     import bfs_simd_benchmarks_gb300 as B
     n = 300
     src = np.arange(299, dtype=np.uint32)
     with B.Graph.from_edges(n, src, src + 1, 32, 2) as g:
+        g.set_options(batch_single_max=single_max)
         with pytest.raises(B.BfsError) as ei:
             g.run_batch([0, 1])
         assert ei.value.status == 8  # BFS_EUNSUPPORTED
