@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--batch-workload", default="rmat22", help="graph of the batched measurement ('none' skips it)")
     ap.add_argument("--batch-sources", type=int, default=4096)
     ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--batch-budget-mb", type=int, default=40960, help="HBM budget of the batched level planes")
     ap.add_argument("--serve", default="c4", help="serving measurement: 'c4' (8 graphs, Poisson load) or 'none'")
     ap.add_argument("--serve-rates", default="2000,10000,50000", help="query arrival rates (queries/s)")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="arrival window per rate")
@@ -221,18 +222,23 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def bench_batched(args, torch, dev):
+def bench_batched(args, torch, dev, graph=None, build_s=0.0):
     """Batched multi-source BFS (bfs_run_batch): every step traverses all the
     sources at once and writes uint8 levels [sources][N] into HBM.  Compared
-    with the single-source kernel on the same graph (the plain GPU BFS)."""
+    with the single-source kernel on the same graph (the plain GPU BFS).
+    `graph` is the single-source workload's graph when both are the same."""
     import bfs_simd_benchmarks_gb300 as B
     from bfs_simd_benchmarks_gb300 import workloads
     wl = workloads.get(args.batch_workload)
-    t0 = time.perf_counter()
-    src, dst = wl.edges()
-    g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s)
-    build_s = time.perf_counter() - t0
-    del src, dst
+    if graph is None:
+        t0 = time.perf_counter()
+        src, dst = wl.edges()
+        g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s)
+        build_s = time.perf_counter() - t0
+        del src, dst
+    else:
+        g = graph
+    g.set_options(batch_budget_mb=args.batch_budget_mb)
     deg = g.degrees()
     sources = wl.sources(deg, args.batch_sources)
     out = torch.empty((len(sources), wl.n), dtype=torch.uint8, device=dev)
@@ -304,7 +310,8 @@ def bench_batched(args, torch, dev):
         "parity": f"batched rows equal single-source levels on {rows_ok}/{len(check)} sources checked",
         "steps": len(ms), "l2": "flushed (256 MiB write) before every batch; batch state far above L2",
     }
-    g.close()
+    if graph is None:
+        g.close()
     del out
     torch.cuda.empty_cache()
     return res
@@ -469,7 +476,8 @@ def main():
 
     batched = None
     if args.batch_workload != "none" and world == 1:
-        batched = bench_batched(args, torch, dev)
+        same = args.batch_workload == args.workload
+        batched = bench_batched(args, torch, dev, g if same else None, t_gen if same else 0.0)
     serving = None
     if args.serve != "none" and world == 1:
         serving = bench_serving(args, torch, dev)
@@ -493,7 +501,7 @@ def main():
             "config": dict(wl.describe(), step=f"{len(sources)} single-source traversals",
                            parallelism="replicas" if world > 1 else "single GPU", mode=args.mode,
                            bottom_up=args.bottom_up,
-                           l2="flushed (256 MiB write) before every traversal; graph 245 MB > L2",
+                           l2=f"flushed (256 MiB write) before every traversal; graph {info['device_bytes'] / 1e6:.0f} MB > L2",
                            grid_ctas=timed[0][2]["grid_ctas"], column_groups=info["num_groups"],
                            graph_build_s=round(t_gen, 2)),
             "single_source": {"gteps": value, "ms_per_traversal_mean": statistics.mean(trav_ms),

@@ -558,7 +558,6 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 	a.last_bits = ns - 64 * (K - 1);
 	a.planes = planes;
 	a.push_div = kBatchPushDiv;
-	a.vec_out = (g->n % 16 == 0 && ((uintptr_t) levels % 16) == 0) ? 1u : 0u;
 	a.row_off = g->dg.row_off;
 	a.col = g->dg.col;
 	a.in_off = g->dg.in_off;

@@ -448,7 +448,6 @@ __device__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t ns, uint32_t 
 		const uint32_t v0 = (tile % vtiles) * kEmitV, k0 = (tile / vtiles) * kEmitW;
 		const uint32_t nv = min(kEmitV, n - v0);
 		const uint32_t nrows = min(kRows, ns - k0 * 64);
-		const bool vec = a.vec_out && nv == kEmitV;
 		// 1. this thread's 64 level bytes
 		if (vi < nv && k0 + wi < K) {
 			const uint32_t v = v0 + vi, k = k0 + wi;
@@ -482,31 +481,51 @@ __device__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t ns, uint32_t 
 				for (int b = 0; b < 4; ++b) col[(4 * q + b) * kEmitStride] = (uint8_t) (o[q] >> (8 * b));
 		}
 		__syncthreads();
-		// 2. rows out
+		// 2. rows out: 16-byte pieces, stored with the widest unit the row's
+		// alignment allows (rows of an N-byte stride start anywhere)
 		for (uint32_t idx = threadIdx.x; idx < kRows * (kEmitV / 16); idx += blockDim.x) {
 			const uint32_t r = idx / (kEmitV / 16), c = (idx % (kEmitV / 16)) * 16;
-			if (r >= nrows) continue;
+			if (r >= nrows || c >= nv) continue;
 			uint8_t *dst = levels + (size_t) (k0 * 64 + r) * n + v0 + c;
 			const uint8_t *sp = lev + r * kEmitStride + c;
-			if (vec) {
-				uint4 x;
-				x.x = *(const uint32_t *) (sp + 0);
-				x.y = *(const uint32_t *) (sp + 4);
-				x.z = *(const uint32_t *) (sp + 8);
-				x.w = *(const uint32_t *) (sp + 12);
+			uint32_t x[4];
+#pragma unroll
+			for (int q = 0; q < 4; ++q) x[q] = *(const uint32_t *) (sp + 4 * q);
+			const uint32_t cnt = min(16u, nv - c);
+			const uintptr_t al = (uintptr_t) dst;
+			if (cnt == 16 && (al & 15) == 0) {
+				uint4 y = make_uint4(x[0], x[1], x[2], x[3]);
 				if (merge) {
 					const uint4 old = __ldcg((const uint4 *) dst);
-					x.x = __vminu4(x.x, old.x);
-					x.y = __vminu4(x.y, old.y);
-					x.z = __vminu4(x.z, old.z);
-					x.w = __vminu4(x.w, old.w);
+					y.x = __vminu4(y.x, old.x);
+					y.y = __vminu4(y.y, old.y);
+					y.z = __vminu4(y.z, old.z);
+					y.w = __vminu4(y.w, old.w);
 				}
-				*(uint4 *) dst = x;
+				*(uint4 *) dst = y;
+			} else if (cnt == 16 && (al & 3) == 0) {
+#pragma unroll
+				for (int q = 0; q < 4; ++q) {
+					uint32_t y = x[q];
+					if (merge) y = __vminu4(y, __ldcg((const unsigned int *) dst + q));
+					((uint32_t *) dst)[q] = y;
+				}
+			} else if (cnt == 16 && (al & 1) == 0) {
+#pragma unroll
+				for (int q = 0; q < 8; ++q) {
+					uint32_t y = (x[q / 2] >> (16 * (q & 1))) & 0xFFFFu;
+					if (merge) {
+						const uint32_t old = __ldcg((const unsigned short *) dst + q);
+						y = __vminu4(y | 0xFFFF0000u, old | 0xFFFF0000u) & 0xFFFFu;
+					}
+					((uint16_t *) dst)[q] = (uint16_t) y;
+				}
 			} else {
+#pragma unroll
 				for (uint32_t b = 0; b < 16; ++b) {
-					if (c + b >= nv) break;
-					const uint8_t x = sp[b];
-					dst[b] = merge ? min(x, ld_cg_u8(dst + b)) : x;
+					if (b >= cnt) break;
+					const uint8_t y = (uint8_t) (x[b / 4] >> (8 * (b & 3)));
+					dst[b] = merge ? min(y, ld_cg_u8(dst + b)) : y;
 				}
 			}
 		}

@@ -52,7 +52,6 @@ struct MsArgs {
 	uint32_t last_bits;   // sources in the last word (1..64)
 	uint32_t planes;      // level planes allocated (>= 2)
 	uint32_t push_div;    // a level pushes while its frontier's edges < m / push_div
-	uint32_t vec_out;     // levels rows start 16-byte aligned (16-byte stores)
 	uint32_t nbig_in;     // destinations with more than kMsPullBig in-edges
 	uint32_t nchunks;     // their in-edge chunks
 	const uint32_t *row_off, *col, *in_off, *in_src;

@@ -188,3 +188,24 @@ def test_many_in_edge_destinations(native, oracle):
     with B.Graph.from_edges(n, src, dst, 512, 8) as g:
         _, st = _check(oracle, arr, g, srcs)
         assert 0 in st["level_push"], "expected pull levels"
+
+
+@pytest.mark.parametrize("planes", [2, 0])
+@pytest.mark.parametrize("n", [2050, 1028, 1001])
+def test_row_alignments_and_merges(native, oracle, n, planes):
+    """Rows of N bytes start at every alignment (N = 2 mod 4: 2-byte stores,
+    N = 4 mod 16: 4-byte stores, odd N: bytes); with 2 planes the output is
+    written in several segments merged by a byte-wise minimum."""
+    import bfs_simd_benchmarks_gb300 as B
+    rng = np.random.default_rng(n)
+    chain = np.arange(40, dtype=np.uint32)
+    s1, d1 = B.gen_rmat(n, 6 * n, seed=n + 1)
+    src = np.concatenate([chain, s1, rng.integers(0, 40, 200).astype(np.uint32)])
+    dst = np.concatenate([chain + 1, d1, rng.integers(41, n, 200).astype(np.uint32)])
+    arr = oracle.arrays_from_edges(n, src, dst, 64, 4)
+    srcs = [0, 3, 17] + B.pick_sources(arr["degrees"], 67, seed=n).tolist()
+    with B.Graph.from_edges(n, src, dst, 64, 4) as g:
+        g.set_options(batch_planes=planes)
+        _, st = _check(oracle, arr, g, srcs)
+        if planes:
+            assert st["spills"] > 0
