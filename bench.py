@@ -261,6 +261,25 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
     ms = [r[0] for r in runs]
     edges = runs[0][1]["edges_traversed"]
     gteps = edges * len(ms) / (sum(ms) / 1e3) / 1e9
+    # the same batch as one CUDA-graph launch (sources resident on the device)
+    d_src = torch.tensor(np.asarray(sources, dtype=np.int64), dtype=torch.int32, device=dev)
+    gms = []
+    with g.batch_graph(d_src.data_ptr(), len(sources), out.data_ptr()) as bgr:
+        for i in range(max(3, args.warmup) + args.batch_steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xFF)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                bgr.launch(stream.cuda_stream)
+                e1.record(stream)
+            gst = g.last_batch_stats()
+            if gst["status"] != 0 or gst["edges_traversed"] != edges:
+                raise RuntimeError("CUDA-graph batch differs from the direct launch")
+            if i >= max(3, args.warmup):
+                gms.append(e0.elapsed_time(e1))
+    cuda_graph = {"ms_per_batch_mean": statistics.mean(gms), "gteps": edges * len(gms) / (sum(gms) / 1e3) / 1e9,
+                  "launch": "bfs_batch_graph_launch: memset + cooperative traversal + output pass as one graph"}
     # the single-source kernel on the same graph, a sample of the same sources
     lev = torch.empty(wl.n, dtype=torch.int32, device=dev)
     single_ms, single_edges, rows_ok = [], 0, 0
@@ -305,6 +324,7 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
         "plain_gpu_bfs": {"gteps": single_gteps, "ms_per_traversal_mean": statistics.mean(single_ms),
                           "sources": len(single_ms), "kernel": "k_bfs_persistent (single source)"},
         "speedup_vs_plain_gpu_bfs": gteps / single_gteps,
+        "cuda_graph": cuda_graph,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "kernels": "k_ms_bfs + k_ms_emit", "peak_kind": peak_kind, "algorithmic_bytes_per_batch": alg},
         "parity": f"batched rows equal single-source levels on {rows_ok}/{len(check)} sources checked",

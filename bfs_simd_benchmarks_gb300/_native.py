@@ -228,6 +228,10 @@ _SIGNATURES = [
     ("bfs_last_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     ("bfs_run_batch", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(BatchStats)]),
     ("bfs_last_batch_stats", C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
+    ("bfs_run_batch_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("bfs_batch_graph_create", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("bfs_batch_graph_launch", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("bfs_batch_graph_destroy", C.c_int, [C.c_void_p]),
     ("bfs_server_options_default", C.c_int, [C.POINTER(ServerOptions)]),
     ("bfs_server_create", C.c_int, [C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
     ("bfs_server_add_graph", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32)]),

@@ -77,6 +77,7 @@ struct bfs_graph {
 		int grid = 0;
 		bool have_run = false, fresh = false;
 		bool singles = false;        // the last batch ran as single-source traversals
+		bool em_valid = false;       // em marks the last batch's traversal end
 		size_t bytes = 0;
 		std::vector<DevBuf> bufs;
 	} mb;
@@ -539,12 +540,19 @@ __global__ void __launch_bounds__(512) k_levels_u8(const int32_t *lev, uint8_t *
 	}
 }
 
+bool stream_capturing(cudaStream_t st) {
+	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+	return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
+// `dev_sources`: `sources` is device memory (validated by the kernel).
 int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *levels, cudaStream_t st,
-		cudaEvent_t wait_before = nullptr, cudaEvent_t between = nullptr) {
+		cudaEvent_t wait_before = nullptr, cudaEvent_t between = nullptr, bool dev_sources = false) {
 	if (g->host_only) return BFS_EUNSUPPORTED;
 	if (!sources || !levels || ns == 0 || ns > BFS_BATCH_MAX_SOURCES) return BFS_EARG;
-	for (uint32_t i = 0; i < ns; ++i)
-		if (sources[i] >= g->n) return BFS_EARG;
+	if (!dev_sources)
+		for (uint32_t i = 0; i < ns; ++i)
+			if (sources[i] >= g->n) return BFS_EARG;
 	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
 	const uint32_t K = (ns + 63) / 64;
 	uint32_t planes = 0;
@@ -567,8 +575,9 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 	a.chunk_beg = g->ms_chunk_beg;
 	a.nbig_in = g->ms_nbig_in;
 	a.nchunks = g->ms_nchunks;
-	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
-	const bool singles = ns <= g->opt.batch_single_max && g->opt.mode == BFS_MODE_PERSISTENT;
+	const bool capturing = dev_sources && stream_capturing(st);
+	if (!capturing && cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
+	const bool singles = !dev_sources && ns <= g->opt.batch_single_max && g->opt.mode == BFS_MODE_PERSISTENT;
 	if (singles) {
 		// a few sources: one single-source traversal each (queue-driven, no
 		// sweeps over all vertices), rows converted to uint8 on the device
@@ -595,6 +604,12 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 		b.grid = g->grid;
 		// the single-source statistics now describe the last of these runs
 		g->have_run = false;
+	} else if (dev_sources) {
+		// sources already on the device (checked there); device work only, so
+		// the call can be captured into a CUDA graph
+		if (wait_before && cudaStreamWaitEvent(st, wait_before, 0) != cudaSuccess) return BFS_ECUDA;
+		if ((rc = ms_launch(a, sources, ns, levels, g->num_sms, st, &b.grid, capturing ? nullptr : b.em, between)))
+			return rc;
 	} else {
 		// pageable source: the copy has left `sources` when the call returns
 		if (cudaMemcpyAsync(b.d_sources, sources, sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, st) != cudaSuccess)
@@ -602,10 +617,12 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 		if (wait_before && cudaStreamWaitEvent(st, wait_before, 0) != cudaSuccess) return BFS_ECUDA;
 		if ((rc = ms_launch(a, b.d_sources, ns, levels, g->num_sms, st, &b.grid, b.em, between))) return rc;
 	}
-	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
+	b.em_valid = !capturing;
 	b.singles = singles;
 	b.args.planes = planes;
 	b.args.K = K;
+	if (capturing) return BFS_OK;  // timing events belong to the launch of the graph
+	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
 	b.num_sources = ns;
 	b.stream = st;
 	b.have_run = true;
@@ -636,7 +653,7 @@ int collect_batch_stats(bfs_graph *g, bfs_batch_stats *out) {
 	s.grid_ctas = (uint32_t) b.grid;
 	float ms = 0, ems = 0;
 	cudaEventElapsedTime(&ms, b.e0, b.e1);
-	cudaEventElapsedTime(&ems, b.em, b.e1);
+	if (b.em_valid) cudaEventElapsedTime(&ems, b.em, b.e1);
 	s.device_ms = ms;
 	s.output_ms = ems;
 	s.setup_ms = c.stats.t_levels0 > c.stats.t_start ? (c.stats.t_levels0 - c.stats.t_start) * 1e-6 : 0.0;
@@ -663,6 +680,13 @@ int collect_batch_stats(bfs_graph *g, bfs_batch_stats *out) {
 }
 
 } // namespace
+
+struct bfs_batch_graph {
+	bfs_graph *g = nullptr;
+	uint32_t num_sources = 0;
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+};
 
 // ---- hooks of the serving loop (server.cpp) ---------------------------------
 namespace bfsg {
@@ -875,6 +899,82 @@ int bfs_run_batch(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, u
 	int st = run_batch_impl(g, sources, num_sources, levels, (cudaStream_t) stream);
 	if (st || !stats) return st;
 	return collect_batch_stats(g, stats);
+}
+
+int bfs_run_batch_device(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, uint8_t *levels, void *stream) {
+	if (!g) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	return run_batch_impl(g, sources, num_sources, levels, (cudaStream_t) stream, nullptr, nullptr, true);
+}
+
+int bfs_batch_graph_create(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, uint8_t *levels,
+		bfs_batch_graph **out) {
+	if (!g || !out) return BFS_EARG;
+	*out = nullptr;
+	std::lock_guard<std::mutex> lk(g->mu);
+	if (g->host_only) return BFS_EUNSUPPORTED;
+	if (!sources || !levels || num_sources == 0 || num_sources > BFS_BATCH_MAX_SOURCES) return BFS_EARG;
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	// allocate the batch state before capturing (no allocation inside a capture)
+	uint32_t planes = 0;
+	int rc = batch_prepare(g, (num_sources + 63) / 64, &planes);
+	if (rc) return rc;
+	cudaStream_t cs = nullptr;
+	if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return BFS_ECUDA;
+	bfs_batch_graph *bg = new bfs_batch_graph();
+	bg->g = g;
+	bg->num_sources = num_sources;
+	rc = BFS_ECUDA;
+	if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+		rc = run_batch_impl(g, sources, num_sources, levels, cs, nullptr, nullptr, true);
+		cudaGraph_t graph = nullptr;
+		const cudaError_t e = cudaStreamEndCapture(cs, &graph);
+		if (rc == BFS_OK && e == cudaSuccess && graph) {
+			bg->graph = graph;
+			rc = cudaGraphInstantiate(&bg->exec, graph, 0) == cudaSuccess ? BFS_OK : BFS_ECUDA;
+		} else {
+			if (graph) cudaGraphDestroy(graph);
+			if (rc == BFS_OK) rc = BFS_ECUDA;
+		}
+	}
+	cudaGetLastError();
+	cudaStreamDestroy(cs);
+	g->mb.have_run = false;
+	if (rc) {
+		if (bg->exec) cudaGraphExecDestroy(bg->exec);
+		if (bg->graph) cudaGraphDestroy(bg->graph);
+		delete bg;
+		return rc;
+	}
+	*out = bg;
+	return BFS_OK;
+}
+
+int bfs_batch_graph_launch(bfs_batch_graph *bg, void *stream) {
+	if (!bg || !bg->exec) return BFS_EARG;
+	bfs_graph *g = bg->g;
+	std::lock_guard<std::mutex> lk(g->mu);
+	auto &b = g->mb;
+	cudaStream_t st = (cudaStream_t) stream;
+	if (cudaEventRecord(b.e0, st) != cudaSuccess || cudaGraphLaunch(bg->exec, st) != cudaSuccess ||
+			cudaEventRecord(b.e1, st) != cudaSuccess)
+		return BFS_ECUDA;
+	b.num_sources = bg->num_sources;
+	b.args.K = (bg->num_sources + 63) / 64;
+	b.stream = st;
+	b.have_run = true;
+	b.fresh = false;
+	b.singles = false;
+	b.em_valid = false;
+	return BFS_OK;
+}
+
+int bfs_batch_graph_destroy(bfs_batch_graph *bg) {
+	if (!bg) return BFS_EARG;
+	if (bg->exec) cudaGraphExecDestroy(bg->exec);
+	if (bg->graph) cudaGraphDestroy(bg->graph);
+	delete bg;
+	return BFS_OK;
 }
 
 int bfs_last_batch_stats(bfs_graph *g, bfs_batch_stats *stats) {

@@ -557,6 +557,10 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 	if (ok) {
 		for (uint32_t i = t0; i < ns; i += stride) {
 			const uint32_t v = sources[i];
+			if (v >= a.n) {  // device-resident sources are checked here
+				atomicExch(&ctl->err, BFS_EARG);
+				continue;
+			}
 			const size_t x = (size_t) v * a.K + i / 64;
 			const unsigned long long bit = 1ull << (i % 64);
 			atomicOr((unsigned long long *) (a.hist + x), bit);

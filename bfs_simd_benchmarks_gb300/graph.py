@@ -168,10 +168,51 @@ class Graph:
         stats = self.run_batch_device(src, out.data_ptr(), torch.cuda.current_stream().cuda_stream, stats=True)
         return out, stats
 
+    def run_batch_sources_device(self, sources_ptr: int, num_sources: int, levels_ptr: int, stream: int = 0) -> None:
+        """bfs_run_batch_device: sources already in device memory (uint32)."""
+        N.check(N.load().bfs_run_batch_device(self._h, C.c_void_p(sources_ptr), num_sources, C.c_void_p(levels_ptr),
+                                              C.c_void_p(stream) if stream else None), "bfs_run_batch_device")
+
+    def batch_graph(self, sources_ptr: int, num_sources: int, levels_ptr: int) -> "BatchGraph":
+        """A CUDA graph of one batched traversal over fixed device buffers."""
+        h = C.c_void_p()
+        N.check(N.load().bfs_batch_graph_create(self._h, C.c_void_p(sources_ptr), num_sources, C.c_void_p(levels_ptr),
+                                                C.byref(h)), "bfs_batch_graph_create")
+        return BatchGraph(h, self)
+
     def last_batch_stats(self) -> dict:
         st = N.BatchStats()
         N.check(N.load().bfs_last_batch_stats(self._h, C.byref(st)), "bfs_last_batch_stats")
         return st.as_dict()
+
+
+class BatchGraph:
+    """An instantiated CUDA graph of one batched traversal (bfs_batch_graph_*)."""
+
+    def __init__(self, handle: C.c_void_p, graph: Graph):
+        self._h = handle
+        self._graph = graph
+
+    def launch(self, stream: int = 0) -> None:
+        N.check(N.load().bfs_batch_graph_launch(self._h, C.c_void_p(stream) if stream else None),
+                "bfs_batch_graph_launch")
+
+    def close(self) -> None:
+        if self._h:
+            N.load().bfs_batch_graph_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Server:

@@ -238,6 +238,23 @@ int bfs_run_batch(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, u
 		bfs_batch_stats *stats);
 int bfs_last_batch_stats(bfs_graph *g, bfs_batch_stats *stats);
 
+/* bfs_run_batch with `sources` in device memory: it enqueues device work only
+ * (always the bit-sliced kernel; sources are checked on the device, an
+ * out-of-range one makes the batch report BFS_EARG), so once the graph's batch
+ * state exists it allocates nothing and can be captured into a CUDA graph. */
+int bfs_run_batch_device(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, uint8_t *levels, void *stream);
+
+/* One batched traversal captured into an instantiated CUDA graph: the sources
+ * at a fixed device address (their values are read at each launch) and the
+ * levels at a fixed device address.  Launching it replaces the launch
+ * sequence (control-block clear, the cooperative traversal, the output pass)
+ * by one graph launch; bfs_last_batch_stats then reports it (output_ms 0). */
+typedef struct bfs_batch_graph bfs_batch_graph;
+int bfs_batch_graph_create(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, uint8_t *levels,
+		bfs_batch_graph **out);
+int bfs_batch_graph_launch(bfs_batch_graph *bg, void *stream);
+int bfs_batch_graph_destroy(bfs_batch_graph *bg);
+
 /* ---- serving loop (no counterpart in the reference) ---------------------
  * A server keeps several graphs resident in HBM and answers single-source
  * queries (graph, source) by coalescing the queries waiting on one graph into

@@ -209,3 +209,37 @@ def test_row_alignments_and_merges(native, oracle, n, planes):
         _, st = _check(oracle, arr, g, srcs)
         if planes:
             assert st["spills"] > 0
+
+
+def test_device_sources_and_cuda_graph(native, oracle):
+    """bfs_run_batch_device and a captured CUDA graph launched twice with new
+    source values in the same device buffer: the rows equal bfs_run_batch's."""
+    torch = pytest.importorskip("torch")
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 13
+    src, dst = B.gen_rmat(n, 16 * n, seed=913, permute=True)
+    arr = oracle.arrays_from_edges(n, src, dst, 256, 8)
+    s1 = B.pick_sources(arr["degrees"], 150, seed=1)
+    s2 = B.pick_sources(arr["degrees"], 150, seed=2)
+    with B.Graph.from_edges(n, src, dst, 256, 8) as g:
+        d_src = torch.tensor(s1.astype(np.int64), dtype=torch.int32, device="cuda")
+        out = torch.empty((150, n), dtype=torch.uint8, device="cuda")
+        g.run_batch_sources_device(d_src.data_ptr(), 150, out.data_ptr())
+        st = g.last_batch_stats()
+        assert st["status"] == 0
+        np.testing.assert_array_equal(out.cpu().numpy(), _expect(oracle, arr, s1))
+        with g.batch_graph(d_src.data_ptr(), 150, out.data_ptr()) as bg:
+            for srcs in (s2, s1):
+                d_src.copy_(torch.tensor(srcs.astype(np.int64), dtype=torch.int32))
+                out.fill_(7)
+                torch.cuda.synchronize()
+                bg.launch()
+                st = g.last_batch_stats()
+                assert st["status"] == 0 and st["num_sources"] == 150
+                np.testing.assert_array_equal(out.cpu().numpy(), _expect(oracle, arr, srcs))
+        # a source out of range is reported by the device
+        d_src[3] = n
+        with pytest.raises(B.BfsError) as ei:
+            g.run_batch_sources_device(d_src.data_ptr(), 150, out.data_ptr())
+            g.last_batch_stats()
+        assert ei.value.status == 4
