@@ -173,6 +173,17 @@ def cpu_baseline(wl, src, dst, sources, seconds: float, per_call=None):
                       f"(traversal only), oracle/bfs_oracle.c OpenMP build"}, levels, arr
 
 
+def aggregate_replicas(torch, total_ms: float, edges: int, dev, world: int):
+    """Replicas: the job's time is the slowest rank's, its work every rank's."""
+    if world <= 1:
+        return total_ms, float(edges)
+    t = torch.tensor([total_ms, float(edges)], dtype=torch.float64, device=dev)
+    tmax = t.clone()
+    torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+    return float(tmax[0]), float(t[1])
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -462,14 +473,7 @@ def main():
         if st["status"] != 0:
             raise RuntimeError(f"device status {st['status']}")
     total_ms = sum(trav_ms)
-    if world > 1:
-        t = torch.tensor([total_ms, float(edges)], dtype=torch.float64, device=dev)
-        tmax = t.clone()
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-        total_ms_max, edges_all = float(tmax[0]), float(t[1])
-    else:
-        total_ms_max, edges_all = total_ms, float(edges)
+    total_ms_max, edges_all = aggregate_replicas(torch, total_ms, edges, dev, world)
     value = edges_all / (total_ms_max / 1e3) / 1e9
 
     # roofline of the traversal kernel (k_bfs_persistent), per launch
