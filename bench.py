@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--batch-sources", type=int, default=4096)
     ap.add_argument("--batch-steps", type=int, default=5)
     ap.add_argument("--batch-budget-mb", type=int, default=40960, help="HBM budget of the batched level planes")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (measure with the default options)")
     ap.add_argument("--serve", default="c4", help="serving measurement: 'c4' (8 graphs, Poisson load) or 'none'")
     ap.add_argument("--serve-rates", default="2000,10000,50000", help="query arrival rates (queries/s)")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="arrival window per rate")
@@ -255,6 +256,15 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
     out = torch.empty((len(sources), wl.n), dtype=torch.uint8, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     stream = torch.cuda.Stream(device=dev)
+    tuned = None
+    if not args.no_tune:
+        t_t = time.perf_counter()
+        r = g.tune(sources, single=False, batch=True)
+        tuned = {"batch_push_div": r["options"]["batch_push_div"], "tuned_gteps": r["batch_gteps"],
+                 "default_gteps": r["default_batch_gteps"], "trials": r["num_trials"],
+                 "seconds": round(time.perf_counter() - t_t, 2),
+                 "note": "the bit-sliced kernel reads CSR + in-edge lists only: tile width and stripe length "
+                         "do not enter it, so only its push/pull threshold is tuned"}
     runs = []
     for i in range(max(3, args.warmup) + args.batch_steps):
         with torch.cuda.stream(stream):
@@ -336,6 +346,7 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
                           "sources": len(single_ms), "kernel": "k_bfs_persistent (single source)"},
         "speedup_vs_plain_gpu_bfs": gteps / single_gteps,
         "cuda_graph": cuda_graph,
+        "autotune": tuned,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "kernels": "k_ms_bfs + k_ms_emit", "peak_kind": peak_kind, "algorithmic_bytes_per_batch": alg},
         "parity": f"batched rows equal single-source levels on {rows_ok}/{len(check)} sources checked",
@@ -432,6 +443,14 @@ def main():
         sources = sources[: args.sources]
     n = wl.n
     sw = wl.s * wl.w
+    tuned = None
+    if not args.no_tune and args.mode == "persistent":
+        t_t = time.perf_counter()
+        r = g.tune(sources, single=True)
+        tuned = {"options": {k: r["options"][k] for k in ("bottom_up", "to_dense_ratio", "to_sparse_ratio",
+                                                           "warp_max_degree", "cta_max_degree")},
+                 "tuned_gteps_kernel": r["single_gteps"], "default_gteps_kernel": r["default_single_gteps"],
+                 "trials": r["num_trials"], "seconds": round(time.perf_counter() - t_t, 2)}
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     lev = torch.empty(n, dtype=torch.int32, device=dev)
@@ -527,6 +546,7 @@ def main():
                            bottom_up=args.bottom_up,
                            l2=f"flushed (256 MiB write) before every traversal; graph {info['device_bytes'] / 1e6:.0f} MB > L2",
                            grid_ctas=timed[0][2]["grid_ctas"], column_groups=info["num_groups"],
+                           autotune=tuned,
                            graph_build_s=round(t_gen, 2)),
             "single_source": {"gteps": value, "ms_per_traversal_mean": statistics.mean(trav_ms),
                               "ms_per_traversal_p50": statistics.median(trav_ms),

@@ -7,6 +7,7 @@ from ._native import BfsError, load as load_library  # noqa: F401
 from .graph import (  # noqa: F401
     Graph,
     Server,
+    autotune,
     gen_rmat,
     pick_sources,
     tool_column_major,
@@ -18,6 +19,6 @@ from .graph import (  # noqa: F401
 )
 
 __all__ = [
-    "BfsError", "Graph", "Server", "gen_rmat", "load_library", "pick_sources", "tool_column_major",
+    "BfsError", "Graph", "Server", "autotune", "gen_rmat", "load_library", "pick_sources", "tool_column_major",
     "tool_coo_tiling", "tool_csr_tiling", "tool_vertex_remap", "write_edge_list", "write_level_dump",
 ]

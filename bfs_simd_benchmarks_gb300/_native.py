@@ -72,7 +72,7 @@ class Options(C.Structure):
         ("batch_planes", C.c_uint32),
         ("batch_budget_mb", C.c_uint32),
         ("batch_single_max", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("batch_push_div", C.c_uint32),
     ]
 
 
@@ -143,6 +143,43 @@ class Stats(C.Structure):
         k = min(self.num_steps, BFS_TRACE_MAX)
         d["trace"] = list(self.trace[:k])
         d["step_ms"] = [round(x, 5) for x in self.step_ms[:k]]
+        return d
+
+
+BFS_TUNE_SINGLE, BFS_TUNE_BATCH, BFS_TUNE_MAX_TRIALS = 1, 2, 256
+
+
+class TuneTrial(C.Structure):
+    _fields_ = [
+        ("tile_width", C.c_uint32),
+        ("stripe_length", C.c_uint32),
+        ("options", Options),
+        ("gteps", C.c_double),
+        ("kind", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [
+        ("tile_width", C.c_uint32),
+        ("stripe_length", C.c_uint32),
+        ("options", Options),
+        ("single_gteps", C.c_double),
+        ("batch_gteps", C.c_double),
+        ("default_single_gteps", C.c_double),
+        ("default_batch_gteps", C.c_double),
+        ("num_trials", C.c_uint32),
+        ("from_cache", C.c_uint32),
+        ("trials", TuneTrial * BFS_TUNE_MAX_TRIALS),
+    ]
+
+    def as_dict(self) -> dict:
+        opt = lambda o: {k: getattr(o, k) for k, _ in Options._fields_}  # noqa: E731
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("options", "trials")}
+        d["options"] = opt(self.options)
+        d["trials"] = [{"tile_width": t.tile_width, "stripe_length": t.stripe_length, "gteps": t.gteps,
+                        "kind": t.kind, "options": opt(t.options)} for t in self.trials[:self.num_trials]]
         return d
 
 
@@ -232,6 +269,9 @@ _SIGNATURES = [
     ("bfs_batch_graph_create", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_void_p)]),
     ("bfs_batch_graph_launch", C.c_int, [C.c_void_p, C.c_void_p]),
     ("bfs_batch_graph_destroy", C.c_int, [C.c_void_p]),
+    ("bfs_tune_options", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_uint32, C.POINTER(TuneResult)]),
+    ("bfs_autotune", C.c_int, [C.c_uint32, C.c_uint64, _u32p, _u32p, _u32p, C.c_uint32, _u32p, C.c_uint32, _u32p,
+                               C.c_uint32, C.c_uint32, C.c_char_p, C.POINTER(TuneResult)]),
     ("bfs_server_options_default", C.c_int, [C.POINTER(ServerOptions)]),
     ("bfs_server_create", C.c_int, [C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
     ("bfs_server_add_graph", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32)]),

@@ -18,7 +18,6 @@ namespace {
 
 constexpr uint32_t kMaxGroupVertices = 32768;  // shared-memory bitmaps of one column group
 constexpr uint32_t kGroupsPerCta = 1;
-constexpr uint32_t kBatchPushDiv = 16;       // batched levels push while frontier edges < E / 16
 constexpr uint32_t kBatchDefaultPlanes = 32; // level planes when sized from the budget
 
 struct DevBuf {
@@ -150,6 +149,7 @@ void default_options(bfs_options *o) {
 	o->batch_planes = 0;
 	o->batch_budget_mb = 40960;
 	o->batch_single_max = 4;
+	o->batch_push_div = 16;
 }
 
 // Builds the device copy of a validated host graph.
@@ -565,7 +565,7 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 	a.K = K;
 	a.last_bits = ns - 64 * (K - 1);
 	a.planes = planes;
-	a.push_div = kBatchPushDiv;
+	a.push_div = std::max<uint32_t>(1, g->opt.batch_push_div);
 	a.row_off = g->dg.row_off;
 	a.col = g->dg.col;
 	a.in_off = g->dg.in_off;
@@ -853,7 +853,8 @@ int bfs_set_options(bfs_graph *g, const bfs_options *opt) {
 	if (!g || !opt) return BFS_EARG;
 	if (opt->mode > BFS_MODE_STEPWISE || opt->bottom_up > BFS_BU_STREAM || opt->to_dense_ratio == 0 || opt->to_sparse_ratio == 0 ||
 			opt->warp_max_degree == 0 || opt->cta_max_degree < opt->warp_max_degree || opt->batch_planes == 1 ||
-			opt->batch_planes > kMsMaxLevel + 1 || (opt->batch_planes == 0 && opt->batch_budget_mb == 0))
+			opt->batch_planes > kMsMaxLevel + 1 || (opt->batch_planes == 0 && opt->batch_budget_mb == 0) ||
+			opt->batch_push_div == 0)
 		return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);
 	g->opt = *opt;

@@ -113,7 +113,7 @@ class Graph:
     def options(self) -> dict:
         o = N.Options()
         N.check(N.load().bfs_get_options(self._h, C.byref(o)), "bfs_get_options")
-        return {k: getattr(o, k) for k, _ in N.Options._fields_ if k != "reserved"}
+        return {k: getattr(o, k) for k, _ in N.Options._fields_}
 
     def set_options(self, **kw) -> None:
         o = N.Options()
@@ -179,6 +179,15 @@ class Graph:
         N.check(N.load().bfs_batch_graph_create(self._h, C.c_void_p(sources_ptr), num_sources, C.c_void_p(levels_ptr),
                                                 C.byref(h)), "bfs_batch_graph_create")
         return BatchGraph(h, self)
+
+    def tune(self, sources, single: bool = True, batch: bool = False) -> dict:
+        """bfs_tune_options: times candidate options on these sources, keeps the best."""
+        src = _u32(sources)
+        r = N.TuneResult()
+        flags = (N.BFS_TUNE_SINGLE if single else 0) | (N.BFS_TUNE_BATCH if batch else 0)
+        N.check(N.load().bfs_tune_options(self._h, _ptr(src, C.c_uint32), src.size, flags, C.byref(r)),
+                "bfs_tune_options")
+        return r.as_dict()
 
     def last_batch_stats(self) -> dict:
         st = N.BatchStats()
@@ -291,6 +300,20 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def autotune(num_vertices: int, src, dst, sources, tile_widths=(512, 1024, 2048, 4096), stripe_lengths=(8, 16, 32),
+             single: bool = True, batch: bool = False, cache_path: str | None = None) -> dict:
+    """bfs_autotune: the best tile shape and options of an edge list, by measurement."""
+    s, d, so = _u32(src), _u32(dst), _u32(sources)
+    w, sl = _u32(tile_widths), _u32(stripe_lengths)
+    r = N.TuneResult()
+    flags = (N.BFS_TUNE_SINGLE if single else 0) | (N.BFS_TUNE_BATCH if batch else 0)
+    N.check(N.load().bfs_autotune(num_vertices, s.size, _ptr(s, C.c_uint32), _ptr(d, C.c_uint32),
+                                  _ptr(so, C.c_uint32), so.size, _ptr(w, C.c_uint32), w.size, _ptr(sl, C.c_uint32),
+                                  sl.size, flags, cache_path.encode() if cache_path else None, C.byref(r)),
+            "bfs_autotune")
+    return r.as_dict()
 
 
 # ---- tools (the reference's tools/ CLIs) ------------------------------

@@ -128,7 +128,8 @@ typedef struct bfs_options {
 	uint32_t batch_budget_mb;  /* bfs_run_batch: HBM budget of the level planes in MiB (default 40960) */
 	uint32_t batch_single_max; /* bfs_run_batch: batches of at most this many sources run as back-to-back
 	                              single-source traversals (default 4; 0 = always bit-sliced) */
-	uint32_t reserved;
+	uint32_t batch_push_div;   /* bfs_run_batch: a level is pushed top-down while its frontier's out-edges
+	                              < E / batch_push_div, pulled bottom-up after (default 16) */
 } bfs_options;
 
 /* Bottom-up step variants.  PULL: every unvisited destination of a column
@@ -254,6 +255,45 @@ int bfs_batch_graph_create(bfs_graph *g, const uint32_t *sources, uint32_t num_s
 		bfs_batch_graph **out);
 int bfs_batch_graph_launch(bfs_batch_graph *bg, void *stream);
 int bfs_batch_graph_destroy(bfs_batch_graph *bg);
+
+/* ---- autotuner (no counterpart in the reference; it replaces choosing W, S
+ * by hand with tools/tile-size-computer and the T_RATIO constant) -------- */
+#define BFS_TUNE_SINGLE 1u  /* tune the single-source options (variant, switch ratios, bucket bounds) */
+#define BFS_TUNE_BATCH 2u   /* tune batch_push_div on one batch of all the sources */
+#define BFS_TUNE_MAX_TRIALS 256
+
+typedef struct bfs_tune_trial {
+	uint32_t tile_width, stripe_length;
+	bfs_options options;
+	double gteps;              /* single-source trials: sum m(s) / sum kernel time; batch trials: the batch's */
+	uint32_t kind;             /* BFS_TUNE_SINGLE or BFS_TUNE_BATCH */
+	uint32_t reserved;
+} bfs_tune_trial;
+
+typedef struct bfs_tune_result {
+	uint32_t tile_width, stripe_length;   /* the best shape (bfs_autotune) */
+	bfs_options options;                  /* the best options for it */
+	double single_gteps;                  /* measured with them (0 if not tuned) */
+	double batch_gteps;
+	double default_single_gteps;          /* the defaults at the first shape tried, for comparison */
+	double default_batch_gteps;
+	uint32_t num_trials;
+	uint32_t from_cache;                  /* 1: read from the cache file, nothing measured */
+	bfs_tune_trial trials[BFS_TUNE_MAX_TRIALS];
+} bfs_tune_result;
+
+/* Tunes the options of one resident graph on the given sources (coordinate
+ * descent, every candidate timed on the device) and leaves the best set. */
+int bfs_tune_options(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, uint32_t flags,
+		bfs_tune_result *result);
+/* Builds the graph of an edge list (bfs_graph_from_edges) at every tile width
+ * x stripe length given, tunes each (bfs_tune_options) and reports the best.
+ * With a cache file, a graph already tuned (same N, E and out-degree
+ * signature, same flags) is answered from it, and a new result is appended. */
+int bfs_autotune(uint32_t num_vertices, uint64_t num_edges, const uint32_t *src, const uint32_t *dst,
+		const uint32_t *sources, uint32_t num_sources, const uint32_t *tile_widths, uint32_t num_widths,
+		const uint32_t *stripe_lengths, uint32_t num_stripes, uint32_t flags, const char *cache_path,
+		bfs_tune_result *result);
 
 /* ---- serving loop (no counterpart in the reference) ---------------------
  * A server keeps several graphs resident in HBM and answers single-source

@@ -1,0 +1,57 @@
+"""The autotuner: options and tile shapes chosen by measurement leave the
+levels unchanged, the tuned options are applied to the graph, and a second
+bfs_autotune on the same graph is answered from the cache file."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_tune_options_keeps_levels(native, oracle):
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 14
+    src, dst = B.gen_rmat(n, 16 * n, seed=55, permute=True)
+    arr = oracle.arrays_from_edges(n, src, dst, 1024, 16)
+    srcs = B.pick_sources(arr["degrees"], 40, seed=5)
+    with B.Graph.from_edges(n, src, dst, 1024, 16) as g:
+        r = g.tune(srcs, single=True, batch=True)
+        assert r["single_gteps"] > 0 and r["batch_gteps"] > 0
+        assert r["single_gteps"] >= r["default_single_gteps"] * 0.99 or r["num_trials"] > 1
+        assert r["num_trials"] >= 10 and {t["kind"] for t in r["trials"]} == {1, 2}
+        opts = g.options()
+        for k in ("to_dense_ratio", "to_sparse_ratio", "bottom_up", "batch_push_div"):
+            assert opts[k] == r["options"][k]
+        for s in srcs[:6]:
+            lev, par, _ = g.run(int(s))
+            np.testing.assert_array_equal(lev, oracle.bfs_levels(arr, int(s)))
+            assert oracle.check_parents(arr, int(s), lev, par) == 0
+        lev, st = g.run_batch(srcs)
+        got = lev.cpu().numpy()
+        for i, s in enumerate(srcs[:6]):
+            ref = oracle.bfs_levels(arr, int(s))
+            np.testing.assert_array_equal(got[i], np.where(ref < 0, 255, ref).astype(np.uint8))
+
+
+def test_autotune_shapes_and_cache(native, oracle, tmp_path):
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 13
+    src, dst = B.gen_rmat(n, 16 * n, seed=66)
+    arr = oracle.arrays_from_edges(n, src, dst, 512, 8)
+    srcs = B.pick_sources(arr["degrees"], 8, seed=1)
+    cache = str(tmp_path / "tune.txt")
+    r1 = B.autotune(n, src, dst, srcs, tile_widths=(512, 2048), stripe_lengths=(8, 32), cache_path=cache)
+    assert r1["from_cache"] == 0 and r1["tile_width"] in (512, 2048) and r1["stripe_length"] in (8, 32)
+    shapes = {(t["tile_width"], t["stripe_length"]) for t in r1["trials"]}
+    assert shapes == {(512, 8), (512, 32), (2048, 8), (2048, 32)}
+    r2 = B.autotune(n, src, dst, srcs, tile_widths=(512, 2048), stripe_lengths=(8, 32), cache_path=cache)
+    assert r2["from_cache"] == 1
+    assert (r2["tile_width"], r2["stripe_length"]) == (r1["tile_width"], r1["stripe_length"])
+    assert r2["options"] == r1["options"]
+    # the tuned shape and options give the reference's levels
+    with B.Graph.from_edges(n, src, dst, r1["tile_width"], r1["stripe_length"]) as g:
+        g.set_options(**{k: v for k, v in r1["options"].items()})
+        for s in srcs:
+            lev, _, _ = g.run(int(s))
+            np.testing.assert_array_equal(lev, oracle.bfs_levels(arr, int(s)))

@@ -290,3 +290,14 @@ def test_server_option_errors_without_device(native):
         with pytest.raises(B.BfsError) as ei:
             B.Server()
         assert ei.value.status == 9
+
+
+def test_autotune_argument_errors(native):
+    import bfs_simd_benchmarks_gb300 as B
+    src, dst = np.array([0, 1], np.uint32), np.array([1, 2], np.uint32)
+    with pytest.raises(B.BfsError) as ei:
+        B.autotune(3, src, dst, [5])                 # source out of range
+    assert ei.value.status == 4
+    with pytest.raises(B.BfsError) as ei:
+        B.autotune(3, src, dst, [0], single=False)   # nothing to tune
+    assert ei.value.status == 4
