@@ -35,6 +35,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 L2_FLUSH_BYTES = 256 << 20
+DEVICE_BUILD_EDGES = 1 << 26  # graphs this large build their layout on the GPU (BFS_LOAD_DEVICE_BUILD)
 
 
 def parse():
@@ -245,7 +246,7 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
     if graph is None:
         t0 = time.perf_counter()
         src, dst = wl.edges()
-        g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s)
+        g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s, device_build=wl.m >= DEVICE_BUILD_EDGES)
         build_s = time.perf_counter() - t0
         del src, dst
     else:
@@ -371,7 +372,7 @@ def bench_serving(args, torch, dev):
     graphs = []
     for wl in workloads.serve_graphs():
         src, dst = wl.edges()
-        graphs.append((wl, B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s)))
+        graphs.append((wl, B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s, device_build=wl.m >= DEVICE_BUILD_EDGES)))
         del src, dst
     build_s = time.perf_counter() - t0
     srv = B.Server(budget_bytes=40 * 10**9)
@@ -433,7 +434,7 @@ def main():
     wl = workloads.get(args.workload)
     t_gen = time.perf_counter()
     src, dst = wl.edges()
-    g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s)
+    g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s, device_build=wl.m >= DEVICE_BUILD_EDGES)
     g.set_options(mode=args.mode, bottom_up=args.bottom_up)
     info = g.info()
     t_gen = time.perf_counter() - t_gen

@@ -25,6 +25,7 @@ BFS_ENODEV = 9
 BFS_LOAD_WEIGHTED = 0x1
 BFS_LOAD_PREFER_REORDER = 0x2
 BFS_LOAD_HOST_ONLY = 0x4
+BFS_LOAD_DEVICE_BUILD = 0x8
 
 BFS_MODE_PERSISTENT = 0
 BFS_MODE_STEPWISE = 1

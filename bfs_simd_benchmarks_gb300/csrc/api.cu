@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "build_device.h"
 #include "internal.h"
 #include "kernels_api.h"
 #include "msbfs.h"
@@ -152,6 +153,94 @@ void default_options(bfs_options *o) {
 	o->batch_push_div = 16;
 }
 
+int device_setup(bfs_graph *g) {
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+		cudaGetLastError();
+		return BFS_ENODEV;
+	}
+	if (cudaGetDevice(&g->device) != cudaSuccess) return BFS_ECUDA;
+	if (cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->device) != cudaSuccess) return BFS_ECUDA;
+	int coop = 0;
+	cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device);
+	return coop ? BFS_OK : BFS_EUNSUPPORTED;
+}
+
+// The DevGraph fields that follow from the shape and the group plan.
+void set_shape(bfs_graph *g, const PackedTiles &pk, uint64_t packed_words) {
+	g->num_groups = pk.num_groups;
+	g->packed_words = packed_words;
+	DevGraph &d = g->dg;
+	d.n = g->n;
+	d.m = (uint32_t) g->m;
+	d.w = g->w;
+	d.s = g->s;
+	d.side = g->side;
+	d.num_stripes = g->num_stripes;
+	d.sw = g->s * g->w;
+	d.vbits = pk.vbits;
+	d.cbits = pk.cbits;
+	d.ushift = pk.vbits + pk.cbits;
+	d.vmask = (1u << pk.vbits) - 1u;
+	d.cmask = (1u << pk.cbits) - 1u;
+	d.num_groups = pk.num_groups;
+	d.max_group_words = (pk.max_group_vertices + 31) / 32;
+	d.slice_words = (d.sw + 31) / 32;
+	d.nwords = (g->n + 31) / 32;
+	d.bm_words = d.num_stripes * d.slice_words;  // bulk copies read whole slices
+	d.tma = (d.sw % 128 == 0) ? 1u : 0u;
+	d.tma_batch = std::max<uint32_t>(1, std::min<uint32_t>(kMaxSliceBatch, kTmaSliceWords / d.slice_words));
+	d.pull_long_cap = 4096;
+}
+
+// Batched pull: destinations with many in-edges and their chunks.
+int upload_big_in(bfs_graph *g, const std::vector<uint32_t> &in_off) {
+	std::vector<uint32_t> in_big, chunk_v, chunk_beg;
+	for (uint32_t v = 0; v < g->n; ++v) {
+		if (in_off[v + 1] - in_off[v] <= kMsPullBig) continue;
+		in_big.push_back(v);
+		for (uint32_t b = in_off[v]; b < in_off[v + 1]; b += kMsChunk) {
+			chunk_v.push_back(v);
+			chunk_beg.push_back(b);
+		}
+	}
+	g->ms_nbig_in = (uint32_t) in_big.size();
+	g->ms_nchunks = (uint32_t) chunk_v.size();
+	int st;
+	if ((st = dev_upload(g, &g->ms_in_big, in_big))) return st;
+	if ((st = dev_upload(g, &g->ms_chunk_v, chunk_v))) return st;
+	return dev_upload(g, &g->ms_chunk_beg, chunk_beg);
+}
+
+// Run context, events and the persistent grid.
+int alloc_run(bfs_graph *g) {
+	DevGraph &d = g->dg;
+	RunCtx &r = g->rc;
+	int st;
+	if ((st = dev_alloc(g, &r.vis, d.nwords))) return st;
+	for (int i = 0; i < 3; ++i) {
+		if ((st = dev_alloc(g, &r.bm[i], d.bm_words))) return st;
+		if ((st = dev_alloc(g, &r.sf[i], d.num_stripes))) return st;
+	}
+	for (int set = 0; set < 2; ++set)
+		for (int b = 0; b < 3; ++b)
+			if ((st = dev_alloc(g, &r.q[set][b], g->n))) return st;
+	if ((st = dev_alloc(g, &r.ctr, 3))) return st;
+	if ((st = dev_alloc(g, &r.part, 6 * (size_t) kMaxGrid))) return st;
+	if ((st = dev_alloc(g, &r.stats, 1))) return st;
+	if ((st = dev_alloc(g, &r.bar, 2))) return st;
+	if ((st = dev_alloc(g, &r.err, 1))) return st;
+	if ((st = dev_alloc(g, &g->level_buf, g->n))) return st;
+	if ((st = dev_alloc(g, &g->parent_buf, g->n))) return st;
+	if (cudaMallocHost(&g->h_stats, sizeof(DevStats)) != cudaSuccess) return BFS_ENOMEM;
+	if (cudaMallocHost(&g->h_part, sizeof(unsigned long long) * 2 * kMaxGrid) != cudaSuccess) return BFS_ENOMEM;
+	if (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess ||
+			cudaEventCreate(&g->evm) != cudaSuccess)
+		return BFS_ECUDA;
+	g->batch = std::max<uint32_t>(1, std::min<uint32_t>(kMaxSliceBatch, kSliceBudgetWords / std::max<uint32_t>(1, d.slice_words)));
+	return persistent_grid(d, g->batch, g->num_sms, &g->grid, &g->smem);
+}
+
 // Builds the device copy of a validated host graph.
 int upload(bfs_graph *g, HostGraph &h) {
 	g->n = h.n;
@@ -166,45 +255,14 @@ int upload(bfs_graph *g, HostGraph &h) {
 	g->degrees = h.degrees;
 	default_options(&g->opt);
 	if (g->host_only) return BFS_OK;
-
-	int ndev = 0;
-	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-		cudaGetLastError();
-		return BFS_ENODEV;
-	}
-	if (cudaGetDevice(&g->device) != cudaSuccess) return BFS_ECUDA;
-	if (cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->device) != cudaSuccess) return BFS_ECUDA;
-	int coop = 0;
-	cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device);
-	if (!coop) return BFS_EUNSUPPORTED;
+	int st = device_setup(g);
+	if (st) return st;
 
 	PackedTiles pk;
-	int st = pack_tiles(h, (uint32_t) g->num_sms * 2 * kGroupsPerCta, kMaxGroupVertices, pk);  // about one group per CTA
+	st = pack_tiles(h, (uint32_t) g->num_sms * 2 * kGroupsPerCta, kMaxGroupVertices, pk);  // about one group per CTA
 	if (st) return st;
-	g->num_groups = pk.num_groups;
-	g->packed_words = pk.words.size();
-
+	set_shape(g, pk, pk.words.size());
 	DevGraph &d = g->dg;
-	d.n = h.n;
-	d.m = (uint32_t) h.m;
-	d.w = h.w;
-	d.s = h.s;
-	d.side = h.side;
-	d.num_stripes = h.num_stripes;
-	d.sw = h.s * h.w;
-	d.vbits = pk.vbits;
-	d.cbits = pk.cbits;
-	d.ushift = pk.vbits + pk.cbits;
-	d.vmask = (1u << pk.vbits) - 1u;
-	d.cmask = (1u << pk.cbits) - 1u;
-	d.num_groups = pk.num_groups;
-	d.max_group_words = (pk.max_group_vertices + 31) / 32;
-	d.slice_words = (d.sw + 31) / 32;
-	d.nwords = (h.n + 31) / 32;
-	d.bm_words = d.num_stripes * d.slice_words;  // bulk copies read whole slices
-	d.tma = (d.sw % 128 == 0) ? 1u : 0u;
-	d.tma_batch = std::max<uint32_t>(1, std::min<uint32_t>(kMaxSliceBatch, kTmaSliceWords / d.slice_words));
-	d.pull_long_cap = 4096;
 	if ((st = dev_upload(g, &d.row_off, h.row_off))) return st;
 	if ((st = dev_upload(g, &d.col, h.csr_dst))) return st;
 	if ((st = dev_upload(g, &d.packed, pk.words))) return st;
@@ -222,49 +280,139 @@ int upload(bfs_graph *g, HostGraph &h) {
 			for (uint32_t e = h.row_off[u]; e < h.row_off[u + 1]; ++e) in_src[fill[h.csr_dst[e]]++] = u;
 		if ((st = dev_upload(g, &d.in_off, in_off))) return st;
 		if ((st = dev_upload(g, &d.in_src, in_src))) return st;
-		// batched pull: destinations with many in-edges and their chunks
-		std::vector<uint32_t> in_big, chunk_v, chunk_beg;
-		for (uint32_t v = 0; v < h.n; ++v) {
-			if (in_off[v + 1] - in_off[v] <= kMsPullBig) continue;
-			in_big.push_back(v);
-			for (uint32_t b = in_off[v]; b < in_off[v + 1]; b += kMsChunk) {
-				chunk_v.push_back(v);
-				chunk_beg.push_back(b);
-			}
+		if ((st = upload_big_in(g, in_off))) return st;
+	}
+	return alloc_run(g);
+}
+
+// Temporary device buffers of the device build, freed on scope exit.
+struct TmpDev {
+	std::vector<void *> ptrs;
+	template <class T> int alloc(T **p, size_t count) {
+		void *q = nullptr;
+		if (cudaMalloc(&q, std::max<size_t>(count * sizeof(T), 16)) != cudaSuccess) {
+			cudaGetLastError();
+			return BFS_ENOMEM;
 		}
-		g->ms_nbig_in = (uint32_t) in_big.size();
-		g->ms_nchunks = (uint32_t) chunk_v.size();
-		if ((st = dev_upload(g, &g->ms_in_big, in_big))) return st;
-		if ((st = dev_upload(g, &g->ms_chunk_v, chunk_v))) return st;
-		if ((st = dev_upload(g, &g->ms_chunk_beg, chunk_beg))) return st;
+		ptrs.push_back(q);
+		*p = (T *) q;
+		return BFS_OK;
 	}
+	~TmpDev() {
+		for (void *p : ptrs) cudaFree(p);
+	}
+};
 
-	// Run context.
-	RunCtx &r = g->rc;
-	if ((st = dev_alloc(g, &r.vis, d.nwords))) return st;
-	for (int i = 0; i < 3; ++i) {
-		if ((st = dev_alloc(g, &r.bm[i], d.bm_words))) return st;
-		if ((st = dev_alloc(g, &r.sf[i], d.num_stripes))) return st;
-	}
-	for (int set = 0; set < 2; ++set)
-		for (int b = 0; b < 3; ++b)
-			if ((st = dev_alloc(g, &r.q[set][b], h.n))) return st;
-	if ((st = dev_alloc(g, &r.ctr, 3))) return st;
-	if ((st = dev_alloc(g, &r.part, 6 * (size_t) kMaxGrid))) return st;
-	if ((st = dev_alloc(g, &r.stats, 1))) return st;
-	if ((st = dev_alloc(g, &r.bar, 2))) return st;
-	if ((st = dev_alloc(g, &r.err, 1))) return st;
-	if ((st = dev_alloc(g, &g->level_buf, h.n))) return st;
-	if ((st = dev_alloc(g, &g->parent_buf, h.n))) return st;
-	if (cudaMallocHost(&g->h_stats, sizeof(DevStats)) != cudaSuccess) return BFS_ENOMEM;
-	if (cudaMallocHost(&g->h_part, sizeof(unsigned long long) * 2 * kMaxGrid) != cudaSuccess) return BFS_ENOMEM;
-	if (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess ||
-			cudaEventCreate(&g->evm) != cudaSuccess)
+// The device layout of an edge list built on the GPU (build_device.cu): CSR
+// and in-edge lists by degree histograms, scans and scatters; the packed
+// column-major segments by a segment histogram, the host's group plan and
+// segment offsets, and a scatter; the out-degrees and in-edge offsets come
+// back for the host-side fields.
+int upload_device_build(bfs_graph *g, uint32_t n, uint64_t m, const uint32_t *src, const uint32_t *dst, uint32_t w,
+		uint32_t s) {
+	g->n = n;
+	g->m = m;
+	g->w = w;
+	g->s = s;
+	g->side = side_length_of(n, w);
+	g->num_stripes = (g->side + s - 1) / s;
+	default_options(&g->opt);
+	int st = device_setup(g);
+	if (st) return st;
+	cudaStream_t cs = nullptr;
+	TmpDev tmp;
+	DevGraph &d = g->dg;
+	uint32_t *d_src = nullptr, *d_dst = nullptr, *out_deg = nullptr, *in_deg = nullptr, *cursor = nullptr, *scan_tmp = nullptr;
+	int *d_err = nullptr;
+	if ((st = tmp.alloc(&d_src, m)) || (st = tmp.alloc(&d_dst, m)) || (st = tmp.alloc(&out_deg, n)) ||
+			(st = tmp.alloc(&in_deg, n)) || (st = tmp.alloc(&cursor, (size_t) n + 1)) ||
+			(st = tmp.alloc(&scan_tmp, dbuild_scan_tmp_words(n))) || (st = tmp.alloc(&d_err, 1)))
+		return st;
+	if (m && (cudaMemcpy(d_src, src, m * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+			cudaMemcpy(d_dst, dst, m * 4, cudaMemcpyHostToDevice) != cudaSuccess))
 		return BFS_ECUDA;
-
-	g->batch = std::max<uint32_t>(1, std::min<uint32_t>(kMaxSliceBatch, kSliceBudgetWords / std::max<uint32_t>(1, d.slice_words)));
-	if ((st = persistent_grid(d, g->batch, g->num_sms, &g->grid, &g->smem))) return st;
-	return BFS_OK;
+	if (cudaMemset(out_deg, 0, (size_t) n * 4) != cudaSuccess || cudaMemset(in_deg, 0, (size_t) n * 4) != cudaSuccess ||
+			cudaMemset(d_err, 0, 4) != cudaSuccess)
+		return BFS_ECUDA;
+	if ((st = dbuild_degrees(d_src, d_dst, m, n, out_deg, in_deg, d_err, g->num_sms, cs))) return st;
+	int herr = 0;
+	if (cudaMemcpy(&herr, d_err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BFS_ECUDA;
+	if (herr) return herr;
+	// CSR and in-edge lists
+	uint32_t *row_off = nullptr, *col = nullptr, *in_off = nullptr, *in_src = nullptr;
+	if ((st = dev_alloc(g, &row_off, (size_t) n + 1)) || (st = dev_alloc(g, &col, m)) ||
+			(st = dev_alloc(g, &in_off, (size_t) n + 1)) || (st = dev_alloc(g, &in_src, m)))
+		return st;
+	if ((st = dbuild_exclusive_scan(out_deg, n, scan_tmp, row_off, cs))) return st;
+	if (cudaMemcpy(cursor, row_off, (size_t) n * 4, cudaMemcpyDeviceToDevice) != cudaSuccess) return BFS_ECUDA;
+	if ((st = dbuild_scatter(d_src, d_dst, m, cursor, col, g->num_sms, cs))) return st;
+	if ((st = dbuild_exclusive_scan(in_deg, n, scan_tmp, in_off, cs))) return st;
+	if (cudaMemcpy(cursor, in_off, (size_t) n * 4, cudaMemcpyDeviceToDevice) != cudaSuccess) return BFS_ECUDA;
+	if ((st = dbuild_scatter(d_dst, d_src, m, cursor, in_src, g->num_sms, cs))) return st;
+	d.row_off = row_off;
+	d.col = col;
+	d.in_off = in_off;
+	d.in_src = in_src;
+	// host-side fields
+	g->degrees.resize(n);
+	std::vector<uint32_t> h_in_off((size_t) n + 1);
+	if (cudaMemcpy(g->degrees.data(), out_deg, (size_t) n * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+			cudaMemcpy(h_in_off.data(), in_off, ((size_t) n + 1) * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return BFS_ECUDA;
+	g->max_degree = 0;
+	for (uint32_t v = 0; v < n; ++v) g->max_degree = std::max(g->max_degree, g->degrees[v]);
+	if ((st = upload_big_in(g, h_in_off))) return st;
+	// packed column-major segments
+	uint32_t *col_edges = nullptr, *hasin = nullptr;
+	if ((st = tmp.alloc(&col_edges, g->side)) || (st = dev_alloc(g, &hasin, ((size_t) n + 31) / 32))) return st;
+	if (cudaMemset(col_edges, 0, (size_t) g->side * 4) != cudaSuccess ||
+			cudaMemset(hasin, 0, ((size_t) n + 31) / 32 * 4) != cudaSuccess)
+		return BFS_ECUDA;
+	if ((st = dbuild_col_hist(d_dst, m, w, col_edges, hasin, g->num_sms, cs))) return st;
+	std::vector<uint32_t> h_col32(g->side);
+	if (cudaMemcpy(h_col32.data(), col_edges, (size_t) g->side * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return BFS_ECUDA;
+	std::vector<uint64_t> h_col(h_col32.begin(), h_col32.end());
+	PackedTiles pk;
+	if ((st = plan_groups(n, w, s, g->side, h_col, m, (uint32_t) g->num_sms * 2 * kGroupsPerCta, kMaxGroupVertices, pk)))
+		return st;
+	std::vector<uint32_t> group_of(g->side);
+	for (uint32_t gi = 0; gi < pk.num_groups; ++gi)
+		for (uint32_t c = pk.group_col[gi]; c < pk.group_col[gi + 1]; ++c) group_of[c] = gi;
+	const uint64_t nseg = (uint64_t) g->num_stripes * pk.num_groups;
+	uint32_t *d_group_of = nullptr, *seg_count = nullptr, *seg_cursor = nullptr, *pad = nullptr;
+	if ((st = tmp.alloc(&d_group_of, g->side)) || (st = tmp.alloc(&seg_count, nseg)) || (st = tmp.alloc(&seg_cursor, nseg)) ||
+			(st = tmp.alloc(&pad, pk.num_groups)))
+		return st;
+	const uint32_t *group_col = nullptr;
+	if ((st = dev_upload(g, &group_col, pk.group_col))) return st;
+	if (cudaMemcpy(d_group_of, group_of.data(), (size_t) g->side * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+			cudaMemset(seg_count, 0, nseg * 4) != cudaSuccess)
+		return BFS_ECUDA;
+	DeviceBuildShape sh{w, s, g->num_stripes, pk.vbits, pk.cbits};
+	if ((st = dbuild_seg_hist(d_src, d_dst, m, sh, d_group_of, seg_count, g->num_sms, cs))) return st;
+	std::vector<uint32_t> h_seg32(nseg);
+	if (cudaMemcpy(h_seg32.data(), seg_count, nseg * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BFS_ECUDA;
+	std::vector<uint64_t> h_seg(h_seg32.begin(), h_seg32.end());
+	if ((st = segment_offsets(h_seg, pk))) return st;
+	const uint64_t words = pk.seg_off[nseg];
+	std::vector<uint32_t> pad_word(pk.num_groups);
+	for (uint32_t gi = 0; gi < pk.num_groups; ++gi) pad_word[gi] = group_pad_word(pk, gi, n, w);
+	const uint32_t *seg_off = nullptr;
+	uint32_t *packed = nullptr;
+	if ((st = dev_upload(g, &seg_off, pk.seg_off)) || (st = dev_alloc(g, &packed, words))) return st;
+	if (cudaMemcpy(seg_cursor, seg_off, nseg * 4, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+			cudaMemcpy(pad, pad_word.data(), pk.num_groups * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+		return BFS_ECUDA;
+	if ((st = dbuild_seg_fill(d_src, d_dst, m, sh, d_group_of, group_col, seg_cursor, packed, g->num_sms, cs))) return st;
+	if ((st = dbuild_seg_pad(seg_off, seg_count, nseg, g->num_stripes, pad, packed, g->num_sms, cs))) return st;
+	if (cudaDeviceSynchronize() != cudaSuccess) return BFS_ECUDA;
+	d.packed = packed;
+	d.seg_off = seg_off;
+	d.group_col = group_col;
+	d.hasin = hasin;
+	set_shape(g, pk, words);
+	return alloc_run(g);
 }
 
 int finish_graph(HostGraph &h, uint32_t flags, bfs_graph **out) {
@@ -779,6 +927,17 @@ int bfs_graph_from_edges(uint32_t num_vertices, uint64_t num_edges, const uint32
 	*out = nullptr;
 	int st = check_shape(num_vertices, num_edges, tile_width, stripe_length);
 	if (st) return st;
+	if ((flags & BFS_LOAD_DEVICE_BUILD) && !(flags & BFS_LOAD_HOST_ONLY)) {
+		bfs_graph *g = new bfs_graph();
+		st = upload_device_build(g, num_vertices, num_edges, src, dst, tile_width, stripe_length);
+		if (st) {
+			release(g);
+			delete g;
+			return st;
+		}
+		*out = g;
+		return BFS_OK;
+	}
 	HostGraph h;
 	init_shape(h, num_vertices, num_edges, tile_width, stripe_length);
 	std::vector<uint32_t> cs;

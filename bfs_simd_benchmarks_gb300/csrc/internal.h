@@ -74,6 +74,12 @@ int colmajor_from_csr(uint32_t n, uint64_t m, uint32_t w, uint32_t s, const uint
 int validate_colmajor(const HostGraph &g);
 int finish_csr(HostGraph &g);
 int pack_tiles(const HostGraph &g, uint32_t target_groups, uint32_t max_group_vertices, PackedTiles &out);
+// the parts of pack_tiles the device build shares: column groups from the
+// in-edges per tile column, a group's padding word, segment offsets (padded)
+int plan_groups(uint32_t n, uint32_t w, uint32_t s, uint32_t side, const std::vector<uint64_t> &col_edges,
+		uint64_t m, uint32_t target_groups, uint32_t max_group_vertices, PackedTiles &out);
+uint32_t group_pad_word(const PackedTiles &out, uint32_t gi, uint32_t n, uint32_t w);
+int segment_offsets(const std::vector<uint64_t> &seg_count, PackedTiles &out);
 
 // small parallel helper
 unsigned host_threads();

@@ -158,8 +158,8 @@ int finish_csr(HostGraph &g) {
 	return BFS_OK;
 }
 
-int pack_tiles(const HostGraph &g, uint32_t target_groups, uint32_t max_group_vertices, PackedTiles &out) {
-	const uint32_t w = g.w, s = g.s, side = g.side, stripes = g.num_stripes;
+int plan_groups(uint32_t n, uint32_t w, uint32_t s, uint32_t side, const std::vector<uint64_t> &col_edges,
+		uint64_t m, uint32_t target_groups, uint32_t max_group_vertices, PackedTiles &out) {
 	out.vbits = ceil_log2(w);
 	out.ubits = ceil_log2((uint64_t) s * w);
 	if (out.vbits + out.ubits > 31) return BFS_EUNSUPPORTED;
@@ -175,18 +175,9 @@ int pack_tiles(const HostGraph &g, uint32_t target_groups, uint32_t max_group_ve
 	if (w > max_group_vertices) return BFS_EUNSUPPORTED;
 	max_cols = std::min(max_cols, cols_by_smem);
 
-	// In-edges per tile column and the in-degree > 0 bitmap.
-	std::vector<uint64_t> col_edges(side, 0);
-	out.hasin_bits.assign(((size_t) g.n + 31) / 32, 0);
-	for (uint64_t i = 0; i < g.m; ++i) {
-		uint32_t v = g.tails[i];
-		col_edges[v / w]++;
-		out.hasin_bits[v >> 5] |= 1u << (v & 31);
-	}
-
 	// Greedy column groups of about m/target_groups edges.
 	if (target_groups == 0) target_groups = 1;
-	uint64_t target = std::max<uint64_t>(1, (g.m + target_groups - 1) / target_groups);
+	uint64_t target = std::max<uint64_t>(1, (m + target_groups - 1) / target_groups);
 	out.group_col.clear();
 	out.group_col.push_back(0);
 	uint64_t acc = 0, cols = 0;
@@ -202,13 +193,53 @@ int pack_tiles(const HostGraph &g, uint32_t target_groups, uint32_t max_group_ve
 	if (out.group_col.back() != side) out.group_col.push_back(side);
 	out.num_groups = (uint32_t) out.group_col.size() - 1;
 	out.max_group_vertices = 0;
-	std::vector<uint32_t> group_of(side);
 	for (uint32_t gi = 0; gi < out.num_groups; ++gi) {
-		for (uint32_t c = out.group_col[gi]; c < out.group_col[gi + 1]; ++c) group_of[c] = gi;
 		uint64_t v0 = (uint64_t) out.group_col[gi] * w;
-		uint64_t v1 = std::min<uint64_t>((uint64_t) out.group_col[gi + 1] * w, g.n);
+		uint64_t v1 = std::min<uint64_t>((uint64_t) out.group_col[gi + 1] * w, n);
 		out.max_group_vertices = std::max<uint32_t>(out.max_group_vertices, (uint32_t) (v1 - v0));
 	}
+	(void) s;
+	return BFS_OK;
+}
+
+uint32_t group_pad_word(const PackedTiles &out, uint32_t gi, uint32_t n, uint32_t w) {
+	// Padding words decode to destination 32*ceil(group_vertices/32): the slot
+	// right after the group's bitmap, which the kernel keeps "visited", so a
+	// padding word is skipped by the ordinary visited test.
+	uint64_t v0 = (uint64_t) out.group_col[gi] * w;
+	uint64_t v1 = std::min<uint64_t>((uint64_t) out.group_col[gi + 1] * w, n);
+	uint64_t d = (v1 - v0 + 31) / 32 * 32;
+	return (uint32_t) (d % w) | (uint32_t) ((d / w) << out.vbits);
+}
+
+int segment_offsets(const std::vector<uint64_t> &seg_count, PackedTiles &out) {
+	const uint64_t nseg = seg_count.size();
+	out.seg_off.assign(nseg + 1, 0);
+	uint64_t words = 0;
+	for (uint64_t j = 0; j < nseg; ++j) {
+		out.seg_off[j] = (uint32_t) words;
+		words += (seg_count[j] + 3) & ~uint64_t(3);
+		if (words > 0xFFFFFFF0ull) return BFS_EUNSUPPORTED;
+	}
+	out.seg_off[nseg] = (uint32_t) words;
+	return BFS_OK;
+}
+
+int pack_tiles(const HostGraph &g, uint32_t target_groups, uint32_t max_group_vertices, PackedTiles &out) {
+	const uint32_t w = g.w, s = g.s, side = g.side, stripes = g.num_stripes;
+	// In-edges per tile column and the in-degree > 0 bitmap.
+	std::vector<uint64_t> col_edges(side, 0);
+	out.hasin_bits.assign(((size_t) g.n + 31) / 32, 0);
+	for (uint64_t i = 0; i < g.m; ++i) {
+		uint32_t v = g.tails[i];
+		col_edges[v / w]++;
+		out.hasin_bits[v >> 5] |= 1u << (v & 31);
+	}
+	int st = plan_groups(g.n, w, s, side, col_edges, g.m, target_groups, max_group_vertices, out);
+	if (st) return st;
+	std::vector<uint32_t> group_of(side);
+	for (uint32_t gi = 0; gi < out.num_groups; ++gi)
+		for (uint32_t c = out.group_col[gi]; c < out.group_col[gi + 1]; ++c) group_of[c] = gi;
 
 	// Segment sizes: heads/tails are in column-major order, so the edges of
 	// (stripe, group) are contiguous; count them.
@@ -218,25 +249,10 @@ int pack_tiles(const HostGraph &g, uint32_t target_groups, uint32_t max_group_ve
 		uint32_t k = g.heads[i] / w / s;
 		seg_count[(uint64_t) group_of[g.tails[i] / w] * stripes + k]++;
 	}
-	out.seg_off.assign(nseg + 1, 0);
-	uint64_t words = 0;
-	for (uint64_t j = 0; j < nseg; ++j) {
-		out.seg_off[j] = (uint32_t) words;
-		words += (seg_count[j] + 3) & ~uint64_t(3);
-		if (words > 0xFFFFFFF0ull) return BFS_EUNSUPPORTED;
-	}
-	out.seg_off[nseg] = (uint32_t) words;
-	out.words.assign(words, 0);
-	// Padding words decode to destination 32*ceil(group_vertices/32): the slot
-	// right after the group's bitmap, which the kernel keeps "visited", so a
-	// padding word is skipped by the ordinary visited test.
+	if ((st = segment_offsets(seg_count, out))) return st;
+	out.words.assign(out.seg_off[nseg], 0);
 	std::vector<uint32_t> pad_word(out.num_groups);
-	for (uint32_t gi = 0; gi < out.num_groups; ++gi) {
-		uint64_t v0 = (uint64_t) out.group_col[gi] * w;
-		uint64_t v1 = std::min<uint64_t>((uint64_t) out.group_col[gi + 1] * w, g.n);
-		uint64_t d = (v1 - v0 + 31) / 32 * 32;
-		pad_word[gi] = (uint32_t) (d % w) | (uint32_t) ((d / w) << out.vbits);
-	}
+	for (uint32_t gi = 0; gi < out.num_groups; ++gi) pad_word[gi] = group_pad_word(out, gi, g.n, w);
 	for (uint64_t j = 0; j < nseg; ++j) {
 		uint32_t gi = (uint32_t) (j / stripes);
 		for (uint64_t x = out.seg_off[j] + seg_count[j]; x < out.seg_off[j + 1]; ++x) out.words[x] = pad_word[gi];

@@ -45,13 +45,14 @@ class Graph:
 
     @classmethod
     def from_edges(cls, num_vertices: int, src, dst, tile_width: int, stripe_length: int,
-                   host_only: bool = False) -> "Graph":
+                   host_only: bool = False, device_build: bool = False) -> "Graph":
+        """device_build: build the layout on the GPU (BFS_LOAD_DEVICE_BUILD)."""
         lib = N.load()
         s, d = _u32(src), _u32(dst)
         if s.shape != d.shape:
             raise ValueError("src and dst differ in length")
         h = C.c_void_p()
-        flags = N.BFS_LOAD_HOST_ONLY if host_only else 0
+        flags = (N.BFS_LOAD_HOST_ONLY if host_only else 0) | (N.BFS_LOAD_DEVICE_BUILD if device_build else 0)
         N.check(lib.bfs_graph_from_edges(num_vertices, s.size, _ptr(s, C.c_uint32), _ptr(d, C.c_uint32),
                                          tile_width, stripe_length, flags, C.byref(h)), "bfs_graph_from_edges")
         return cls(h)

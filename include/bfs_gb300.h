@@ -51,6 +51,8 @@ typedef struct bfs_graph bfs_graph;
 #define BFS_LOAD_WEIGHTED 0x1u     /* files carry "u v w" lines (-w); weights are dropped */
 #define BFS_LOAD_PREFER_REORDER 0x2u /* try <data>_reorder_* before <data>_* */
 #define BFS_LOAD_HOST_ONLY 0x4u    /* parse and validate only; allocate nothing on the GPU */
+#define BFS_LOAD_DEVICE_BUILD 0x8u /* bfs_graph_from_edges: build CSR, in-edge lists and packed tiles on the
+                                      GPU (edge order inside rows and tiles unspecified; results unchanged) */
 
 /*
  * Loads a graph from the reference's tiled text files and uploads it to HBM.

@@ -221,3 +221,36 @@ def test_pokec_shape_64_sources(native, oracle):
             k = min(len(trace), st["num_steps"])
             assert st["trace"][:k] == trace[:k]
         assert oracle.check_parents(arr, int(sv), lev, par) == 0
+
+
+@pytest.mark.parametrize("shape", [(1 << 14, 16, 1024, 16, True), (20011, 7, 512, 8, False), (1 << 12, 24, 4096, 32, True)])
+def test_device_build_matches_host_build(native, oracle, shape):
+    """BFS_LOAD_DEVICE_BUILD: the same degrees, groups and packed size as the
+    host build, and the reference's levels in both bottom-up variants and
+    batched."""
+    import bfs_simd_benchmarks_gb300 as B
+    n, ef, w, s, perm = shape
+    src, dst = B.gen_rmat(n, ef * n, seed=n + w, permute=perm)
+    arr = oracle.arrays_from_edges(n, src, dst, w, s)
+    srcs = B.pick_sources(arr["degrees"], 6, seed=3)
+    with B.Graph.from_edges(n, src, dst, w, s) as gh, B.Graph.from_edges(n, src, dst, w, s, device_build=True) as gd:
+        ih, idv = gh.info(), gd.info()
+        for k in ("num_vertices", "num_edges", "num_groups", "packed_words", "max_out_degree", "side_length",
+                  "num_stripes"):
+            assert ih[k] == idv[k], k
+        np.testing.assert_array_equal(gh.degrees(), gd.degrees())
+        for bu in ("pull", "stream"):
+            gd.set_options(bottom_up=bu)
+            for sv in srcs:
+                _check_run(B, oracle, arr, gd, sv)
+        lev, st = gd.run_batch(B.pick_sources(arr["degrees"], 70, seed=4))
+        exp = np.where(oracle.bfs_levels(arr, int(B.pick_sources(arr["degrees"], 70, seed=4)[0])) < 0, 255,
+                       oracle.bfs_levels(arr, int(B.pick_sources(arr["degrees"], 70, seed=4)[0])))
+        np.testing.assert_array_equal(lev.cpu().numpy()[0], exp.astype(np.uint8))
+
+
+def test_device_build_rejects_bad_ids(native):
+    import bfs_simd_benchmarks_gb300 as B
+    with pytest.raises(B.BfsError) as ei:
+        B.Graph.from_edges(10, np.array([1, 2], np.uint32), np.array([3, 10], np.uint32), 4, 2, device_build=True)
+    assert ei.value.status == 2
