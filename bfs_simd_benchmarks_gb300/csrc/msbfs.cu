@@ -43,6 +43,8 @@ constexpr int kMsWarps = kMsThreads / 32;
 constexpr uint32_t kMsWq = 64;          // per-warp staged queue appends (pull)
 constexpr uint32_t kMsBig = 1024;       // push: higher-degree vertices are spread over the grid
 constexpr int kMsGather = 4;            // pull: frontier rows gathered per round
+constexpr uint32_t kLaneMaxWords = 2;   // pull: up to this many words per vertex ...
+constexpr uint32_t kLaneMaxDeg = 32;    // ... destinations of at most this in-degree go one per lane
 constexpr uint32_t kEmitV = 128;        // output tile: 128 vertices x 4 words (256 sources)
 constexpr uint32_t kEmitW = 4;
 constexpr uint32_t kEmitStride = 132;   // shared row stride in bytes (33 words: column writes spread over banks)
@@ -51,6 +53,9 @@ constexpr uint32_t kEmitBytes = kEmitW * 64 * kEmitStride;
 __device__ __forceinline__ uint64_t ld_cg64(const uint64_t *p) { return __ldcg((const unsigned long long *) p); }
 __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
 	return (uint64_t) __shfl_sync(kFull, (unsigned long long) x, src);
+}
+__device__ __forceinline__ uint64_t shfl_xor64(uint64_t x, int mask) {
+	return (uint64_t) __shfl_xor_sync(kFull, (unsigned long long) x, mask);
 }
 __device__ __forceinline__ uint32_t deg_of(const MsArgs &a, uint32_t v) {
 	return __ldg(a.row_off + v + 1) - __ldg(a.row_off + v);
@@ -287,6 +292,89 @@ __device__ __forceinline__ uint32_t block_perm(uint32_t x, uint32_t bits) {
 	return x;
 }
 
+__device__ __forceinline__ uint64_t warp_or64(uint64_t x) {
+#pragma unroll
+	for (int d = 16; d > 0; d >>= 1) x |= shfl_xor64(x, d);
+	return x;
+}
+
+// ms_gather for K <= 2 words per vertex: lanes take in-edges (32 per step)
+// instead of words, read the neighbour's needed non-zero words and OR them
+// across the warp.  Inputs and outputs are word 0 / word 1 in every lane.
+__device__ __forceinline__ void ms_gather_edges(const MsArgs &a, const uint64_t *cur, const uint64_t *actc,
+		uint32_t beg, uint32_t end, uint64_t f0, uint64_t f1, uint64_t vis0, uint64_t vis1, uint64_t &acc0,
+		uint64_t &acc1, unsigned long long &gathered) {
+	const uint32_t K = a.K;
+	const unsigned lane = lane_id();
+	for (uint32_t e0 = beg; e0 < end; e0 += 32) {
+		const bool n0 = ((vis0 | acc0) & f0) != f0, n1 = ((vis1 | acc1) & f1) != f1;
+		if (!n0 && !n1) break;  // uniform: every lane holds the same words
+		const uint32_t e = e0 + lane;
+		const uint32_t u = e < end ? __ldg(a.in_src + e) : 0u;
+		const uint64_t m = e < end ? ld_cg64(actc + u) : 0ull;
+		const uint64_t g0 = (n0 && (m & 1ull)) ? ld_cg64(cur + (size_t) u * K) : 0ull;
+		const uint64_t g1 = (n1 && (m & 2ull)) ? ld_cg64(cur + (size_t) u * K + 1) : 0ull;
+		gathered += m != 0ull;
+		acc0 |= warp_or64(g0);
+		acc1 |= warp_or64(g1);
+	}
+}
+
+// Pull of one destination by one lane (K <= kLaneMaxWords words per vertex,
+// at most kLaneMaxDeg in-edges): the lane walks the in-edges four at a time,
+// reads a neighbour's word only where its mask is set and the destination
+// still lacks sources, and stops when every source has arrived.  Lanes with
+// `mine` false only take part in the warp-wide appends.
+__device__ __forceinline__ void ms_pull_lane(const MsArgs &a, const uint64_t *cur, const uint64_t *actc,
+		uint64_t *nxt, uint64_t *actn, uint32_t v, uint32_t beg, uint32_t end, bool mine, unsigned long long &actdeg,
+		unsigned long long &gathered, MsCounters *cn, uint32_t *qn) {
+	const uint32_t K = a.K;
+	const uint64_t last = a.last_bits == 64 ? ~0ull : ((1ull << a.last_bits) - 1);
+	const uint64_t f0 = K == 1 ? last : ~0ull, f1 = K == 2 ? last : 0ull;
+	uint64_t vis0 = 0, vis1 = 0, acc0 = 0, acc1 = 0;
+	bool any = false;
+	uint32_t d = 0;
+	if (mine) {
+		const size_t row = (size_t) v * K;
+		vis0 = ld_cg64(a.vis + row);
+		vis1 = K == 2 ? ld_cg64(a.vis + row + 1) : 0ull;
+		for (uint32_t e = beg; e < end; e += 4) {
+			if (((vis0 | acc0) & f0) == f0 && ((vis1 | acc1) & f1) == f1) break;
+			uint32_t u[4];
+			uint64_t m[4];
+#pragma unroll
+			for (int t = 0; t < 4; ++t) u[t] = e + t < end ? __ldg(a.in_src + e + t) : 0xFFFFFFFFu;
+#pragma unroll
+			for (int t = 0; t < 4; ++t) m[t] = u[t] != 0xFFFFFFFFu ? ld_cg64(actc + u[t]) : 0ull;
+			const bool n0 = ((vis0 | acc0) & f0) != f0, n1 = ((vis1 | acc1) & f1) != f1;
+			uint64_t g0[4], g1[4];
+#pragma unroll
+			for (int t = 0; t < 4; ++t) {
+				g0[t] = (n0 && (m[t] & 1ull)) ? ld_cg64(cur + (size_t) u[t] * K) : 0ull;
+				g1[t] = (n1 && (m[t] & 2ull)) ? ld_cg64(cur + (size_t) u[t] * K + 1) : 0ull;
+				gathered += m[t] != 0ull;
+			}
+#pragma unroll
+			for (int t = 0; t < 4; ++t) { acc0 |= g0[t]; acc1 |= g1[t]; }
+		}
+		const uint64_t w0 = acc0 & ~vis0 & f0, w1 = acc1 & ~vis1 & f1;
+		nxt[row] = w0;
+		if (w0) a.vis[row] = vis0 | w0;
+		if (K == 2) {
+			nxt[row + 1] = w1;
+			if (w1) a.vis[row + 1] = vis1 | w1;
+		}
+		actn[v] = (w0 ? 1ull : 0ull) | (w1 ? 2ull : 0ull);
+		if (((vis0 | w0) & f0) == f0 && ((vis1 | w1) & f1) == f1) a.done[v] = 1;
+		any = (w0 | w1) != 0ull;
+		if (any) {
+			d = deg_of(a, v);
+			actdeg += d;
+		}
+	}
+	ms_append(a, cn, qn, v, any && d <= kMsBig, any && d > kMsBig);
+}
+
 // Pull, destinations with at most kMsPullBig in-edges.  A warp screens 32
 // consecutive destinations at once (their in-edge ranges and "every source
 // has arrived" flags, lane-parallel), clears the rows of those with nothing
@@ -326,7 +414,14 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, cons
 		uint64_t *blk = nxt + (size_t) vb * K;
 		for (uint32_t x = lane; x < nb * K; x += 32)
 			if (!((needm >> (x / K)) & 1u)) blk[x] = 0ull;
-		for (uint32_t m = needm; m; m &= m - 1) {
+		// few words per vertex: every lane takes its own low in-degree destination
+		uint32_t warpm = needm;
+		if (K <= kLaneMaxWords) {
+			const bool mine = needy && lend - lbeg <= kLaneMaxDeg;
+			warpm &= ~__ballot_sync(kFull, mine);
+			ms_pull_lane(a, cur, actc, nxt, actn, vl, lbeg, lend, mine, actdeg, gathered, cn, qn);
+		}
+		for (uint32_t m = warpm; m; m &= m - 1) {
 			const int jj = __ffs(m) - 1;
 			const uint32_t v = vb + jj;
 			const uint32_t beg = __shfl_sync(kFull, lbeg, jj), end = __shfl_sync(kFull, lend, jj);
@@ -334,7 +429,15 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, cons
 			const uint64_t vis0 = w0 ? ld_cg64(a.vis + row + lane) : 0ull;
 			const uint64_t vis1 = w1 ? ld_cg64(a.vis + row + lane + 32) : 0ull;
 			uint64_t acc0 = 0, acc1 = 0;
-			if (!fm.complete(vis0, vis1)) ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
+			if (K <= kLaneMaxWords) {
+				// lanes hold words lane; the edge-parallel gather wants both words everywhere
+				uint64_t a0 = 0, a1 = 0;
+				ms_gather_edges(a, cur, actc, beg, end, shfl64(fm.f0, 0), shfl64(fm.f0, 1), shfl64(vis0, 0),
+						shfl64(vis0, 1), a0, a1, gathered);
+				acc0 = lane == 0 ? a0 : (lane == 1 ? a1 : 0ull);
+			} else if (!fm.complete(vis0, vis1)) {
+				ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
+			}
 			const uint64_t n0 = acc0 & ~vis0 & fm.f0, n1 = acc1 & ~vis1 & fm.f1;
 			if (w0) { nxt[row + lane] = n0; if (n0) a.vis[row + lane] = vis0 | n0; }
 			if (w1) { nxt[row + lane + 32] = n1; if (n1) a.vis[row + lane + 32] = vis1 | n1; }
@@ -377,7 +480,14 @@ __device__ void ms_pull_chunks(const MsArgs &a, const uint64_t *cur, const uint6
 		const uint64_t vis1 = w1 ? ld_cg64(a.vis + row + lane + 32) : 0ull;
 		if (fm.complete(vis0, vis1)) continue;
 		uint64_t acc0 = 0, acc1 = 0;
-		ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
+		if (K <= kLaneMaxWords) {
+			uint64_t a0 = 0, a1 = 0;
+			ms_gather_edges(a, cur, actc, beg, end, shfl64(fm.f0, 0), shfl64(fm.f0, 1), shfl64(vis0, 0), shfl64(vis0, 1),
+					a0, a1, gathered);
+			acc0 = lane == 0 ? a0 : (lane == 1 ? a1 : 0ull);
+		} else {
+			ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
+		}
 		const uint64_t n0 = acc0 & ~vis0 & fm.f0, n1 = acc1 & ~vis1 & fm.f1;
 		if (n0) atomicOr((unsigned long long *) (nxt + row + lane), (unsigned long long) n0);
 		if (n1) atomicOr((unsigned long long *) (nxt + row + lane + 32), (unsigned long long) n1);
@@ -437,7 +547,7 @@ __device__ __forceinline__ uint32_t nibble_bytes(uint32_t nib) {
 	return ((nib * 0x00204081u) & 0x01010101u) * 0xFFu;  // bit i -> byte i all ones
 }
 
-__device__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t ns, uint32_t base, uint32_t first, uint32_t last,
+__device__ __noinline__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t ns, uint32_t base, uint32_t first, uint32_t last,
 		bool merge, uint8_t *lev) {
 	constexpr uint32_t kRows = kEmitW * 64;
 	const uint32_t K = a.K, n = a.n;
