@@ -95,23 +95,27 @@ __device__ __forceinline__ void visit_and_append(const bool (&has)[kTdPerLane], 
 	uint32_t word[kTdPerLane];
 #pragma unroll
 	for (int q = 0; q < kTdPerLane; ++q) word[q] = has[q] ? ld_cg(r.vis + (v[q] >> 5)) : ~0u;
-#pragma unroll
-	for (int q = 0; q < kTdPerLane; ++q) {
-		const uint32_t bit = 1u << (v[q] & 31);
-		if (!(word[q] & bit)) word[q] = atomicOr(r.vis + (v[q] >> 5), bit);
-	}
-	uint32_t deg[kTdPerLane];
+	// The claim is a compare-and-swap on the destination's own level (-1 ->
+	// next level): only edges to the same destination contend, not the 32
+	// destinations of a bitmap word.  The visited bit follows with a
+	// reduction whose result nobody waits for.
 	bool claimed[kTdPerLane];
 #pragma unroll
 	for (int q = 0; q < kTdPerLane; ++q) {
-		claimed[q] = !(word[q] & (1u << (v[q] & 31)));
+		claimed[q] = false;
+		if (!(word[q] & (1u << (v[q] & 31))))
+			claimed[q] = atomicCAS((int *) r.level + v[q], -1, next_level) == -1;
+	}
+	uint32_t deg[kTdPerLane];
+#pragma unroll
+	for (int q = 0; q < kTdPerLane; ++q) {
+		if (claimed[q]) atomicOr(r.vis + (v[q] >> 5), 1u << (v[q] & 31));
 		deg[q] = claimed[q] ? __ldg(g.row_off + v[q] + 1) - __ldg(g.row_off + v[q]) : 0u;
 	}
 	uint32_t cnt[3] = {0, 0, 0};
 #pragma unroll
 	for (int q = 0; q < kTdPerLane; ++q) {
 		if (!claimed[q]) continue;
-		r.level[v[q]] = next_level;
 		if (r.parent) r.parent[v[q]] = u[q];
 		acc.count++;
 		acc.degsum += deg[q];
@@ -226,11 +230,19 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 		__syncthreads();
 	}
 	// Medium out-degree, many vertices: a CTA expands a chunk of up to 32
-	// vertices as one flat edge list.
+	// vertices as one flat edge list.  Chunks (about 8 per CTA) are handed out
+	// by a counter, the next one fetched while this one runs: medium degrees
+	// span 33..cta_max_degree, and a fixed assignment left CTAs with the
+	// heavy chunks finishing long after the rest.
 	if (!flat_medium) {
-		const uint32_t chunk = max(1u, min(32u, nM / gridDim.x));
+		__shared__ uint32_t s_next;
+		const uint32_t chunk = max(1u, min(32u, nM / (gridDim.x * 8)));
 		const uint32_t nchunks = (nM + chunk - 1) / chunk;
-		for (uint32_t ci = blockIdx.x; ci < nchunks; ci += gridDim.x) {
+		if (threadIdx.x == 0) s_next = atomicAdd(&out->work, 1u);
+		__syncthreads();
+		uint32_t pending = 0;
+		for (uint32_t ci = s_next; ci < nchunks;) {
+			if (threadIdx.x == 0) pending = atomicAdd(&out->work, 1u);
 			const uint32_t c0 = ci * chunk, cn = min(chunk, nM - c0);
 			if (wid == 0) {
 				uint32_t deg = 0, u = 0, beg = 0;
@@ -264,8 +276,13 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 				}
 				visit_and_append(has, uu, vv, nl, g, r, wq, p, acc);
 			}
-			if (threadIdx.x == 0) { acc.td_edges += total; acc.td_vertices += cn; }
+			if (threadIdx.x == 0) {
+				acc.td_edges += total;
+				acc.td_vertices += cn;
+				s_next = pending;
+			}
 			__syncthreads();
+			ci = s_next;
 		}
 	}
 	// Small out-degree: one warp expands 32 vertices together; lanes take
@@ -1010,21 +1027,24 @@ __device__ __forceinline__ void flush_step(ThreadAcc &acc, const RunCtx &r, uint
 // Sums the partials of `slot` over the grid (all threads call).
 __device__ __forceinline__ void step_totals(const RunCtx &r, uint32_t slot, uint32_t *count,
 		unsigned long long *degsum) {
-	__shared__ unsigned long long tot[2];
-	if (warp_id() == 0) {
-		unsigned long long c = 0, d = 0;
-		const unsigned long long *pc = part_at(r, slot, 0), *pd = part_at(r, slot, 1);
-		for (uint32_t i = lane_id(); i < gridDim.x; i += 32) {
-			c += __ldcg(pc + i);
-			d += __ldcg(pd + i);
-		}
-		c = warp_sum(c);
-		d = warp_sum(d);
-		if (lane_id() == 0) { tot[0] = c; tot[1] = d; }
+	// every thread loads at most a few partials (one L2 round trip), then a
+	// block reduction
+	__shared__ unsigned long long red[2][kWarps];
+	unsigned long long c = 0, d = 0;
+	const unsigned long long *pc = part_at(r, slot, 0), *pd = part_at(r, slot, 1);
+	for (uint32_t i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+		c += __ldcg(pc + i);
+		d += __ldcg(pd + i);
 	}
+	c = warp_sum(c);
+	d = warp_sum(d);
+	if (lane_id() == 0) { red[0][warp_id()] = c; red[1][warp_id()] = d; }
 	__syncthreads();
-	*count = (uint32_t) tot[0];
-	*degsum = tot[1];
+	unsigned long long tc = 0, td = 0;
+#pragma unroll
+	for (int w = 0; w < kWarps; ++w) { tc += red[0][w]; td += red[1][w]; }
+	*count = (uint32_t) tc;
+	*degsum = td;
 	__syncthreads();
 }
 
