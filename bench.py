@@ -328,9 +328,10 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
         rows_ok += int(np.array_equal(row, ref))
     single_gteps = single_edges / (sum(single_ms) / 1e3) / 1e9
     st = runs[-1][1]
-    # algorithmic bytes of a batch: every level writes its N x K-word plane, each
-    # gathered frontier row costs at least one word, the output is N bytes per source
-    alg = st["depth"] * 8 * st["words_per_vertex"] * wl.n + 8 * st["rows_gathered"] + len(sources) * wl.n
+    # algorithmic bytes of a batch: every level writes its N x K-word plane, every
+    # frontier word a pull reads is 8 B (above 128 sources the device counts one
+    # word per row read, so this is a lower bound), the output is N bytes per source
+    alg = st["depth"] * 8 * st["words_per_vertex"] * wl.n + 8 * st["words_gathered"] + len(sources) * wl.n
     peak, peak_kind = peaks()
     achieved = alg / (statistics.mean(ms) / 1e3) / 1e9
     res = {
@@ -338,7 +339,7 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
         "gteps": gteps, "ms_per_batch_mean": statistics.mean(ms), "ms_per_batch_p50": statistics.median(ms),
         "levels_ms_mean": statistics.mean(r[1]["levels_ms"] for r in runs),
         "edges_traversed_per_batch": edges, "depth": st["depth"], "push_levels": st["push_levels"],
-        "planes": st["planes"], "spills": st["spills"], "rows_gathered": st["rows_gathered"],
+        "planes": st["planes"], "spills": st["spills"], "words_gathered": st["words_gathered"],
         "level_ms": st["level_ms"], "level_frontier": st["level_frontier"], "level_push": st["level_push"],
         "level_phase_ms": st["level_phase_ms"], "setup_ms": st["setup_ms"], "output_ms": st["output_ms"],
         "grid_ctas": st["grid_ctas"], "batch_state_bytes": st["device_bytes"],

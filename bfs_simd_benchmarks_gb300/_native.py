@@ -84,7 +84,7 @@ class BatchStats(C.Structure):
         ("push_levels", C.c_uint32),
         ("status", C.c_int32),
         ("edges_traversed", C.c_uint64),
-        ("rows_gathered", C.c_uint64),
+        ("words_gathered", C.c_uint64),
         ("planes", C.c_uint32),
         ("spills", C.c_uint32),
         ("words_per_vertex", C.c_uint32),

@@ -794,7 +794,7 @@ int collect_batch_stats(bfs_graph *g, bfs_batch_stats *out) {
 	s.push_levels = c.stats.push_levels;
 	s.status = c.err;
 	s.edges_traversed = c.stats.traversed;
-	s.rows_gathered = c.stats.edges;
+	s.words_gathered = c.stats.edges;
 	s.planes = b.args.planes;
 	s.spills = c.stats.spills;
 	s.words_per_vertex = b.args.K;

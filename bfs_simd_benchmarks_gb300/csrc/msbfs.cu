@@ -248,6 +248,7 @@ __device__ __forceinline__ bool ms_gather(const MsArgs &a, const uint64_t *cur, 
 	const uint32_t K = a.K;
 	const unsigned lane = lane_id();
 	bool done = false;
+	uint32_t loads = 0;
 	for (uint32_t e0 = beg; e0 < end && !done; e0 += 32) {
 		const uint32_t e = e0 + lane;
 		const uint32_t u = e < end ? __ldg(a.in_src + e) : 0u;
@@ -257,7 +258,6 @@ __device__ __forceinline__ bool ms_gather(const MsArgs &a, const uint64_t *cur, 
 			const bool need0 = ((acc0 | vis0) & fm.f0) != fm.f0;
 			const bool need1 = ((acc1 | vis1) & fm.f1) != fm.f1;
 			uint64_t g0[kMsGather], g1[kMsGather];
-			int cnt = 0;
 #pragma unroll
 			for (int t = 0; t < kMsGather; ++t) {
 				uint32_t ut = 0;
@@ -267,7 +267,7 @@ __device__ __forceinline__ bool ms_gather(const MsArgs &a, const uint64_t *cur, 
 					lm &= lm - 1;
 					ut = __shfl_sync(kFull, u, src_lane);
 					mt = shfl64(um, src_lane);
-					++cnt;
+					++loads;  // rows (counted as one word each)
 				}
 				const uint64_t *r = cur + (size_t) ut * K;
 				g0[t] = (need0 && ((mt >> lane) & 1ull)) ? ld_cg64(r + lane) : 0ull;
@@ -275,10 +275,10 @@ __device__ __forceinline__ bool ms_gather(const MsArgs &a, const uint64_t *cur, 
 			}
 #pragma unroll
 			for (int t = 0; t < kMsGather; ++t) { acc0 |= g0[t]; acc1 |= g1[t]; }
-			if (lane == 0) gathered += cnt;
 			done = fm.complete(acc0 | vis0, acc1 | vis1);
 		}
 	}
+	if (lane_id() == 0) gathered += loads;
 	return done;
 }
 
@@ -312,9 +312,10 @@ __device__ __forceinline__ void ms_gather_edges(const MsArgs &a, const uint64_t 
 		const uint32_t e = e0 + lane;
 		const uint32_t u = e < end ? __ldg(a.in_src + e) : 0u;
 		const uint64_t m = e < end ? ld_cg64(actc + u) : 0ull;
-		const uint64_t g0 = (n0 && (m & 1ull)) ? ld_cg64(cur + (size_t) u * K) : 0ull;
-		const uint64_t g1 = (n1 && (m & 2ull)) ? ld_cg64(cur + (size_t) u * K + 1) : 0ull;
-		gathered += m != 0ull;
+		const bool l0 = n0 && (m & 1ull), l1 = n1 && (m & 2ull);
+		const uint64_t g0 = l0 ? ld_cg64(cur + (size_t) u * K) : 0ull;
+		const uint64_t g1 = l1 ? ld_cg64(cur + (size_t) u * K + 1) : 0ull;
+		gathered += (unsigned long long) l0 + l1;
 		acc0 |= warp_or64(g0);
 		acc1 |= warp_or64(g1);
 	}
@@ -350,9 +351,10 @@ __device__ __forceinline__ void ms_pull_lane(const MsArgs &a, const uint64_t *cu
 			uint64_t g0[4], g1[4];
 #pragma unroll
 			for (int t = 0; t < 4; ++t) {
-				g0[t] = (n0 && (m[t] & 1ull)) ? ld_cg64(cur + (size_t) u[t] * K) : 0ull;
-				g1[t] = (n1 && (m[t] & 2ull)) ? ld_cg64(cur + (size_t) u[t] * K + 1) : 0ull;
-				gathered += m[t] != 0ull;
+				const bool l0 = n0 && (m[t] & 1ull), l1 = n1 && (m[t] & 2ull);
+				g0[t] = l0 ? ld_cg64(cur + (size_t) u[t] * K) : 0ull;
+				g1[t] = l1 ? ld_cg64(cur + (size_t) u[t] * K + 1) : 0ull;
+				gathered += (unsigned long long) l0 + l1;
 			}
 #pragma unroll
 			for (int t = 0; t < 4; ++t) { acc0 |= g0[t]; acc1 |= g1[t]; }

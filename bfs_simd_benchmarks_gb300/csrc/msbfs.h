@@ -26,7 +26,7 @@ struct MsStats {
 	unsigned int spills;           // times the level planes filled up and were written out early
 	unsigned int base;             // level of plane 0 when the traversal ended
 	unsigned int complete;         // 1: every level ran (the output pass may go)
-	unsigned long long edges;      // in-neighbour frontier rows gathered by pull levels
+	unsigned long long edges;      // frontier words (64-bit) read by pull levels
 	unsigned long long traversed;  // sum over (source, reached vertex) of out-degree
 	unsigned long long t_levels0;  // device clock (ns) when the first level starts
 	unsigned long long t_levels1;  // ... and when the last one has ended
