@@ -256,6 +256,8 @@ _SIGNATURES = [
      [C.c_uint32, C.c_uint64, _u32p, _u32p, _u32p, _u32p, _u32p, C.c_uint32, C.c_uint32, C.c_uint32,
       C.POINTER(C.c_void_p)]),
     ("bfs_graph_free", C.c_int, [C.c_void_p]),
+    ("bfs_graph_save", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("bfs_graph_load_binary", C.c_int, [C.c_char_p, C.c_uint32, C.POINTER(C.c_void_p)]),
     ("bfs_graph_get_info", C.c_int, [C.c_void_p, C.POINTER(GraphInfo)]),
     ("bfs_graph_get_degrees", C.c_int, [C.c_void_p, _u32p]),
     ("bfs_options_default", C.c_int, [C.POINTER(Options)]),

@@ -836,6 +836,136 @@ struct bfs_batch_graph {
 	cudaGraphExec_t exec = nullptr;
 };
 
+// ---- binary graph files ------------------------------------------------------
+// A header of fixed-width fields, then every array of the device layout in a
+// fixed order, little-endian uint32.  The layout is this library's (CSR,
+// in-edge lists, packed column-major segments), not the reference's text
+// families; it reloads without parsing or rebuilding.
+namespace {
+
+constexpr uint64_t kBinMagic = 0x31304D4247534642ull;  // "BFSGBM01"
+
+struct BinHeader {
+	uint64_t magic;
+	uint32_t n, w, s, side, num_stripes;
+	uint32_t vbits, cbits, num_groups, max_group_vertices;
+	uint32_t max_degree, nbig_in, nchunks, reserved;
+	uint64_t m, packed_words;
+};
+
+constexpr size_t kBinChunk = (size_t) 64 << 20;  // words per host staging chunk
+
+int write_dev(FILE *f, const uint32_t *d, size_t count, std::vector<uint32_t> &buf) {
+	for (size_t i = 0; i < count; i += kBinChunk) {
+		const size_t c = std::min(kBinChunk, count - i);
+		buf.resize(c);
+		if (cudaMemcpy(buf.data(), d + i, c * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BFS_ECUDA;
+		if (std::fwrite(buf.data(), 4, c, f) != c) return BFS_EIO;
+	}
+	return BFS_OK;
+}
+
+int read_dev(FILE *f, bfs_graph *g, const uint32_t **out, size_t count, std::vector<uint32_t> &buf) {
+	uint32_t *d = nullptr;
+	int st = dev_alloc(g, &d, count);
+	if (st) return st;
+	for (size_t i = 0; i < count; i += kBinChunk) {
+		const size_t c = std::min(kBinChunk, count - i);
+		buf.resize(c);
+		if (std::fread(buf.data(), 4, c, f) != c) return BFS_EFORMAT;
+		if (cudaMemcpy(d + i, buf.data(), c * 4, cudaMemcpyHostToDevice) != cudaSuccess) return BFS_ECUDA;
+	}
+	*out = d;
+	return BFS_OK;
+}
+
+int save_binary(const bfs_graph *g, FILE *f) {
+	const DevGraph &d = g->dg;
+	BinHeader h{};
+	h.magic = kBinMagic;
+	h.n = g->n;
+	h.w = g->w;
+	h.s = g->s;
+	h.side = g->side;
+	h.num_stripes = g->num_stripes;
+	h.vbits = d.vbits;
+	h.cbits = d.cbits;
+	h.num_groups = d.num_groups;
+	h.max_group_vertices = d.max_group_words * 32;
+	h.max_degree = g->max_degree;
+	h.nbig_in = g->ms_nbig_in;
+	h.nchunks = g->ms_nchunks;
+	h.m = g->m;
+	h.packed_words = g->packed_words;
+	if (std::fwrite(&h, sizeof h, 1, f) != 1) return BFS_EIO;
+	if (std::fwrite(g->degrees.data(), 4, g->n, f) != g->n) return BFS_EIO;
+	std::vector<uint32_t> buf;
+	const size_t nseg = (size_t) g->num_stripes * d.num_groups;
+	int st;
+	if ((st = write_dev(f, d.row_off, (size_t) g->n + 1, buf)) || (st = write_dev(f, d.col, g->m, buf)) ||
+			(st = write_dev(f, d.in_off, (size_t) g->n + 1, buf)) || (st = write_dev(f, d.in_src, g->m, buf)) ||
+			(st = write_dev(f, d.packed, g->packed_words, buf)) || (st = write_dev(f, d.seg_off, nseg + 1, buf)) ||
+			(st = write_dev(f, d.group_col, (size_t) d.num_groups + 1, buf)) ||
+			(st = write_dev(f, d.hasin, ((size_t) g->n + 31) / 32, buf)) ||
+			(st = write_dev(f, g->ms_in_big, g->ms_nbig_in, buf)) || (st = write_dev(f, g->ms_chunk_v, g->ms_nchunks, buf)) ||
+			(st = write_dev(f, g->ms_chunk_beg, g->ms_nchunks, buf)))
+		return st;
+	return BFS_OK;
+}
+
+int load_binary(bfs_graph *g, FILE *f, uint32_t flags) {
+	BinHeader h{};
+	if (std::fread(&h, sizeof h, 1, f) != 1 || h.magic != kBinMagic) return BFS_EFORMAT;
+	if (h.n == 0 || h.w == 0 || h.s == 0 || h.side != side_length_of(h.n, h.w) ||
+			h.num_stripes != (h.side + h.s - 1) / h.s || h.m > 0xFFFFFFFFull || h.num_groups == 0 ||
+			h.num_groups > h.side || h.vbits > 31 || h.cbits > 16)
+		return BFS_EFORMAT;
+	g->n = h.n;
+	g->m = h.m;
+	g->w = h.w;
+	g->s = h.s;
+	g->side = h.side;
+	g->num_stripes = h.num_stripes;
+	g->max_degree = h.max_degree;
+	g->host_only = flags & BFS_LOAD_HOST_ONLY;
+	default_options(&g->opt);
+	g->degrees.resize(h.n);
+	if (std::fread(g->degrees.data(), 4, h.n, f) != h.n) return BFS_EFORMAT;
+	uint64_t sum = 0;
+	for (uint32_t x : g->degrees) sum += x;
+	if (sum != h.m) return BFS_EFORMAT;
+	if (g->host_only) return BFS_OK;
+	int st = device_setup(g);
+	if (st) return st;
+	PackedTiles pk;
+	pk.vbits = h.vbits;
+	pk.cbits = h.cbits;
+	pk.num_groups = h.num_groups;
+	pk.max_group_vertices = h.max_group_vertices;
+	DevGraph &d = g->dg;
+	std::vector<uint32_t> buf;
+	const size_t nseg = (size_t) h.num_stripes * h.num_groups;
+	const uint32_t *in_big = nullptr, *chunk_v = nullptr, *chunk_beg = nullptr;
+	if ((st = read_dev(f, g, &d.row_off, (size_t) h.n + 1, buf)) || (st = read_dev(f, g, &d.col, h.m, buf)) ||
+			(st = read_dev(f, g, &d.in_off, (size_t) h.n + 1, buf)) || (st = read_dev(f, g, &d.in_src, h.m, buf)) ||
+			(st = read_dev(f, g, &d.packed, h.packed_words, buf)) || (st = read_dev(f, g, &d.seg_off, nseg + 1, buf)) ||
+			(st = read_dev(f, g, &d.group_col, (size_t) h.num_groups + 1, buf)) ||
+			(st = read_dev(f, g, &d.hasin, ((size_t) h.n + 31) / 32, buf)) ||
+			(st = read_dev(f, g, &in_big, h.nbig_in, buf)) || (st = read_dev(f, g, &chunk_v, h.nchunks, buf)) ||
+			(st = read_dev(f, g, &chunk_beg, h.nchunks, buf)))
+		return st;
+	if (std::fgetc(f) != EOF) return BFS_EFORMAT;  // trailing bytes: not a file this version wrote
+	g->ms_in_big = in_big;
+	g->ms_chunk_v = chunk_v;
+	g->ms_chunk_beg = chunk_beg;
+	g->ms_nbig_in = h.nbig_in;
+	g->ms_nchunks = h.nchunks;
+	set_shape(g, pk, h.packed_words);
+	return alloc_run(g);
+}
+
+} // namespace
+
 // ---- hooks of the serving loop (server.cpp) ---------------------------------
 namespace bfsg {
 
@@ -968,6 +1098,34 @@ int bfs_graph_from_arrays(uint32_t num_vertices, uint64_t num_edges, const uint3
 	if (tile_offsets) h.tile_offsets.assign(tile_offsets, tile_offsets + (uint64_t) h.side * h.side);
 	if ((st = validate_colmajor(h))) return st;
 	return finish_graph(h, flags, out);
+}
+
+int bfs_graph_save(const bfs_graph *g, const char *path) {
+	if (!g || !path) return BFS_EARG;
+	if (g->host_only) return BFS_EUNSUPPORTED;
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	FILE *f = std::fopen(path, "wb");
+	if (!f) return BFS_EIO;
+	const int st = save_binary(g, f);
+	const bool closed = std::fclose(f) == 0;
+	return st ? st : (closed ? BFS_OK : BFS_EIO);
+}
+
+int bfs_graph_load_binary(const char *path, uint32_t flags, bfs_graph **out) {
+	if (!path || !out) return BFS_EARG;
+	*out = nullptr;
+	FILE *f = std::fopen(path, "rb");
+	if (!f) return BFS_EIO;
+	bfs_graph *g = new bfs_graph();
+	const int st = load_binary(g, f, flags);
+	std::fclose(f);
+	if (st) {
+		release(g);
+		delete g;
+		return st;
+	}
+	*out = g;
+	return BFS_OK;
 }
 
 int bfs_graph_free(bfs_graph *g) {

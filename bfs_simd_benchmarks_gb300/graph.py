@@ -71,6 +71,17 @@ class Graph:
             flags, C.byref(h)), "bfs_graph_from_arrays")
         return cls(h)
 
+    @classmethod
+    def load_binary(cls, path: str, host_only: bool = False) -> "Graph":
+        """A graph written by Graph.save (bfs_graph_load_binary)."""
+        h = C.c_void_p()
+        N.check(N.load().bfs_graph_load_binary(path.encode(), N.BFS_LOAD_HOST_ONLY if host_only else 0, C.byref(h)),
+                f"bfs_graph_load_binary({path})")
+        return cls(h)
+
+    def save(self, path: str) -> None:
+        N.check(N.load().bfs_graph_save(self._h, path.encode()), f"bfs_graph_save({path})")
+
     # ---- lifetime -----------------------------------------------------
     def close(self) -> None:
         if self._h:

@@ -92,6 +92,15 @@ int bfs_graph_from_arrays(uint32_t num_vertices, uint64_t num_edges, const uint3
 
 int bfs_graph_free(bfs_graph *g);
 
+/* Binary graph files (no counterpart in the reference, whose only format is
+ * text): bfs_graph_save writes the graph's device layout (CSR, in-edge lists,
+ * packed column-major segments) with a versioned header; bfs_graph_load_binary
+ * reads it back onto the current device without parsing or rebuilding
+ * (BFS_LOAD_HOST_ONLY: header and degrees only).  A file from another version
+ * or a truncated one gives BFS_EFORMAT. */
+int bfs_graph_save(const bfs_graph *g, const char *path);
+int bfs_graph_load_binary(const char *path, uint32_t flags, bfs_graph **out);
+
 typedef struct bfs_graph_info {
 	uint32_t num_vertices;     /* NNODES */
 	uint32_t tile_width;       /* TILE_WIDTH */

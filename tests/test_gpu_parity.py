@@ -254,3 +254,33 @@ def test_device_build_rejects_bad_ids(native):
     with pytest.raises(B.BfsError) as ei:
         B.Graph.from_edges(10, np.array([1, 2], np.uint32), np.array([3, 10], np.uint32), 4, 2, device_build=True)
     assert ei.value.status == 2
+
+
+def test_binary_save_load_roundtrip(native, oracle, tmp_path):
+    """bfs_graph_save / bfs_graph_load_binary: the same layout and the
+    reference's levels after a reload; truncated files are refused."""
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 13
+    src, dst = B.gen_rmat(n, 16 * n, seed=808, permute=True)
+    arr = oracle.arrays_from_edges(n, src, dst, 512, 8)
+    path = str(tmp_path / "g.bin")
+    with B.Graph.from_edges(n, src, dst, 512, 8, device_build=True) as g:
+        g.save(path)
+        info = g.info()
+    with B.Graph.load_binary(path) as g2:
+        i2 = g2.info()
+        for k in ("num_vertices", "num_edges", "num_groups", "packed_words", "max_out_degree", "tile_width",
+                  "stripe_length"):
+            assert info[k] == i2[k], k
+        np.testing.assert_array_equal(g2.degrees(), arr["degrees"])
+        for bu in ("pull", "stream"):
+            g2.set_options(bottom_up=bu)
+            for sv in B.pick_sources(arr["degrees"], 4, seed=8):
+                _check_run(B, oracle, arr, g2, sv)
+    with B.Graph.load_binary(path, host_only=True) as g3:
+        np.testing.assert_array_equal(g3.degrees(), arr["degrees"])
+    data = open(path, "rb").read()
+    open(path, "wb").write(data[: len(data) - 100])
+    with pytest.raises(B.BfsError) as ei:
+        B.Graph.load_binary(path)
+    assert ei.value.status == 2

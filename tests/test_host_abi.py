@@ -301,3 +301,20 @@ def test_autotune_argument_errors(native):
     with pytest.raises(B.BfsError) as ei:
         B.autotune(3, src, dst, [0], single=False)   # nothing to tune
     assert ei.value.status == 4
+
+
+def test_binary_load_errors(native, tmp_path):
+    """bfs_graph_load_binary refuses missing, foreign and empty files before any device work."""
+    import bfs_simd_benchmarks_gb300 as B
+    with pytest.raises(B.BfsError) as ei:
+        B.Graph.load_binary(str(tmp_path / "missing.bin"))
+    assert ei.value.status == 1
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(b"not a graph file at all" * 8)
+    with pytest.raises(B.BfsError) as ei:
+        B.Graph.load_binary(str(bad))
+    assert ei.value.status == 2
+    (tmp_path / "empty.bin").write_bytes(b"")
+    with pytest.raises(B.BfsError) as ei:
+        B.Graph.load_binary(str(tmp_path / "empty.bin"), host_only=True)
+    assert ei.value.status == 2
