@@ -26,6 +26,7 @@ BFS_LOAD_WEIGHTED = 0x1
 BFS_LOAD_PREFER_REORDER = 0x2
 BFS_LOAD_HOST_ONLY = 0x4
 BFS_LOAD_DEVICE_BUILD = 0x8
+BFS_TOOL_DEVICE = 0x10
 
 BFS_MODE_PERSISTENT = 0
 BFS_MODE_STEPWISE = 1
@@ -257,6 +258,7 @@ _SIGNATURES = [
       C.POINTER(C.c_void_p)]),
     ("bfs_graph_free", C.c_int, [C.c_void_p]),
     ("bfs_graph_save", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("bfs_graph_bfs_order", C.c_int, [C.c_void_p, C.c_uint32, _u32p]),
     ("bfs_graph_load_binary", C.c_int, [C.c_char_p, C.c_uint32, C.POINTER(C.c_void_p)]),
     ("bfs_graph_get_info", C.c_int, [C.c_void_p, C.POINTER(GraphInfo)]),
     ("bfs_graph_get_degrees", C.c_int, [C.c_void_p, _u32p]),

@@ -1100,6 +1100,25 @@ int bfs_graph_from_arrays(uint32_t num_vertices, uint64_t num_edges, const uint3
 	return finish_graph(h, flags, out);
 }
 
+int bfs_graph_bfs_order(bfs_graph *g, uint32_t source, uint32_t *vertex_map) {
+	if (!g || !vertex_map) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	int st = run_impl(g, source, g->level_buf, g->parent_buf, 0);
+	if (st) return st;
+	if ((st = collect_stats(g, nullptr))) return st;
+	std::vector<int32_t> lev(g->n);
+	if (cudaMemcpy(lev.data(), g->level_buf, sizeof(int32_t) * g->n, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return BFS_ECUDA;
+	// labels by (level, old id); unreached vertices last, by old id
+	int32_t maxl = -1;
+	for (int32_t l : lev) maxl = std::max(maxl, l);
+	std::vector<uint32_t> off((size_t) maxl + 3, 0);
+	for (int32_t l : lev) off[(l < 0 ? maxl + 1 : l) + 1]++;
+	for (size_t i = 1; i < off.size(); ++i) off[i] += off[i - 1];
+	for (uint32_t v = 0; v < g->n; ++v) vertex_map[v] = off[lev[v] < 0 ? maxl + 1 : lev[v]]++;
+	return BFS_OK;
+}
+
 int bfs_graph_save(const bfs_graph *g, const char *path) {
 	if (!g || !path) return BFS_EARG;
 	if (g->host_only) return BFS_EUNSUPPORTED;

@@ -337,7 +337,6 @@ int bfs_tool_column_major(const char *data, uint32_t w, uint32_t min_s, uint32_t
 // the CSR-ordered edges relabelled as <data>_reorder (make_up_data :42-64).
 int bfs_tool_vertex_remap(const char *data, uint32_t flags) {
 	if (!data) return BFS_EARG;
-	(void) flags;
 	std::string prefix = std::string(data) + "_untiled";
 	uint32_t n;
 	uint64_t m;
@@ -350,24 +349,33 @@ int bfs_tool_vertex_remap(const char *data, uint32_t flags) {
 	for (uint32_t v = 0; v < n; ++v) start[v + 1] = start[v] + deg[v];
 	if (start[n] != m) return BFS_EFORMAT;
 	std::vector<uint32_t> map(n, kUnvisited), frontier, next;
-	std::vector<uint8_t> seen(n, 0);
-	uint32_t top = 0;
-	if (n) {
-		map[0] = top++;
-		seen[0] = 1;
-		frontier.push_back(0);
+	if (flags & BFS_TOOL_DEVICE) {
+		// the BFS on the GPU, the labels from its levels (same map)
+		bfs_graph *g = nullptr;
+		if ((st = bfs_graph_from_edges(n, m, s.data(), d.data(), 1024, 16, BFS_LOAD_DEVICE_BUILD, &g))) return st;
+		st = bfs_graph_bfs_order(g, 0, map.data());
+		bfs_graph_free(g);
+		if (st) return st;
+	} else {
+		std::vector<uint8_t> seen(n, 0);
+		uint32_t top = 0;
+		if (n) {
+			map[0] = top++;
+			seen[0] = 1;
+			frontier.push_back(0);
+		}
+		while (!frontier.empty()) {
+			next.clear();
+			for (uint32_t u : frontier)
+				for (uint64_t e = start[u]; e < start[u + 1]; ++e)
+					if (!seen[d[e]]) { seen[d[e]] = 1; next.push_back(d[e]); }
+			std::sort(next.begin(), next.end());
+			for (uint32_t v : next) map[v] = top++;
+			frontier.swap(next);
+		}
+		for (uint32_t v = 0; v < n; ++v)
+			if (map[v] == kUnvisited) map[v] = top++;
 	}
-	while (!frontier.empty()) {
-		next.clear();
-		for (uint32_t u : frontier)
-			for (uint64_t e = start[u]; e < start[u + 1]; ++e)
-				if (!seen[d[e]]) { seen[d[e]] = 1; next.push_back(d[e]); }
-		std::sort(next.begin(), next.end());
-		for (uint32_t v : next) map[v] = top++;
-		frontier.swap(next);
-	}
-	for (uint32_t v = 0; v < n; ++v)
-		if (map[v] == kUnvisited) map[v] = top++;
 	std::string out = std::string(data) + "_reorder";
 	FILE *f = std::fopen(out.c_str(), "wb");
 	if (!f) return BFS_EIO;

@@ -151,6 +151,12 @@ class Graph:
                 f"bfs_run(source={source})")
         return lev, par, st.as_dict()
 
+    def bfs_order(self, source: int = 0) -> np.ndarray:
+        """tools/vertex_id_remap's relabelling from a GPU traversal: map[old] = new."""
+        out = np.empty(self.num_vertices, dtype=np.uint32)
+        N.check(N.load().bfs_graph_bfs_order(self._h, int(source), _ptr(out, C.c_uint32)), "bfs_graph_bfs_order")
+        return out
+
     def run_device(self, source: int, levels_ptr: int, parents_ptr: int = 0, stream: int = 0) -> None:
         """Enqueues a traversal writing caller-owned device buffers on `stream`."""
         N.check(N.load().bfs_run_device(self._h, int(source), C.c_void_p(levels_ptr),
@@ -342,8 +348,9 @@ def tool_column_major(data: str, w: int, min_s: int, max_s: int) -> None:
     N.check(N.load().bfs_tool_column_major(data.encode(), w, min_s, max_s, 0), f"column_major_tile {data}")
 
 
-def tool_vertex_remap(data: str) -> None:
-    N.check(N.load().bfs_tool_vertex_remap(data.encode(), 0), f"vertex_id_remap {data}")
+def tool_vertex_remap(data: str, device: bool = False) -> None:
+    N.check(N.load().bfs_tool_vertex_remap(data.encode(), N.BFS_TOOL_DEVICE if device else 0),
+            f"vertex_id_remap {data}")
 
 
 def write_level_dump(directory: str, levels) -> None:

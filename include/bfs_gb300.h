@@ -422,8 +422,15 @@ int bfs_tool_coo_tiling(const char *data, uint32_t min_w, uint32_t max_w, uint32
 int bfs_tool_column_major(const char *data, uint32_t w, uint32_t min_s, uint32_t max_s,
 		uint32_t flags);
 /* tools/vertex_id_remap/bfs.cpp main: <data>_untiled-* -> <data>_reorder
- * (BFS-discovery relabelling from vertex 0). */
+ * (BFS-discovery relabelling from vertex 0).  flags BFS_TOOL_DEVICE: the BFS
+ * runs on the GPU (bfs_graph_bfs_order); the files are the same. */
+#define BFS_TOOL_DEVICE 0x10u
 int bfs_tool_vertex_remap(const char *data, uint32_t flags);
+
+/* The relabelling of tools/vertex_id_remap (bfs.cpp:465-491) from a GPU
+ * traversal: vertex_map[old] = new, by BFS level from `source` and ascending
+ * old id within a level, unreached vertices last in ascending old id. */
+int bfs_graph_bfs_order(bfs_graph *g, uint32_t source, uint32_t *vertex_map);
 
 /* ---- synthetic inputs (no counterpart in the reference) ------------------ */
 #define BFS_RMAT_NO_SELF_LOOPS 0x1u

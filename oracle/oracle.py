@@ -174,6 +174,14 @@ def tool_column_major(base: str, w: int, s_len: int) -> None:
     _ok(lib().orc_tool_column_major(base.encode(), w, s_len), "column_major")
 
 
+def vertex_remap_map(arr: dict) -> np.ndarray:
+    """tools/vertex_id_remap's map (BFS from vertex 0), map[old] = new."""
+    out = np.empty(arr["n"], dtype=np.uint32)
+    _ok(lib().orc_vertex_remap_map(arr["n"], _p(arr["row_start"]), _p(arr["degrees"]), _p(arr["csr_dst"]), _p(out)),
+        "vertex_remap_map")
+    return out
+
+
 def tool_vertex_remap(base: str) -> None:
     _ok(lib().orc_tool_vertex_remap(base.encode()), "vertex_remap")
 

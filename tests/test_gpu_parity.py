@@ -284,3 +284,22 @@ def test_binary_save_load_roundtrip(native, oracle, tmp_path):
     with pytest.raises(B.BfsError) as ei:
         B.Graph.load_binary(path)
     assert ei.value.status == 2
+
+
+@pytest.mark.parametrize("name", ["rmat12p_w100_s5", "tiny_dups_w8_s2", "chain300_w32_s4", "sparse15_w16_s2"])
+def test_bfs_order_matches_vertex_id_remap(native, oracle, name, tmp_path):
+    """bfs_graph_bfs_order (GPU levels) gives tools/vertex_id_remap's map, and the
+    tool with BFS_TOOL_DEVICE writes the same _reorder file as the host tool."""
+    import shutil
+    import bfs_simd_benchmarks_gb300 as B
+    c = load_case(name)
+    arr = oracle.arrays_from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"])
+    with B.Graph.from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"]) as g:
+        np.testing.assert_array_equal(g.bfs_order(0), oracle.vertex_remap_map(arr))
+    base = str(tmp_path / "out.x")
+    B.write_edge_list(base, c["n"], c["src"], c["dst"])
+    B.tool_csr_tiling(base)
+    B.tool_vertex_remap(base)
+    host = open(base + "_reorder", "rb").read()
+    B.tool_vertex_remap(base, device=True)
+    assert open(base + "_reorder", "rb").read() == host
