@@ -45,6 +45,7 @@ constexpr uint32_t kMsBig = 1024;       // push: higher-degree vertices are spre
 constexpr int kMsGather = 4;            // pull: frontier rows gathered per round
 constexpr uint32_t kLaneMaxWords = 2;   // pull: up to this many words per vertex ...
 constexpr uint32_t kLaneMaxDeg = 32;    // ... destinations of at most this in-degree go one per lane
+constexpr uint32_t kGroupMaxWords = 16; // pull: up to this many words, in-neighbour rows in lane groups
 constexpr uint32_t kEmitV = 128;        // output tile: 128 vertices x 4 words (256 sources)
 constexpr uint32_t kEmitW = 4;
 constexpr uint32_t kEmitStride = 132;   // shared row stride in bytes (33 words: column writes spread over banks)
@@ -298,6 +299,51 @@ __device__ __forceinline__ uint64_t warp_or64(uint64_t x) {
 	return x;
 }
 
+// ms_gather for 2 < K <= 16 words per vertex: the warp is split into
+// 32 / kp groups of kp lanes (kp = K rounded up to a power of two); a group
+// reads one in-neighbour row (lane k its word k), so a round reads
+// kMsGather * 32 / kp rows; the groups' words are OR-ed together after every
+// round for the early exit.  `vis` and `f` are the lane's word k (the same in
+// every group); acc comes back in every group.
+__device__ __forceinline__ void ms_gather_grouped(const MsArgs &a, const uint64_t *cur, const uint64_t *actc,
+		uint32_t beg, uint32_t end, uint32_t kp, uint64_t f, uint64_t vis, uint64_t &acc, unsigned long long &gathered) {
+	const uint32_t K = a.K;
+	const unsigned lane = lane_id();
+	const uint32_t k = lane & (kp - 1), grp = lane / kp, ngrp = 32 / kp;
+	const bool wk = k < K;
+	uint32_t loads = 0;
+	bool done = __all_sync(kFull, ((vis | acc) & f) == f);
+	for (uint32_t e0 = beg; e0 < end && !done; e0 += 32) {
+		const uint32_t e = e0 + lane;
+		const uint32_t u = e < end ? __ldg(a.in_src + e) : 0u;
+		const uint64_t um = e < end ? ld_cg64(actc + u) : 0ull;
+		uint32_t lm = __ballot_sync(kFull, um != 0ull);
+		while (lm && !done) {
+			const bool need = ((vis | acc) & f) != f;
+			const uint32_t nlive = __popc(lm);
+			uint64_t gv[kMsGather];
+#pragma unroll
+			for (int t = 0; t < kMsGather; ++t) {
+				const uint32_t idx = t * ngrp + grp;
+				const int src = idx < nlive ? (int) __fns(lm, 0, idx + 1) : 0;
+				const uint32_t ut = __shfl_sync(kFull, u, src);
+				const uint64_t mt = shfl64(um, src);
+				const bool ld = idx < nlive && need && wk && ((mt >> k) & 1ull);
+				gv[t] = ld ? ld_cg64(cur + (size_t) ut * K + k) : 0ull;
+				loads += ld;
+			}
+#pragma unroll
+			for (int t = 0; t < kMsGather; ++t) acc |= gv[t];
+			for (uint32_t d = kp; d < 32; d <<= 1) acc |= shfl_xor64(acc, d);
+			const uint32_t took = min(nlive, (uint32_t) kMsGather * ngrp);
+			if (took == nlive) lm = 0;
+			else lm &= ~((1u << __fns(lm, 0, took + 1)) - 1u);
+			done = __all_sync(kFull, ((vis | acc) & f) == f);
+		}
+	}
+	gathered += loads;
+}
+
 // ms_gather for K <= 2 words per vertex: lanes take in-edges (32 per step)
 // instead of words, read the neighbour's needed non-zero words and OR them
 // across the warp.  Inputs and outputs are word 0 / word 1 in every lane.
@@ -437,6 +483,12 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, cons
 				ms_gather_edges(a, cur, actc, beg, end, shfl64(fm.f0, 0), shfl64(fm.f0, 1), shfl64(vis0, 0),
 						shfl64(vis0, 1), a0, a1, gathered);
 				acc0 = lane == 0 ? a0 : (lane == 1 ? a1 : 0ull);
+			} else if (K <= kGroupMaxWords) {
+				const uint32_t kp = K <= 4 ? 4 : (K <= 8 ? 8 : 16);
+				const uint32_t kw = lane & (kp - 1);
+				uint64_t ag = 0;
+				ms_gather_grouped(a, cur, actc, beg, end, kp, shfl64(fm.f0, kw), shfl64(vis0, kw), ag, gathered);
+				acc0 = lane < kp ? ag : 0ull;
 			} else if (!fm.complete(vis0, vis1)) {
 				ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
 			}
@@ -487,6 +539,12 @@ __device__ void ms_pull_chunks(const MsArgs &a, const uint64_t *cur, const uint6
 			ms_gather_edges(a, cur, actc, beg, end, shfl64(fm.f0, 0), shfl64(fm.f0, 1), shfl64(vis0, 0), shfl64(vis0, 1),
 					a0, a1, gathered);
 			acc0 = lane == 0 ? a0 : (lane == 1 ? a1 : 0ull);
+		} else if (K <= kGroupMaxWords) {
+			const uint32_t kp = K <= 4 ? 4 : (K <= 8 ? 8 : 16);
+			const uint32_t kw = lane & (kp - 1);
+			uint64_t ag = 0;
+			ms_gather_grouped(a, cur, actc, beg, end, kp, shfl64(fm.f0, kw), shfl64(vis0, kw), ag, gathered);
+			acc0 = lane < kp ? ag : 0ull;
 		} else {
 			ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
 		}
