@@ -329,7 +329,7 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
     single_gteps = single_edges / (sum(single_ms) / 1e3) / 1e9
     st = runs[-1][1]
     # algorithmic bytes of a batch: every level writes its N x K-word plane, every
-    # frontier word a pull reads is 8 B (above 1024 sources the device counts one
+    # frontier word a pull reads is 8 B (above 512 sources the device counts one
     # word per row read, so this is a lower bound), the output is N bytes per source
     alg = st["depth"] * 8 * st["words_per_vertex"] * wl.n + 8 * st["words_gathered"] + len(sources) * wl.n
     peak, peak_kind = peaks()

@@ -45,7 +45,7 @@ constexpr uint32_t kMsBig = 1024;       // push: higher-degree vertices are spre
 constexpr int kMsGather = 4;            // pull: frontier rows gathered per round
 constexpr uint32_t kLaneMaxWords = 2;   // pull: up to this many words per vertex ...
 constexpr uint32_t kLaneMaxDeg = 32;    // ... destinations of at most this in-degree go one per lane
-constexpr uint32_t kGroupMaxWords = 16; // pull: up to this many words, in-neighbour rows in lane groups
+constexpr uint32_t kGroupMaxWords = 8;  // pull: up to this many words, in-neighbour rows in lane groups
 constexpr uint32_t kEmitV = 128;        // output tile: 128 vertices x 4 words (256 sources)
 constexpr uint32_t kEmitW = 4;
 constexpr uint32_t kEmitStride = 132;   // shared row stride in bytes (33 words: column writes spread over banks)
@@ -484,7 +484,7 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, cons
 						shfl64(vis0, 1), a0, a1, gathered);
 				acc0 = lane == 0 ? a0 : (lane == 1 ? a1 : 0ull);
 			} else if (K <= kGroupMaxWords) {
-				const uint32_t kp = K <= 4 ? 4 : (K <= 8 ? 8 : 16);
+				const uint32_t kp = K <= 4 ? 4 : 8;
 				const uint32_t kw = lane & (kp - 1);
 				uint64_t ag = 0;
 				ms_gather_grouped(a, cur, actc, beg, end, kp, shfl64(fm.f0, kw), shfl64(vis0, kw), ag, gathered);
@@ -540,7 +540,7 @@ __device__ void ms_pull_chunks(const MsArgs &a, const uint64_t *cur, const uint6
 					a0, a1, gathered);
 			acc0 = lane == 0 ? a0 : (lane == 1 ? a1 : 0ull);
 		} else if (K <= kGroupMaxWords) {
-			const uint32_t kp = K <= 4 ? 4 : (K <= 8 ? 8 : 16);
+			const uint32_t kp = K <= 4 ? 4 : 8;
 			const uint32_t kw = lane & (kp - 1);
 			uint64_t ag = 0;
 			ms_gather_grouped(a, cur, actc, beg, end, kp, shfl64(fm.f0, kw), shfl64(vis0, kw), ag, gathered);

@@ -213,7 +213,7 @@ typedef struct bfs_batch_stats {
 	uint32_t push_levels;      /* levels expanded top-down (the others pulled bottom-up) */
 	int32_t status;            /* BFS_OK, BFS_ETIMEOUT, or BFS_EUNSUPPORTED (a level above 254) */
 	uint64_t edges_traversed;  /* sum over the sources of the out-degrees of the vertices each reached */
-	uint64_t words_gathered;   /* frontier words read by pull levels (batches of more than 1024 sources
+	uint64_t words_gathered;   /* frontier words read by pull levels (batches of more than 512 sources
 	                              count one per in-neighbour row read: a lower bound) */
 	uint32_t planes;           /* level planes held (levels kept before an early output pass) */
 	uint32_t spills;           /* early output passes (traversal deeper than the planes) */
