@@ -368,7 +368,7 @@ int upload_device_build(bfs_graph *g, uint32_t n, uint64_t m, const uint32_t *sr
 	if (cudaMemset(col_edges, 0, (size_t) g->side * 4) != cudaSuccess ||
 			cudaMemset(hasin, 0, ((size_t) n + 31) / 32 * 4) != cudaSuccess)
 		return BFS_ECUDA;
-	if ((st = dbuild_col_hist(d_dst, m, w, col_edges, hasin, g->num_sms, cs))) return st;
+	if ((st = dbuild_col_hist(d_dst, m, w, g->side, col_edges, hasin, g->num_sms, cs))) return st;
 	std::vector<uint32_t> h_col32(g->side);
 	if (cudaMemcpy(h_col32.data(), col_edges, (size_t) g->side * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
 		return BFS_ECUDA;

@@ -124,14 +124,29 @@ __global__ void k_scatter(const uint32_t *key, const uint32_t *val, uint64_t m, 
 		out[atomicAdd(cursor + key[i], 1u)] = val[i];
 }
 
-__global__ void k_col_hist(const uint32_t *dst, uint64_t m, uint32_t w, uint32_t *col_edges, uint32_t *hasin) {
+constexpr uint32_t kColHistSmem = 12288;  // tile columns counted in shared memory
+
+// In-edges per tile column (a per-CTA shared histogram when the columns fit:
+// every edge hits one of few counters) and the has-in-edge bitmap.
+__global__ void k_col_hist(const uint32_t *dst, uint64_t m, uint32_t w, uint32_t side, uint32_t *col_edges,
+		uint32_t *hasin) {
+	__shared__ uint32_t hist[kColHistSmem];
+	const bool local = side <= kColHistSmem;
+	if (local)
+		for (uint32_t c = threadIdx.x; c < side; c += blockDim.x) hist[c] = 0;
+	__syncthreads();
 	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
 	for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
 		const uint32_t v = dst[i];
-		atomicAdd(col_edges + v / w, 1u);
+		if (local) atomicAdd(hist + v / w, 1u);
+		else atomicAdd(col_edges + v / w, 1u);
 		const uint32_t bit = 1u << (v & 31);
 		if (!(ld_cg(hasin + (v >> 5)) & bit)) atomicOr(hasin + (v >> 5), bit);
 	}
+	__syncthreads();
+	if (local)
+		for (uint32_t c = threadIdx.x; c < side; c += blockDim.x)
+			if (hist[c]) atomicAdd(col_edges + c, hist[c]);
 }
 
 __device__ __forceinline__ uint32_t seg_of(uint32_t u, uint32_t v, const DeviceBuildShape &sh, const uint32_t *group_of) {
@@ -198,9 +213,9 @@ int dbuild_scatter(const uint32_t *key, const uint32_t *val, uint64_t m, uint32_
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }
 
-int dbuild_col_hist(const uint32_t *dst, uint64_t m, uint32_t w, uint32_t *col_edges, uint32_t *hasin, int num_sms,
-		cudaStream_t st) {
-	k_col_hist<<<grid_for(m, num_sms), kBThreads, 0, st>>>(dst, m, w, col_edges, hasin);
+int dbuild_col_hist(const uint32_t *dst, uint64_t m, uint32_t w, uint32_t side, uint32_t *col_edges, uint32_t *hasin,
+		int num_sms, cudaStream_t st) {
+	k_col_hist<<<grid_for(m, num_sms), kBThreads, 0, st>>>(dst, m, w, side, col_edges, hasin);
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }
 

@@ -24,8 +24,8 @@ int dbuild_exclusive_scan(const uint32_t *in, uint32_t n, uint32_t *tmp, uint32_
 int dbuild_scatter(const uint32_t *key, const uint32_t *val, uint64_t m, uint32_t *cursor, uint32_t *out, int num_sms,
 		cudaStream_t st);
 // in-edges per tile column and the has-in-edge bitmap (both zeroed by the caller)
-int dbuild_col_hist(const uint32_t *dst, uint64_t m, uint32_t w, uint32_t *col_edges, uint32_t *hasin, int num_sms,
-		cudaStream_t st);
+int dbuild_col_hist(const uint32_t *dst, uint64_t m, uint32_t w, uint32_t side, uint32_t *col_edges, uint32_t *hasin,
+		int num_sms, cudaStream_t st);
 // edges per packed segment (group(v) * stripes + stripe(u)), zeroed by the caller
 int dbuild_seg_hist(const uint32_t *src, const uint32_t *dst, uint64_t m, const DeviceBuildShape &sh,
 		const uint32_t *group_of, uint32_t *seg_count, int num_sms, cudaStream_t st);
