@@ -274,6 +274,7 @@ _SIGNATURES = [
     ("bfs_batch_graph_create", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_void_p)]),
     ("bfs_batch_graph_launch", C.c_int, [C.c_void_p, C.c_void_p]),
     ("bfs_batch_graph_destroy", C.c_int, [C.c_void_p]),
+    ("bfs_tile_size_range", C.c_int, [C.c_uint32, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     ("bfs_tune_options", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_uint32, C.POINTER(TuneResult)]),
     ("bfs_autotune", C.c_int, [C.c_uint32, C.c_uint64, _u32p, _u32p, _u32p, C.c_uint32, _u32p, C.c_uint32, _u32p,
                                C.c_uint32, C.c_uint32, C.c_char_p, C.POINTER(TuneResult)]),

@@ -14,6 +14,7 @@
 //     the graph's size and out-degree signature.
 // Levels never depend on these choices (they are checked equal in the tests);
 // only time does.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -206,6 +207,29 @@ int tune(Tuner &t, uint32_t flags, bfs_options *best_out, double *single_out, do
 
 extern "C" {
 
+// tools/tile-size-computer/tile-size-computer.cpp:21-56, restated: the
+// smallest power-of-two width (from 64) whose SIDE^2 tile count fits 32 bits
+// and whose tiles average at least 8 edges is the minimum; the maximum is
+// a quarter of the first width, doubling from there, at which SIDE <= 64.
+int bfs_tile_size_range(uint32_t num_vertices, uint64_t num_edges, uint32_t *min_width, uint32_t *max_width) {
+	if (!min_width || !max_width || num_vertices == 0 || num_edges > 0xFFFFFFFFull) return BFS_EARG;
+	auto side = [&](uint64_t w) { return (uint64_t) num_vertices / w + (num_vertices % w ? 1 : 0); };
+	auto tiles = [&](uint64_t w) { const uint64_t sl = side(w); return sl * sl; };
+	uint64_t w = 64;
+	while (tiles(w) > 4294967295ull) w *= 2;
+	while ((uint32_t) (num_edges / tiles(w)) < 8) {
+		if (w > (1ull << 40)) return BFS_EARG;  // too few edges for any width (the tool would not stop)
+		w *= 2;
+	}
+	const uint64_t lo = w;
+	while (side(w) > 64) w *= 2;
+	w = std::max<uint64_t>(1, w / 2);
+	if (w > 0xFFFFFFFFull || lo > 0xFFFFFFFFull) return BFS_EARG;
+	*min_width = (uint32_t) lo;
+	*max_width = (uint32_t) w;
+	return BFS_OK;
+}
+
 int bfs_tune_options(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, uint32_t flags,
 		bfs_tune_result *result) {
 	if (!g || !sources || !num_sources || !result || !(flags & (BFS_TUNE_SINGLE | BFS_TUNE_BATCH))) return BFS_EARG;
@@ -227,10 +251,21 @@ int bfs_autotune(uint32_t num_vertices, uint64_t num_edges, const uint32_t *src,
 		const uint32_t *sources, uint32_t num_sources, const uint32_t *tile_widths, uint32_t num_widths,
 		const uint32_t *stripe_lengths, uint32_t num_stripes, uint32_t flags, const char *cache_path,
 		bfs_tune_result *result) {
-	if (!result || !sources || !num_sources || !tile_widths || !num_widths || !stripe_lengths || !num_stripes ||
-			(num_edges && (!src || !dst)) || !(flags & (BFS_TUNE_SINGLE | BFS_TUNE_BATCH)))
+	if (!result || !sources || !num_sources || !stripe_lengths || !num_stripes || (num_edges && (!src || !dst)) ||
+			!(flags & (BFS_TUNE_SINGLE | BFS_TUNE_BATCH)) || (num_widths && !tile_widths))
 		return BFS_EARG;
 	std::memset(result, 0, sizeof(*result));
+	std::vector<uint32_t> widths(tile_widths, tile_widths + num_widths);
+	if (widths.empty()) {
+		// the tile-size computer's range (powers of two), within what the packing holds
+		uint32_t lo = 0, hi = 0;
+		int st = bfs_tile_size_range(num_vertices, num_edges, &lo, &hi);
+		if (st) return st;
+		for (uint64_t w = lo; w <= std::max(lo, hi) && w <= 8192; w *= 2) widths.push_back((uint32_t) w);
+		if (widths.empty()) widths.push_back(std::min<uint32_t>(lo, 8192));
+	}
+	tile_widths = widths.data();
+	num_widths = (uint32_t) widths.size();
 	for (uint32_t i = 0; i < num_sources; ++i)
 		if (sources[i] >= num_vertices) return BFS_EARG;
 	// signature: N, E, out-degrees, flags and the shapes searched

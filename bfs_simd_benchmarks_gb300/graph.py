@@ -320,11 +320,19 @@ class Server:
             pass
 
 
+def tile_size_range(num_vertices: int, num_edges: int) -> tuple[int, int]:
+    """tools/tile-size-computer's (min_tile_size, max_tile_size)."""
+    lo, hi = C.c_uint32(), C.c_uint32()
+    N.check(N.load().bfs_tile_size_range(num_vertices, num_edges, C.byref(lo), C.byref(hi)), "bfs_tile_size_range")
+    return lo.value, hi.value
+
+
 def autotune(num_vertices: int, src, dst, sources, tile_widths=(512, 1024, 2048, 4096), stripe_lengths=(8, 16, 32),
              single: bool = True, batch: bool = False, cache_path: str | None = None) -> dict:
-    """bfs_autotune: the best tile shape and options of an edge list, by measurement."""
+    """bfs_autotune: the best tile shape and options of an edge list, by measurement.
+    tile_widths=None: the powers of two in tile_size_range(N, E)."""
     s, d, so = _u32(src), _u32(dst), _u32(sources)
-    w, sl = _u32(tile_widths), _u32(stripe_lengths)
+    w, sl = _u32(tile_widths if tile_widths is not None else []), _u32(stripe_lengths)
     r = N.TuneResult()
     flags = (N.BFS_TUNE_SINGLE if single else 0) | (N.BFS_TUNE_BATCH if batch else 0)
     N.check(N.load().bfs_autotune(num_vertices, s.size, _ptr(s, C.c_uint32), _ptr(d, C.c_uint32),

@@ -294,6 +294,12 @@ typedef struct bfs_tune_result {
 	bfs_tune_trial trials[BFS_TUNE_MAX_TRIALS];
 } bfs_tune_result;
 
+/* tools/tile-size-computer: the range of tile widths it recommends for N
+ * vertices and E edges (its "min_tile_size: .., max_tile_size: .." line,
+ * tools/tile-size-computer/tile-size-computer.cpp:21-56).  bfs_autotune with
+ * no tile widths searches the powers of two in this range. */
+int bfs_tile_size_range(uint32_t num_vertices, uint64_t num_edges, uint32_t *min_width, uint32_t *max_width);
+
 /* Tunes the options of one resident graph on the given sources (coordinate
  * descent, every candidate timed on the device) and leaves the best set. */
 int bfs_tune_options(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, uint32_t flags,

@@ -55,3 +55,21 @@ def test_autotune_shapes_and_cache(native, oracle, tmp_path):
         for s in srcs:
             lev, _, _ = g.run(int(s))
             np.testing.assert_array_equal(lev, oracle.bfs_levels(arr, int(s)))
+
+
+def test_autotune_default_widths_from_tile_size_range(native, oracle):
+    """With no tile widths, bfs_autotune searches the powers of two of the
+    tile-size computer's range (capped at what the packing holds)."""
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 13
+    src, dst = B.gen_rmat(n, 16 * n, seed=67)
+    srcs = B.pick_sources(np.bincount(src, minlength=n), 4, seed=2)
+    lo, hi = B.tile_size_range(n, src.size)
+    r = B.autotune(n, src, dst, srcs, tile_widths=None, stripe_lengths=(16,))
+    widths = {t["tile_width"] for t in r["trials"]}
+    expect = set()
+    w = lo
+    while w <= max(lo, hi) and w <= 8192:
+        expect.add(w)
+        w *= 2
+    assert widths == expect and r["tile_width"] in expect

@@ -318,3 +318,17 @@ def test_binary_load_errors(native, tmp_path):
     with pytest.raises(B.BfsError) as ei:
         B.Graph.load_binary(str(tmp_path / "empty.bin"), host_only=True)
     assert ei.value.status == 2
+
+
+def test_tile_size_range_matches_reference_tool(native):
+    """bfs_tile_size_range against the reference's tile-size-computer outputs
+    (tests/golden/tile_size.json, made by its own binary)."""
+    import json
+    import bfs_simd_benchmarks_gb300 as B
+    with open(os.path.join(ROOT, "tests", "golden", "tile_size.json")) as f:
+        cases = json.load(f)
+    assert len(cases) >= 10
+    for c in cases:
+        assert B.tile_size_range(c["vertices"], c["edges"]) == (c["min_tile_size"], c["max_tile_size"]), c
+    with pytest.raises(B.BfsError):
+        B.tile_size_range(10, 3)   # too few edges for any width
