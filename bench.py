@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=5)
     ap.add_argument("--batch-budget-mb", type=int, default=40960, help="HBM budget of the batched level planes")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (measure with the default options)")
+    ap.add_argument("--bc-sources", type=int, default=16, help="betweenness measurement: sources (0 skips it)")
     ap.add_argument("--serve", default="c4", help="serving measurement: 'c4' (8 graphs, Poisson load) or 'none'")
     ap.add_argument("--serve-rates", default="2000,10000,50000", help="query arrival rates (queries/s)")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="arrival window per rate")
@@ -361,6 +362,93 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
     return res
 
 
+def bench_bc(args, torch, dev, g, sources, flush, arr=None):
+    """Betweenness dependencies (bfs_bc_run_device, apps/betweennessCentrality_simd
+    /bc.cpp:1717): per source one single-source traversal and one dependency
+    launch (level sort, path counts, dependency sums).  GTEPS = sum of m(s)
+    (out-degrees of reached vertices) / device time, L2 flushed before each
+    source; e2e through bfs_bc_run with float dependencies copied to the host."""
+    n = g.num_vertices
+    srcs = [int(s) for s in sources[: args.bc_sources]]
+    stream = torch.cuda.Stream(device=dev)
+    dep = torch.empty(n, dtype=torch.float32, device=dev)
+    sig = torch.empty(n, dtype=torch.int32, device=dev)
+
+    def one(s):
+        with torch.cuda.stream(stream):
+            flush.fill_(s & 0xFF)
+        g.bc_device(s, dep.data_ptr(), sig.data_ptr(), stream.cuda_stream)
+        st = g.bc_stats()
+        if st["status"] != 0:
+            raise RuntimeError(f"betweenness device status {st['status']}")
+        return st
+
+    for _ in range(max(1, args.warmup)):
+        one(srcs[0])
+    torch.cuda.synchronize()
+    sts = []
+    for _ in range(args.steps):
+        for s in srcs:
+            sts.append(one(s))
+    dev_ms = sum(st["device_ms"] for st in sts)
+    trav_ms = sum(st["traversal_ms"] for st in sts)
+    edges = sum(st["edges_reached"] for st in sts)
+    k_ms = dev_ms - trav_ms
+    read_edges = sum(st["edges_forward"] + st["edges_reverse"] for st in sts)
+    reached = sum(st["reached"] for st in sts)
+    # algorithmic bytes of the dependency launch: per edge read its neighbour id
+    # and the neighbour's level (8 B); per reached vertex its level, two offset
+    # pairs, its order slot, path count, sum and dependency (40 B); per vertex
+    # the sort's level read and the initialised outputs (12 B)
+    alg = 8 * read_edges + 40 * reached + 12 * n * len(sts)
+    peak, _ = peaks()
+    ach = alg / (k_ms / 1e3) / 1e9 if k_ms > 0 else 0.0
+    # e2e: host dependencies
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_edges = 0
+    for s in srcs:
+        d, _, st = g.bc(s, paths=False)
+        e2e_edges += st["edges_reached"]
+    e2e_s = time.perf_counter() - t0
+    out = {
+        "what": "betweenness dependencies of single sources (forward path counts + reverse float sums)",
+        "sources": len(srcs), "steps": args.steps,
+        "gteps": edges / (dev_ms / 1e3) / 1e9,
+        "ms_per_source_mean": dev_ms / len(sts),
+        "traversal_ms_mean": trav_ms / len(sts),
+        "dependency_kernel_ms_mean": k_ms / len(sts),
+        "phase_ms_mean": {k: statistics.mean(st[k] for st in sts) for k in ("sort_ms", "paths_ms", "dependencies_ms")},
+        "depth_mean": statistics.mean(st["depth"] for st in sts),
+        "roofline": {"kernel": "k_bc", "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": ach / peak if peak else None, "algorithmic_bytes_per_launch": alg / len(sts)},
+        "e2e": {"value": e2e_edges / e2e_s / 1e9, "unit": "GTEPS", "d2h_bytes_per_step": 4 * n * len(srcs),
+                "note": "bfs_bc_run(): float dependencies to host memory"},
+        "gpu_launches": 3 * len(sts),
+    }
+    if arr is not None:
+        from oracle import oracle as O
+        ok = 0
+        checked = srcs[:2]
+        cpu_s = 0.0
+        cpu_edges = 0
+        deg = arr["degrees"].astype(np.uint64)
+        for s in checked:
+            t1 = time.perf_counter()
+            osig, odep, ocost, oscale = O.bc_single(arr, s)
+            cpu_s += time.perf_counter() - t1
+            cpu_edges += int(deg[ocost >= 0].sum())
+            d, p, _ = g.bc(s)
+            ok += int(np.array_equal(p, osig) and
+                      bool((np.abs(d.astype(np.float64) - odep) <= 1e-4 * (np.abs(oscale) + 1)).all()))
+        out["parity"] = (f"{ok}/{len(checked)} sources: path counts bit-exact, dependencies within "
+                         "1e-4 x (scale + 1) of the oracle")
+        out["cpu_baseline"] = {"value": cpu_edges / cpu_s / 1e9, "unit": "GTEPS", "cores": 1, "kind": "port",
+                               "sample": f"{len(checked)} sources, oracle/bfs_oracle.c orc_bc_single (sequential, "
+                                         "includes building the reverse graph)"}
+    return out
+
+
 def bench_serving(args, torch, dev):
     """The serving loop: 8 resident R-MAT graphs (scales 14, 16, 18-23, edge
     factor 16) under a 40 GB HBM admission budget; open-loop Poisson arrivals
@@ -529,13 +617,17 @@ def main():
 
     cpu = None
     parity = None
+    cpu_arr = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu, cpu_levels, _ = cpu_baseline(wl, src, dst, sources, args.cpu_seconds)
+        cpu, cpu_levels, cpu_arr = cpu_baseline(wl, src, dst, sources, args.cpu_seconds)
         ok = 0
         for s, ref in cpu_levels.items():
             got, _, _ = g.run(s, parents=False)
             ok += int(np.array_equal(got, ref))
         parity = f"levels bit-exact on {ok}/{len(cpu_levels)} sources checked against the oracle"
+    bc = None
+    if args.bc_sources > 0 and world == 1:
+        bc = bench_bc(args, torch, dev, g, sources, flush, cpu_arr)
     if rank == 0:
         clocks = clk.summary()
         line = {
@@ -576,6 +668,7 @@ def main():
             "parity": parity,
             "batched": batched,
             "serving": serving,
+            "betweenness": bc,
         }
         print(json.dumps(line))
     if world > 1:

@@ -78,6 +78,27 @@ class Options(C.Structure):
     ]
 
 
+class BcStats(C.Structure):
+    _fields_ = [
+        ("num_sources", C.c_uint32),
+        ("depth", C.c_uint32),
+        ("reached", C.c_uint32),
+        ("status", C.c_uint32),
+        ("edges_reached", C.c_uint64),
+        ("edges_forward", C.c_uint64),
+        ("edges_reverse", C.c_uint64),
+        ("device_ms", C.c_float),
+        ("traversal_ms", C.c_float),
+        ("sort_ms", C.c_float),
+        ("paths_ms", C.c_float),
+        ("dependencies_ms", C.c_float),
+        ("grid_ctas", C.c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class BatchStats(C.Structure):
     _fields_ = [
         ("num_sources", C.c_uint32),
@@ -270,6 +291,11 @@ _SIGNATURES = [
     ("bfs_last_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     ("bfs_run_batch", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(BatchStats)]),
     ("bfs_last_batch_stats", C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
+    ("bfs_bc_run", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(BcStats)]),
+    ("bfs_bc_run_device", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("bfs_bc_last_stats", C.c_int, [C.c_void_p, C.POINTER(BcStats)]),
+    ("bfs_bc_accumulate", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_void_p, C.POINTER(BcStats)]),
+    ("bfs_bc_accumulate_device", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("bfs_run_batch_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("bfs_batch_graph_create", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_void_p)]),
     ("bfs_batch_graph_launch", C.c_int, [C.c_void_p, C.c_void_p]),

@@ -11,6 +11,7 @@
 #include "build_device.h"
 #include "internal.h"
 #include "kernels_api.h"
+#include "bc.h"
 #include "msbfs.h"
 
 using namespace bfsg;
@@ -81,6 +82,18 @@ struct bfs_graph {
 		size_t bytes = 0;
 		std::vector<DevBuf> bufs;
 	} mb;
+	// betweenness state, allocated by the first bfs_bc_* call
+	struct Bc {
+		uint32_t *sigma = nullptr, *order = nullptr, *cnt = nullptr, *kstart = nullptr;
+		float *dacc = nullptr, *delta = nullptr, *acc = nullptr;
+		BcControl *ctl = nullptr;
+		BcControl *h_ctl = nullptr;  // pinned
+		cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+		cudaStream_t stream = nullptr;   // of the last enqueued run
+		int grid = 0;
+		size_t bytes = 0;
+		std::vector<DevBuf> bufs;
+	} bc;
 	std::mutex mu;
 };
 
@@ -119,8 +132,20 @@ void release_batch(bfs_graph *g) {
 	g->mb.planes_alloc = 0;
 }
 
+void release_bc(bfs_graph *g) {
+	auto &b = g->bc;
+	for (auto &x : b.bufs) cudaFree(x.p);
+	b.bufs.clear();
+	if (b.h_ctl) cudaFreeHost(b.h_ctl);
+	if (b.e0) cudaEventDestroy(b.e0);
+	if (b.e1) cudaEventDestroy(b.e1);
+	if (b.e2) cudaEventDestroy(b.e2);
+	b = bfs_graph::Bc{};
+}
+
 void release(bfs_graph *g) {
 	release_batch(g);
+	release_bc(g);
 	if (g->mb.h_ctl) cudaFreeHost(g->mb.h_ctl);
 	if (g->mb.e0) cudaEventDestroy(g->mb.e0);
 	if (g->mb.e1) cudaEventDestroy(g->mb.e1);
@@ -827,6 +852,117 @@ int collect_batch_stats(bfs_graph *g, bfs_batch_stats *out) {
 	return s.status;
 }
 
+// ---- betweenness dependencies ----------------------------------------------
+template <class T> int bc_alloc(bfs_graph *g, T **out, size_t count) {
+	size_t bytes = std::max<size_t>(sizeof(T) * count, 16);
+	void *p = nullptr;
+	if (cudaMalloc(&p, bytes) != cudaSuccess) {
+		cudaGetLastError();
+		return BFS_ENOMEM;
+	}
+	g->bc.bufs.push_back({p, bytes});
+	g->bc.bytes += bytes;
+	*out = (T *) p;
+	return BFS_OK;
+}
+
+int bc_prepare(bfs_graph *g) {
+	auto &b = g->bc;
+	if (b.ctl) return BFS_OK;
+	int rc;
+	if ((rc = bc_alloc(g, &b.sigma, g->n)) || (rc = bc_alloc(g, &b.order, g->n)) ||
+			(rc = bc_alloc(g, &b.dacc, g->n)) || (rc = bc_alloc(g, &b.delta, g->n)) ||
+			(rc = bc_alloc(g, &b.acc, g->n)) || (rc = bc_alloc(g, &b.cnt, kBcCntCap)) ||
+			(rc = bc_alloc(g, &b.kstart, 2 * (size_t) kBcMaxLevels + 1)) || (rc = bc_alloc(g, &b.ctl, 1))) {
+		release_bc(g);
+		return rc;
+	}
+	if (cudaMallocHost(&b.h_ctl, sizeof(BcControl)) != cudaSuccess || cudaEventCreate(&b.e0) != cudaSuccess ||
+			cudaEventCreate(&b.e1) != cudaSuccess || cudaEventCreate(&b.e2) != cudaSuccess) {
+		cudaGetLastError();
+		release_bc(g);
+		return BFS_ENOMEM;
+	}
+	return BFS_OK;
+}
+
+// Enqueues a traversal from `source` (always the persistent kernel: its
+// device-side step count and status feed the dependency launch) and the
+// dependency launch.  sigma / delta: where the path counts and dependencies go
+// (the graph's own buffers when null); acc: accumulated into when non-null.
+int bc_enqueue(bfs_graph *g, uint32_t source, uint32_t *sigma, float *delta, float *acc, cudaStream_t st) {
+	auto &b = g->bc;
+	RunCtx r = g->rc;
+	r.level = g->level_buf;
+	r.parent = nullptr;
+	StepParams p{};
+	p.source = source;
+	p.warp_max_degree = g->opt.warp_max_degree;
+	p.cta_max_degree = g->opt.cta_max_degree;
+	p.bottom_up = g->opt.bottom_up;
+	p.to_dense_threshold = g->m / std::max<uint32_t>(1, g->opt.to_dense_ratio);
+	p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
+	int rc;
+	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
+	if ((rc = launch_init(g->dg, r, st, g->num_sms))) return rc;
+	if ((rc = launch_persistent(g->dg, r, p, g->batch, g->grid, g->smem, st))) return rc;
+	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
+	BcArgs a{};
+	a.n = g->n;
+	a.source = source;
+	a.row_off = g->dg.row_off;
+	a.col = g->dg.col;
+	a.in_off = g->dg.in_off;
+	a.in_src = g->dg.in_src;
+	a.level = g->level_buf;
+	a.num_steps = &r.stats->num_steps;
+	a.bfs_status = &r.stats->status;
+	a.sigma = sigma ? sigma : b.sigma;
+	a.dacc = b.dacc;
+	a.delta = delta ? delta : b.delta;
+	a.acc = acc;
+	a.order = b.order;
+	a.cnt = b.cnt;
+	a.kstart = b.kstart;
+	a.ctl = b.ctl;
+	if ((rc = bc_launch(a, g->num_sms, st, &b.grid))) return rc;
+	if (cudaEventRecord(b.e2, st) != cudaSuccess) return BFS_ECUDA;
+	b.stream = st;
+	// the traversal's own statistics and events were not recorded
+	g->have_run = false;
+	return BFS_OK;
+}
+
+int bc_collect(bfs_graph *g, bfs_bc_stats *out) {
+	auto &b = g->bc;
+	cudaStream_t st = b.stream;
+	if (cudaMemcpyAsync(b.h_ctl, b.ctl, sizeof(BcControl), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+			cudaStreamSynchronize(st) != cudaSuccess)
+		return BFS_ECUDA;
+	const BcControl &c = *b.h_ctl;
+	if (out) {
+		bfs_bc_stats s{};
+		s.num_sources = 1;
+		s.depth = c.depth;
+		s.reached = c.reached;
+		s.status = (uint32_t) c.err;
+		s.edges_reached = c.edges_reached;
+		s.edges_forward = c.edges_fwd;
+		s.edges_reverse = c.edges_rev;
+		float ms = 0, tms = 0;
+		cudaEventElapsedTime(&ms, b.e0, b.e2);
+		cudaEventElapsedTime(&tms, b.e0, b.e1);
+		s.device_ms = ms;
+		s.traversal_ms = tms;
+		if (c.t[0] && c.t[1] >= c.t[0]) s.sort_ms = (float) ((c.t[1] - c.t[0]) * 1e-6);
+		if (c.t[1] && c.t[2] >= c.t[1]) s.paths_ms = (float) ((c.t[2] - c.t[1]) * 1e-6);
+		if (c.t[2] && c.t[3] >= c.t[2]) s.dependencies_ms = (float) ((c.t[3] - c.t[2]) * 1e-6);
+		s.grid_ctas = (uint32_t) b.grid;
+		*out = s;
+	}
+	return c.err;
+}
+
 } // namespace
 
 struct bfs_batch_graph {
@@ -1318,6 +1454,105 @@ int bfs_last_batch_stats(bfs_graph *g, bfs_batch_stats *stats) {
 	if (!g) return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);
 	return collect_batch_stats(g, stats);
+}
+
+// ---- betweenness (apps/betweennessCentrality_simd/bc.cpp:1717) ------------
+
+int bfs_bc_run(bfs_graph *g, uint32_t source, float *dependencies, uint32_t *num_paths, bfs_bc_stats *stats) {
+	if (!g) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	if (g->host_only) return BFS_EUNSUPPORTED;
+	if (source >= g->n) return BFS_EARG;
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	int rc = bc_prepare(g);
+	if (rc) return rc;
+	if ((rc = bc_enqueue(g, source, nullptr, nullptr, nullptr, 0))) return rc;
+	if ((rc = bc_collect(g, stats))) return rc;
+	if (dependencies &&
+			cudaMemcpy(dependencies, g->bc.delta, sizeof(float) * g->n, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return BFS_ECUDA;
+	if (num_paths && cudaMemcpy(num_paths, g->bc.sigma, sizeof(uint32_t) * g->n, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return BFS_ECUDA;
+	return BFS_OK;
+}
+
+int bfs_bc_run_device(bfs_graph *g, uint32_t source, float *dependencies, uint32_t *num_paths, void *stream) {
+	if (!g) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	if (g->host_only) return BFS_EUNSUPPORTED;
+	if (source >= g->n) return BFS_EARG;
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	int rc = bc_prepare(g);
+	if (rc) return rc;
+	return bc_enqueue(g, source, num_paths, dependencies, nullptr, (cudaStream_t) stream);
+}
+
+int bfs_bc_last_stats(bfs_graph *g, bfs_bc_stats *stats) {
+	if (!g || !stats) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	if (!g->bc.ctl) return BFS_EARG;
+	return bc_collect(g, stats);
+}
+
+int bfs_bc_accumulate(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *centrality,
+		bfs_bc_stats *stats) {
+	if (!g || !sources || !num_sources || !centrality) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	if (g->host_only) return BFS_EUNSUPPORTED;
+	for (uint32_t i = 0; i < num_sources; ++i)
+		if (sources[i] >= g->n) return BFS_EARG;
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	int rc = bc_prepare(g);
+	if (rc) return rc;
+	auto &b = g->bc;
+	if (cudaMemsetAsync(b.acc, 0, sizeof(float) * g->n, 0) != cudaSuccess) return BFS_ECUDA;
+	cudaEvent_t start = nullptr;
+	if (cudaEventCreate(&start) != cudaSuccess || cudaEventRecord(start, 0) != cudaSuccess) {
+		if (start) cudaEventDestroy(start);
+		return BFS_ECUDA;
+	}
+	bfs_bc_stats total{};
+	for (uint32_t i = 0; i < num_sources && rc == BFS_OK; ++i) {
+		rc = bc_enqueue(g, sources[i], nullptr, nullptr, b.acc, 0);
+		bfs_bc_stats one{};
+		if (rc == BFS_OK) rc = bc_collect(g, &one);
+		if (rc == BFS_OK) {
+			total.depth = std::max(total.depth, one.depth);
+			total.reached = one.reached;
+			total.edges_reached += one.edges_reached;
+			total.edges_forward += one.edges_forward;
+			total.edges_reverse += one.edges_reverse;
+			total.traversal_ms += one.traversal_ms;
+			total.sort_ms += one.sort_ms;
+			total.paths_ms += one.paths_ms;
+			total.dependencies_ms += one.dependencies_ms;
+			total.num_sources++;
+		}
+	}
+	float ms = 0;
+	if (rc == BFS_OK) cudaEventElapsedTime(&ms, start, b.e2);
+	cudaEventDestroy(start);
+	if (rc) return rc;
+	total.device_ms = ms;
+	total.grid_ctas = (uint32_t) b.grid;
+	if (stats) *stats = total;
+	if (cudaMemcpy(centrality, b.acc, sizeof(float) * g->n, cudaMemcpyDeviceToHost) != cudaSuccess) return BFS_ECUDA;
+	return BFS_OK;
+}
+
+int bfs_bc_accumulate_device(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *centrality,
+		void *stream) {
+	if (!g || !sources || !num_sources || !centrality) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	if (g->host_only) return BFS_EUNSUPPORTED;
+	for (uint32_t i = 0; i < num_sources; ++i)
+		if (sources[i] >= g->n) return BFS_EARG;
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	int rc = bc_prepare(g);
+	if (rc) return rc;
+	for (uint32_t i = 0; i < num_sources; ++i)
+		if ((rc = bc_enqueue(g, sources[i], nullptr, nullptr, centrality, (cudaStream_t) stream))) return rc;
+	return BFS_OK;
 }
 
 } // extern "C"

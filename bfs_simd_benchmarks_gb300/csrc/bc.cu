@@ -1,0 +1,406 @@
+// bc.cu -- betweenness-centrality dependencies of one source, on the device.
+//
+// The reference's BC() (apps/betweennessCentrality_simd/bc.cpp:1717-2097)
+// runs a forward BFS that adds path counts along every edge into a newly
+// reached vertex (BFS_kernel_sparse :572-775, bfs_kernel_dense :1083-1162),
+// keeps every level's frontier, then walks the frontiers backwards adding
+// 1/paths to each vertex and pushing its sum to unvisited in-neighbours over
+// the reverse graph (:1987-2030), and finally turns the sums into
+// dependencies (:2032-2061).
+//
+// Here the levels come from the single-source traversal (k_bfs_persistent),
+// and one cooperative launch does the rest with pulls instead of pushes, so
+// that no atomics touch the values and every sum has a fixed order:
+//   1. level sort: reached vertices are ordered by (level, class), with the
+//      vertices whose in- or out-degree exceeds kBcBig first in each level.
+//      Each warp owns a range of 32*q vertices and counts / places them with
+//      __match_any_sync, so the order is deterministic.
+//   2. path counts, level by level: sigma(v) = sum of sigma(u) over in-edges
+//      u -> v with level(u) = level(v) - 1 (unsigned, wraps like the
+//      reference's unsigned adds).
+//   3. dependency sums, deepest level first: D(v) = 1/sigma(v) + sum of D(w)
+//      over out-edges v -> w with level(w) = level(v) + 1; the output is
+//      (D - 1/sigma) / (1/sigma), 0 where sigma is 0 -- the reference's float
+//      formulas, with its signed int -> float conversion of the counts.
+// Per level, big vertices are reduced by a whole CTA each, the rest by warps
+// that take 32 vertices and walk their concatenated edge lists 32 edges at a
+// time (owner by a binary search over the warp's degree prefix, segmented
+// shuffle scan per 32 edges).
+#include "bc.h"
+
+#include <algorithm>
+#include <type_traits>
+
+#include "../../include/bfs_gb300.h"
+#include "device_common.cuh"
+
+namespace bfsg {
+namespace {
+
+constexpr int kBcThreads = 512;
+constexpr int kBcWarps = kBcThreads / 32;
+constexpr int kBcUnroll = 4;
+
+struct BcShared {
+	float f[kBcWarps];
+	uint32_t u[kBcWarps];
+	unsigned long long e[kBcWarps];
+	uint32_t scan[kBcWarps];
+	uint32_t total;
+};
+__device__ __shared__ BcShared bsh;
+
+template <class T> __device__ __forceinline__ T *bsh_slot();
+template <> __device__ __forceinline__ float *bsh_slot<float>() { return bsh.f; }
+template <> __device__ __forceinline__ uint32_t *bsh_slot<uint32_t>() { return bsh.u; }
+template <> __device__ __forceinline__ unsigned long long *bsh_slot<unsigned long long>() { return bsh.e; }
+
+// CTA-wide sum with a fixed association (all threads call; warp 0 gets it).
+template <class T> __device__ __forceinline__ T block_sum(T x) {
+	T *slot = bsh_slot<T>();
+	x = warp_sum(x);
+	if (lane_id() == 0) slot[warp_id()] = x;
+	__syncthreads();
+	T t = T(0);
+	if (warp_id() == 0) {
+		t = lane_id() < (unsigned) kBcWarps ? slot[lane_id()] : T(0);
+		t = warp_sum(t);
+	}
+	__syncthreads();
+	return t;
+}
+
+// CTA-wide exclusive scan; *total gets the CTA's sum (all threads call).
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t *total) {
+	const unsigned lane = lane_id(), wid = warp_id();
+	const uint32_t incl = warp_incl_scan(x);
+	if (lane == 31) bsh.scan[wid] = incl;
+	__syncthreads();
+	if (wid == 0) {
+		const uint32_t w = lane < (unsigned) kBcWarps ? bsh.scan[lane] : 0u;
+		const uint32_t wi = warp_incl_scan(w);
+		if (lane < (unsigned) kBcWarps) bsh.scan[lane] = wi - w;
+		if (lane == 31) bsh.total = wi;
+	}
+	__syncthreads();
+	const uint32_t r = incl - x + bsh.scan[wid];
+	*total = bsh.total;
+	__syncthreads();
+	return r;
+}
+
+__device__ __forceinline__ float ld_cg_f(const float *p) { return __ldcg(p); }
+
+// Sort key of a vertex: 2*level + (small ? 1 : 0); -1 for unreached and
+// out-of-range ids.
+__device__ __forceinline__ int vertex_key(const BcArgs &a, uint64_t v, uint32_t depth, int *bad) {
+	if (v >= a.n) return -1;
+	const int lv = a.level[v];
+	if (lv < 0) return -1;
+	if ((uint32_t) lv > depth) { *bad = 1; return -1; }
+	const uint32_t od = a.row_off[v + 1] - a.row_off[v];
+	const uint32_t id = a.in_off[v + 1] - a.in_off[v];
+	return 2 * lv + ((od > kBcBig || id > kBcBig) ? 0 : 1);
+}
+
+template <bool kFwd> struct Dir {
+	using T = typename std::conditional<kFwd, uint32_t, float>::type;
+	static __device__ __forceinline__ const uint32_t *off(const BcArgs &a) { return kFwd ? a.in_off : a.row_off; }
+	static __device__ __forceinline__ const uint32_t *adj(const BcArgs &a) { return kFwd ? a.in_src : a.col; }
+	static __device__ __forceinline__ T value(const BcArgs &a, uint32_t u);
+};
+template <> __device__ __forceinline__ uint32_t Dir<true>::value(const BcArgs &a, uint32_t u) { return ld_cg(a.sigma + u); }
+template <> __device__ __forceinline__ float Dir<false>::value(const BcArgs &a, uint32_t u) { return ld_cg_f(a.dacc + u); }
+
+// Sum over the edge list of one vertex by the whole CTA (result in warp 0).
+template <bool kFwd>
+__device__ __forceinline__ typename Dir<kFwd>::T cta_vertex_sum(const BcArgs &a, uint32_t v, int target) {
+	using T = typename Dir<kFwd>::T;
+	const uint32_t *adj = Dir<kFwd>::adj(a);
+	const uint64_t beg = Dir<kFwd>::off(a)[v], end = Dir<kFwd>::off(a)[v + 1];
+	T s = T(0);
+	for (uint64_t e = beg + threadIdx.x; e < end; e += (uint64_t) kBcThreads * kBcUnroll) {
+		uint32_t nb[kBcUnroll];
+		int lv[kBcUnroll];
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k) {
+			const uint64_t ee = e + (uint64_t) k * kBcThreads;
+			nb[k] = ee < end ? __ldg(adj + ee) : 0xFFFFFFFFu;
+		}
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k) lv[k] = nb[k] != 0xFFFFFFFFu ? __ldg(a.level + nb[k]) : -2;
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k)
+			if (lv[k] == target) s += Dir<kFwd>::value(a, nb[k]);
+	}
+	return block_sum(s);
+}
+
+// Sums of the edge lists of 32 vertices order[first .. min(first+32, end))
+// by one warp; lane i gets vertex i's sum (0 for lanes past `end`).
+template <bool kFwd>
+__device__ __forceinline__ typename Dir<kFwd>::T warp_group_sum(const BcArgs &a, uint32_t v, bool valid, int target,
+		bool skip, unsigned long long *edges) {
+	using T = typename Dir<kFwd>::T;
+	const unsigned lane = lane_id();
+	uint32_t beg = 0, deg = 0;
+	if (valid) {
+		beg = Dir<kFwd>::off(a)[v];
+		deg = Dir<kFwd>::off(a)[v + 1] - beg;
+	}
+	if (skip) deg = 0;
+	*edges += deg;
+	const uint32_t incl = warp_incl_scan(deg);
+	const uint32_t excl = incl - deg;
+	const uint32_t total = __shfl_sync(kFull, incl, 31);
+	const uint32_t *adj = Dir<kFwd>::adj(a);
+	T acc = T(0);
+	for (uint32_t f0 = 0; f0 < total; f0 += 32u * kBcUnroll) {
+		uint32_t nb[kBcUnroll], own[kBcUnroll];
+		int lv[kBcUnroll];
+		T val[kBcUnroll];
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k) {
+			const uint32_t f = f0 + (uint32_t) k * 32u + lane;
+			// owner = number of lanes whose inclusive prefix is <= f
+			uint32_t o = 0;
+#pragma unroll
+			for (uint32_t step = 16; step > 0; step >>= 1) {
+				const uint32_t x = __shfl_sync(kFull, incl, o + step - 1);
+				if (x <= f) o += step;
+			}
+			const uint32_t ob = __shfl_sync(kFull, beg, o);
+			const uint32_t oe = __shfl_sync(kFull, excl, o);
+			const bool on = f < total;
+			own[k] = on ? o : 32u;
+			nb[k] = on ? __ldg(adj + ob + (f - oe)) : 0u;
+		}
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k) lv[k] = own[k] < 32u ? __ldg(a.level + nb[k]) : -2;
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k) val[k] = lv[k] == target ? Dir<kFwd>::value(a, nb[k]) : T(0);
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k) {
+			T x = val[k];
+			const uint32_t o = own[k];
+#pragma unroll
+			for (uint32_t dd = 1; dd < 32; dd <<= 1) {
+				const T y = __shfl_up_sync(kFull, x, dd);
+				const uint32_t oo = __shfl_up_sync(kFull, o, dd);
+				if (lane >= dd && oo == o) x += y;
+			}
+			// the last lane of this vertex's run in these 32 edges holds its sum
+			const uint32_t base = f0 + (uint32_t) k * 32u;
+			const bool mine = deg > 0 && incl > base && excl < base + 32u;
+			const uint32_t src = mine ? min(incl, base + 32u) - 1u - base : 0u;
+			const T got = __shfl_sync(kFull, x, src);
+			if (mine) acc += got;
+		}
+	}
+	return acc;
+}
+
+__device__ __forceinline__ void finish_dependency(const BcArgs &a, uint32_t v, float sum) {
+	const uint32_t sg = ld_cg(a.sigma + v);
+	const float inv = sg ? 1.0f / (float) (int) sg : 0.0f;
+	const float dv = sum + inv;
+	a.dacc[v] = dv;
+	const float del = inv != 0.0f ? (dv - inv) / inv : 0.0f;
+	a.delta[v] = del;
+	if (a.acc && v != a.source) a.acc[v] += del;
+}
+
+__global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
+	BcControl *ctl = a.ctl;
+	const unsigned lane = lane_id();
+	const uint32_t gw = blockIdx.x * kBcWarps + warp_id();
+	const uint32_t tw = gridDim.x * kBcWarps;
+	if (blockIdx.x == 0 && threadIdx.x == 0) ctl->t[0] = global_timer_ns();
+	// the traversal's outcome decides for every CTA alike
+	const int bfs_st = *(const volatile int *) a.bfs_status;
+	const uint32_t steps = *(const volatile uint32_t *) a.num_steps;
+	if (bfs_st != 0 || steps == 0 || steps > kBcMaxLevels) {
+		if (blockIdx.x == 0 && threadIdx.x == 0)
+			ctl->err = bfs_st != 0 ? bfs_st : (steps == 0 ? BFS_ECUDA : BFS_EUNSUPPORTED);
+		return;
+	}
+	const uint32_t depth = steps - 1;
+	const uint32_t K = 2u * steps;
+	const uint64_t W32 = ((uint64_t) a.n + 31) / 32;
+	uint64_t q = (K * W32 + kBcCntCap - 1) / kBcCntCap;
+	if (q == 0) q = 1;
+	uint64_t R = (W32 + q - 1) / q;
+	while ((uint64_t) K * R > kBcCntCap) {
+		++q;
+		R = (W32 + q - 1) / q;
+	}
+	const uint64_t KR = (uint64_t) K * R;
+
+	// ---- 1a. count (level key, range) and initialise the outputs ----------
+	unsigned long long my_edges = 0;
+	uint32_t my_reached = 0;
+	int bad = 0;
+	for (uint64_t r = gw; r < R; r += tw) {
+		for (uint32_t k = lane; k < K; k += 32) a.cnt[(uint64_t) k * R + r] = 0;
+		__syncwarp();
+		const uint64_t v0 = r * 32 * q;
+		for (uint64_t j = 0; j < q; ++j) {
+			const uint64_t v = v0 + j * 32 + lane;
+			const int key = vertex_key(a, v, depth, &bad);
+			if (v < a.n) {
+				a.sigma[v] = v == a.source ? 1u : 0u;
+				a.delta[v] = 0.0f;
+			}
+			if (key >= 0) {
+				++my_reached;
+				my_edges += a.row_off[v + 1] - a.row_off[v];
+			}
+			const unsigned mm = __match_any_sync(kFull, key);
+			if (key >= 0 && lane == (unsigned) (__ffs(mm) - 1)) a.cnt[(uint64_t) key * R + r] += __popc(mm);
+			__syncwarp();
+		}
+	}
+	{
+		const unsigned long long e = block_sum(my_edges);
+		const uint32_t rc = block_sum(my_reached);
+		const uint32_t b = block_sum((uint32_t) bad);
+		if (threadIdx.x == 0) {
+			if (e) atomicAdd(&ctl->edges_reached, e);
+			if (rc) atomicAdd(&ctl->reached, rc);
+			if (b) atomicExch(&ctl->err, BFS_ECUDA);
+		}
+	}
+	if (!grid_barrier(ctl->bar, &ctl->err)) return;
+
+	// ---- 1b. exclusive scan of the counters (key-major) --------------------
+	const uint64_t L = (KR + gridDim.x - 1) / gridDim.x;
+	const uint64_t lo = (uint64_t) blockIdx.x * L < KR ? (uint64_t) blockIdx.x * L : KR;
+	const uint64_t hi = lo + L < KR ? lo + L : KR;
+	{
+		uint32_t s = 0;
+		for (uint64_t i = lo + threadIdx.x; i < hi; i += kBcThreads) s += a.cnt[i];
+		s = block_sum(s);
+		if (threadIdx.x == 0) ctl->blk[blockIdx.x] = s;
+	}
+	if (!grid_barrier(ctl->bar, &ctl->err)) return;
+	{
+		uint32_t base = 0;
+		for (uint32_t c = threadIdx.x; c < blockIdx.x; c += kBcThreads) base += ld_cg(ctl->blk + c);
+		base = block_sum(base);
+		if (warp_id() == 0 && lane == 0) bsh.u[0] = base;
+		__syncthreads();
+		base = bsh.u[0];
+		__syncthreads();
+		for (uint64_t t0 = lo; t0 < hi; t0 += kBcThreads) {
+			const uint64_t i = t0 + threadIdx.x;
+			const uint32_t x = i < hi ? a.cnt[i] : 0u;
+			uint32_t tot;
+			const uint32_t ex = block_excl_scan(x, &tot) + base;
+			if (i < hi) {
+				a.cnt[i] = ex;
+				if (i % R == 0) a.kstart[i / R] = ex;
+			}
+			base += tot;
+		}
+		if (blockIdx.x == 0 && threadIdx.x == 0) a.kstart[K] = ld_cg(&ctl->reached);
+	}
+	if (!grid_barrier(ctl->bar, &ctl->err)) return;
+
+	// ---- 1c. place the vertices ------------------------------------------
+	for (uint64_t r = gw; r < R; r += tw) {
+		const uint64_t v0 = r * 32 * q;
+		for (uint64_t j = 0; j < q; ++j) {
+			const uint64_t v = v0 + j * 32 + lane;
+			int dummy = 0;
+			const int key = vertex_key(a, v, depth, &dummy);
+			const unsigned mm = __match_any_sync(kFull, key);
+			const unsigned leader = (unsigned) (__ffs(mm) - 1);
+			uint32_t base = 0;
+			if (key >= 0 && lane == leader) base = ld_cg(a.cnt + (uint64_t) key * R + r);
+			base = __shfl_sync(kFull, base, leader);
+			if (key >= 0) {
+				a.order[base + __popc(mm & lanemask_lt())] = (uint32_t) v;
+				if (lane == leader) a.cnt[(uint64_t) key * R + r] = base + __popc(mm);
+			}
+			__syncwarp();
+		}
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) ctl->t[1] = global_timer_ns();
+	if (!grid_barrier(ctl->bar, &ctl->err)) return;
+
+	// ---- 2. path counts, level by level ----------------------------------
+	unsigned long long e_fwd = 0, e_rev = 0;
+	for (uint32_t d = 1; d <= depth; ++d) {
+		const uint32_t bb = ld_cg(a.kstart + 2 * d), be = ld_cg(a.kstart + 2 * d + 1), se = ld_cg(a.kstart + 2 * d + 2);
+		for (uint32_t i = bb + blockIdx.x; i < be; i += gridDim.x) {
+			const uint32_t v = ld_cg(a.order + i);
+			const uint32_t s = cta_vertex_sum<true>(a, v, (int) d - 1);
+			if (threadIdx.x == 0) {
+				a.sigma[v] = s;
+				e_fwd += a.in_off[v + 1] - a.in_off[v];
+			}
+		}
+		const uint32_t groups = (se - be + 31) / 32;
+		for (uint32_t grp = tw - 1 - gw; grp < groups; grp += tw) {
+			const uint32_t idx = be + grp * 32 + lane;
+			const bool valid = idx < se;
+			const uint32_t v = valid ? ld_cg(a.order + idx) : 0u;
+			const uint32_t s = warp_group_sum<true>(a, v, valid, (int) d - 1, false, &e_fwd);
+			if (valid) a.sigma[v] = s;
+		}
+		if (!grid_barrier(ctl->bar, &ctl->err)) return;
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) ctl->t[2] = global_timer_ns();
+
+	// ---- 3. dependency sums, deepest level first ---------------------------
+	for (int d = (int) depth; d >= 0; --d) {
+		const bool deepest = (uint32_t) d == depth;
+		const uint32_t bb = ld_cg(a.kstart + 2 * d), be = ld_cg(a.kstart + 2 * d + 1), se = ld_cg(a.kstart + 2 * d + 2);
+		for (uint32_t i = bb + blockIdx.x; i < be; i += gridDim.x) {
+			const uint32_t v = ld_cg(a.order + i);
+			const float s = deepest ? 0.0f : cta_vertex_sum<false>(a, v, d + 1);
+			if (threadIdx.x == 0) {
+				finish_dependency(a, v, s);
+				if (!deepest) e_rev += a.row_off[v + 1] - a.row_off[v];
+			}
+		}
+		const uint32_t groups = (se - be + 31) / 32;
+		for (uint32_t grp = tw - 1 - gw; grp < groups; grp += tw) {
+			const uint32_t idx = be + grp * 32 + lane;
+			const bool valid = idx < se;
+			const uint32_t v = valid ? ld_cg(a.order + idx) : 0u;
+			const float s = warp_group_sum<false>(a, v, valid, d + 1, deepest, &e_rev);
+			if (valid) finish_dependency(a, v, s);
+		}
+		if (d > 0 && !grid_barrier(ctl->bar, &ctl->err)) return;
+	}
+	{
+		const unsigned long long ef = block_sum(e_fwd);
+		const unsigned long long er = block_sum(e_rev);
+		if (threadIdx.x == 0) {
+			if (ef) atomicAdd(&ctl->edges_fwd, ef);
+			if (er) atomicAdd(&ctl->edges_rev, er);
+			ctl->depth = depth;
+		}
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) ctl->t[3] = global_timer_ns();
+}
+
+} // namespace
+
+int bc_launch(const BcArgs &a, int num_sms, cudaStream_t st, int *grid) {
+	int per_sm = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bc, kBcThreads, 0) != cudaSuccess || per_sm < 1)
+		return BFS_ECUDA;
+	per_sm = std::min(per_sm, 2);
+	const int g = std::min<int>(num_sms * per_sm, (int) kBcMaxGrid);
+	if (grid) *grid = g;
+	if (cudaMemsetAsync(a.ctl, 0, sizeof(BcControl), st) != cudaSuccess) return BFS_ECUDA;
+	BcArgs aa = a;
+	void *args[] = {&aa};
+	if (cudaLaunchCooperativeKernel((const void *) k_bc, dim3(g), dim3(kBcThreads), args, 0, st) != cudaSuccess)
+		return BFS_ECUDA;
+	return BFS_OK;
+}
+
+} // namespace bfsg

@@ -1,0 +1,50 @@
+// bc.h -- betweenness-centrality dependencies of one source on the device
+// (internal): the reference's BC() (apps/betweennessCentrality_simd/bc.cpp:
+// 1717-2097) as one cooperative launch after a single-source traversal.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bfsg {
+
+constexpr uint32_t kBcMaxLevels = 1u << 20;   // deeper traversals are refused (BFS_EUNSUPPORTED)
+constexpr uint32_t kBcCntCap = 1u << 22;      // (level key, vertex range) counters of the level sort
+constexpr uint32_t kBcBig = 1024;             // in- or out-degree above which a whole CTA reduces a vertex
+constexpr uint32_t kBcMaxGrid = 1024;
+
+struct BcControl {
+	unsigned bar[2];            // grid barrier
+	int err;                    // BFS_* status (0 ok)
+	uint32_t depth;             // deepest level
+	uint32_t reached;
+	uint32_t pad;
+	unsigned long long edges_fwd;      // in-edges read by the path-count sweep
+	unsigned long long edges_rev;      // out-edges read by the dependency sweep
+	unsigned long long edges_reached;  // sum of out-degrees of reached vertices
+	unsigned long long t[4];           // global timer: start, sorted, path counts done, end
+	uint32_t blk[kBcMaxGrid];          // per-CTA totals of the counter scan
+};
+
+struct BcArgs {
+	uint32_t n, source;
+	const uint32_t *row_off, *col;     // CSR
+	const uint32_t *in_off, *in_src;   // in-edge lists (the reverse graph)
+	const int32_t *level;              // levels of the traversal from `source`, -1 unreached
+	const uint32_t *num_steps;         // the traversal's step count (deepest level + 1)
+	const int *bfs_status;             // the traversal's status word
+	uint32_t *sigma;                   // [n] shortest-path counts (mod 2^32)
+	float *dacc;                       // [n] (1 + dependency) / paths, the reverse sweep's sums
+	float *delta;                      // [n] dependencies (output)
+	float *acc;                        // [n] or null: += dependency for every vertex but the source
+	uint32_t *order;                   // [n] reached vertices sorted by (level, big first)
+	uint32_t *cnt;                     // [kBcCntCap] counters of the level sort
+	uint32_t *kstart;                  // [2 * kBcMaxLevels + 1] start of every key in `order`
+	BcControl *ctl;
+};
+
+// Enqueues the dependency computation on `st` (after the traversal that wrote
+// a.level).  The control block is cleared first.  *grid gets the CTA count.
+int bc_launch(const BcArgs &a, int num_sms, cudaStream_t st, int *grid);
+
+} // namespace bfsg

@@ -207,6 +207,44 @@ class Graph:
                 "bfs_tune_options")
         return r.as_dict()
 
+    def bc(self, source: int, paths: bool = True):
+        """Betweenness dependencies of one source (bfs_bc_run): float32 [N]
+        dependencies, uint32 [N] shortest-path counts (or None) and the stats."""
+        n = self.num_vertices
+        dep = np.empty(n, dtype=np.float32)
+        sig = np.empty(n, dtype=np.uint32) if paths else None
+        st = N.BcStats()
+        N.check(N.load().bfs_bc_run(self._h, int(source), dep.ctypes.data_as(C.c_void_p),
+                                    sig.ctypes.data_as(C.c_void_p) if paths else None, C.byref(st)), "bfs_bc_run")
+        return dep, sig, st.as_dict()
+
+    def bc_device(self, source: int, dependencies_ptr: int = 0, paths_ptr: int = 0, stream: int = 0) -> None:
+        """bfs_bc_run_device: enqueued on `stream`, results into device buffers."""
+        N.check(N.load().bfs_bc_run_device(self._h, int(source), C.c_void_p(dependencies_ptr) if dependencies_ptr else None,
+                                           C.c_void_p(paths_ptr) if paths_ptr else None,
+                                           C.c_void_p(stream) if stream else None), "bfs_bc_run_device")
+
+    def bc_stats(self) -> dict:
+        st = N.BcStats()
+        N.check(N.load().bfs_bc_last_stats(self._h, C.byref(st)), "bfs_bc_last_stats")
+        return st.as_dict()
+
+    def betweenness(self, sources):
+        """Betweenness centrality over `sources` (bfs_bc_accumulate): float32 [N]
+        sum over sources s != v of the dependencies of s on v, and the stats."""
+        src = _u32(sources)
+        out = np.empty(self.num_vertices, dtype=np.float32)
+        st = N.BcStats()
+        N.check(N.load().bfs_bc_accumulate(self._h, _ptr(src, C.c_uint32), src.size, out.ctypes.data_as(C.c_void_p),
+                                           C.byref(st)), "bfs_bc_accumulate")
+        return out, st.as_dict()
+
+    def betweenness_device(self, sources, centrality_ptr: int, stream: int = 0) -> None:
+        """bfs_bc_accumulate_device: adds into a device float32 [N] buffer."""
+        src = _u32(sources)
+        N.check(N.load().bfs_bc_accumulate_device(self._h, _ptr(src, C.c_uint32), src.size, C.c_void_p(centrality_ptr),
+                                                  C.c_void_p(stream) if stream else None), "bfs_bc_accumulate_device")
+
     def last_batch_stats(self) -> dict:
         st = N.BatchStats()
         N.check(N.load().bfs_last_batch_stats(self._h, C.byref(st)), "bfs_last_batch_stats")

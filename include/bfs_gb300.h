@@ -438,6 +438,53 @@ int bfs_tool_vertex_remap(const char *data, uint32_t flags);
  * old id within a level, unreached vertices last in ascending old id. */
 int bfs_graph_bfs_order(bfs_graph *g, uint32_t source, uint32_t *vertex_map);
 
+/* ---- betweenness centrality --------------------------------------------- */
+/* Replaces BC() of apps/betweennessCentrality_simd/bc.cpp:1717-2097 (which
+ * reads a second, reverse-tiled file family; the in-edge lists of the loaded
+ * graph serve as the reverse graph here).  For one source s it computes the
+ * shortest-path counts num_paths[v] (unsigned 32-bit, wrapping like the
+ * reference's unsigned adds) and the dependencies
+ *   dependencies[v] = sigma(v) * sum over out-edges v -> w one level deeper of
+ *                     (1 + dependencies[w]) / sigma(w),
+ * in float through the reference's formulas: inverse = 1.0f / (float)(int)
+ * num_paths (0 where num_paths is 0), sums of inverses pulled level by level
+ * from the deepest, result (sum - inverse) / inverse.  Unreached vertices get
+ * 0; the source gets the number of other vertices it reaches (the reference
+ * computes it the same way).  Sums are taken in a fixed order: repeated runs
+ * give identical bits.  Traversals deeper than 2^20 levels: BFS_EUNSUPPORTED. */
+typedef struct bfs_bc_stats {
+	uint32_t num_sources;     /* dependency runs counted here */
+	uint32_t depth;           /* deepest level (the largest over the runs) */
+	uint32_t reached;         /* vertices reached from the (last) source */
+	uint32_t status;          /* BFS_* status of the device run */
+	uint64_t edges_reached;   /* sum of the out-degrees of reached vertices, over the runs */
+	uint64_t edges_forward;   /* in-edges read by the path-count sweeps */
+	uint64_t edges_reverse;   /* out-edges read by the dependency sweeps */
+	float device_ms;          /* traversals + dependency launches, device events */
+	float traversal_ms;       /* of which the single-source traversals */
+	float sort_ms;            /* level sort, path counts, dependency sums: device timers */
+	float paths_ms;
+	float dependencies_ms;
+	uint32_t grid_ctas;
+} bfs_bc_stats;
+
+/* dependencies[N] and num_paths[N] are HOST buffers (either may be NULL). */
+int bfs_bc_run(bfs_graph *g, uint32_t source, float *dependencies, uint32_t *num_paths, bfs_bc_stats *stats);
+/* The same enqueued on `stream` into DEVICE buffers (either may be NULL: the
+ * graph's own buffers are used); no host synchronisation. */
+int bfs_bc_run_device(bfs_graph *g, uint32_t source, float *dependencies, uint32_t *num_paths, void *stream);
+/* Statistics of the last bfs_bc_* run (synchronises with it). */
+int bfs_bc_last_stats(bfs_graph *g, bfs_bc_stats *stats);
+/* Betweenness centrality over a set of sources: centrality[v] (HOST, N floats,
+ * overwritten) = sum over the sources s != v of the dependencies of s on v;
+ * over all N sources it is the unnormalised directed betweenness. */
+int bfs_bc_accumulate(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *centrality,
+		bfs_bc_stats *stats);
+/* The same into a DEVICE buffer that is added to (not cleared), enqueued on
+ * `stream`; sources is a host array. */
+int bfs_bc_accumulate_device(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *centrality,
+		void *stream);
+
 /* ---- synthetic inputs (no counterpart in the reference) ------------------ */
 #define BFS_RMAT_NO_SELF_LOOPS 0x1u
 #define BFS_RMAT_DEDUP 0x2u

@@ -880,3 +880,117 @@ unsigned long long orc_check_parents(unsigned n, const unsigned *vertices, const
 }
 
 int orc_max_threads(void) { return omp_get_max_threads(); }
+
+/* ------------------------------------------------------------------------ */
+/* Betweenness-centrality dependencies of one source                        */
+/* ------------------------------------------------------------------------ */
+
+/* The reference's BC() (apps/betweennessCentrality_simd/bc.cpp:1717-2097),
+ * restated sequentially.
+ *
+ * Forward: a level-synchronous BFS from `source` in which every edge u -> v
+ * from the current frontier to a vertex not visited before this step adds
+ * num_paths[u] to num_paths[v] in unsigned 32-bit arithmetic
+ * (BFS_kernel_sparse :572-775 with its CAS loop at :640-648, bfs_kernel_dense
+ * :1083-1162); the frontiers of every level are kept (:1753-1905).
+ * Inverse path counts: 1.0f / (float)(int)num_paths, 0 where num_paths is 0
+ * (:1950-1971, a signed conversion).
+ * Reverse: from the deepest frontier down to the source's, each frontier
+ * vertex is marked visited and adds its inverse to its dependency
+ * (update_visited_sparse_reverse :470-503, update_visited_dense_reverse
+ * :927-989), then every in-neighbour of it not yet visited in the reverse
+ * sweep adds the vertex's dependency (BFS_kernel_sparse_reverse :795-826,
+ * bfs_kernel_dense_reverse :1415-1494, over the reverse graph).
+ * Finally dependency = (dependency - inverse) / inverse where the inverse is
+ * non-zero, else 0 (:2032-2061).  All of it in float, like the reference.
+ *
+ * The reference's sparse step appends a vertex to the next frontier when its
+ * path count was 0 before the add (:649); a count that wraps to exactly 0 mod
+ * 2^32 would append it twice.  This restatement takes every vertex once (the
+ * BFS levels), which is the reference's result whenever no count wraps to 0.
+ *
+ * Outputs: num_paths[n], dependencies[n], cost[n] (levels, -1 unreached) and
+ * scale[n] (may be NULL): the same recurrence in double over absolute values,
+ * (sum |terms|) / |inverse|, the magnitude that bounds the rounding error of a
+ * float evaluation in any summation order. */
+int orc_bc_single(unsigned n, const unsigned *vertices, const unsigned *degrees, const unsigned *edges,
+		unsigned source, unsigned *num_paths, float *dependencies, int *cost, double *scale)
+{
+	if (source >= n) return ORC_EARG;
+	size_t m = 0;
+	for (unsigned v = 0; v < n; ++v) m += degrees[v];
+	unsigned *q = (unsigned *) malloc(sizeof(unsigned) * (size_t) n);
+	unsigned *lvl_beg = (unsigned *) malloc(sizeof(unsigned) * ((size_t) n + 2));
+	unsigned *in_off = (unsigned *) calloc((size_t) n + 1, sizeof(unsigned));
+	unsigned *in_src = (unsigned *) malloc(sizeof(unsigned) * (m ? m : 1));
+	unsigned *fill = (unsigned *) malloc(sizeof(unsigned) * ((size_t) n + 1));
+	float *inv = (float *) malloc(sizeof(float) * (size_t) n);
+	double *dabs = (double *) malloc(sizeof(double) * (size_t) n);
+	char *vis = (char *) calloc(n, 1);
+	if (!q || !lvl_beg || !in_off || !in_src || !fill || !inv || !dabs || !vis) {
+		free(q); free(lvl_beg); free(in_off); free(in_src); free(fill); free(inv); free(dabs); free(vis);
+		return ORC_ENOMEM;
+	}
+	/* reverse graph: in-edges grouped by destination, sources in CSR order */
+	for (unsigned u = 0; u < n; ++u)
+		for (unsigned e = vertices[u]; e < vertices[u] + degrees[u]; ++e) in_off[edges[e] + 1]++;
+	for (unsigned v = 0; v < n; ++v) in_off[v + 1] += in_off[v];
+	memcpy(fill, in_off, sizeof(unsigned) * ((size_t) n + 1));
+	for (unsigned u = 0; u < n; ++u)
+		for (unsigned e = vertices[u]; e < vertices[u] + degrees[u]; ++e) in_src[fill[edges[e]]++] = u;
+
+	/* forward: frontiers q[lvl_beg[l] .. lvl_beg[l+1]) */
+	for (unsigned v = 0; v < n; ++v) { num_paths[v] = 0; cost[v] = -1; dependencies[v] = 0.0f; dabs[v] = 0.0; }
+	unsigned nl = 0, tail = 0;
+	num_paths[source] = 1;
+	cost[source] = 0;
+	q[tail++] = source;
+	lvl_beg[0] = 0;
+	lvl_beg[1] = tail;
+	nl = 1;
+	while (lvl_beg[nl] > lvl_beg[nl - 1]) {
+		const unsigned b = lvl_beg[nl - 1], e = lvl_beg[nl];
+		for (unsigned i = b; i < e; ++i) {
+			const unsigned u = q[i];
+			for (unsigned k = vertices[u]; k < vertices[u] + degrees[u]; ++k) {
+				const unsigned v = edges[k];
+				if (cost[v] >= 0 && cost[v] < (int) nl) continue; /* visited before this step */
+				if (cost[v] < 0) { cost[v] = (int) nl; q[tail++] = v; }
+				num_paths[v] += num_paths[u];
+			}
+		}
+		lvl_beg[++nl] = tail;
+	}
+	/* inverse path counts (signed conversion, as _mm512_cvtepi32_ps) */
+	for (unsigned v = 0; v < n; ++v) inv[v] = num_paths[v] ? 1.0f / (float) (int) num_paths[v] : 0.0f;
+	/* reverse sweep: levels nl-2 .. 0 hold the non-empty frontiers */
+	for (int l = (int) nl - 2; l >= 0; --l) {
+		const unsigned b = lvl_beg[l], e = lvl_beg[l + 1];
+		for (unsigned i = b; i < e; ++i) {
+			const unsigned v = q[i];
+			vis[v] = 1;
+			dependencies[v] += inv[v];
+			dabs[v] += inv[v] < 0 ? -(double) inv[v] : (double) inv[v];
+		}
+		for (unsigned i = b; i < e; ++i) {
+			const unsigned v = q[i];
+			for (unsigned k = in_off[v]; k < in_off[v + 1]; ++k) {
+				const unsigned u = in_src[k];
+				if (vis[u]) continue;
+				dependencies[u] += dependencies[v];
+				dabs[u] += dabs[v];
+			}
+		}
+	}
+	for (unsigned v = 0; v < n; ++v) {
+		if (inv[v] != 0.0f) {
+			dependencies[v] = (dependencies[v] - inv[v]) / inv[v];
+			if (scale) scale[v] = dabs[v] / (inv[v] < 0 ? -(double) inv[v] : (double) inv[v]);
+		} else {
+			dependencies[v] = 0.0f;
+			if (scale) scale[v] = 0.0;
+		}
+	}
+	free(q); free(lvl_beg); free(in_off); free(in_src); free(fill); free(inv); free(dabs); free(vis);
+	return ORC_OK;
+}

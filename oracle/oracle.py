@@ -57,6 +57,8 @@ def lib() -> C.CDLL:
                                C.POINTER(C.c_double)],
             "orc_bfs_levels": [C.c_uint, _u32p, _u32p, _u32p, C.c_uint, _i32p],
             "orc_check_parents": [C.c_uint, _u32p, _u32p, _u32p, C.c_uint, _i32p, _u32p],
+            "orc_bc_single": [C.c_uint, _u32p, _u32p, _u32p, C.c_uint, _u32p, C.POINTER(C.c_float), _i32p,
+                              C.POINTER(C.c_double)],
             "orc_max_threads": [],
         }
         for name, args in sig.items():
@@ -148,6 +150,20 @@ def check_parents(arr: dict, source: int, cost, parents) -> int:
     p = _u(parents)
     return int(lib().orc_check_parents(arr["n"], _p(arr["row_start"]), _p(arr["degrees"]), _p(arr["csr_dst"]),
                                        int(source), _p(c), _p(p)))
+
+
+def bc_single(arr: dict, source: int):
+    """Path counts (uint32), float dependencies, levels and per-vertex error
+    scale of one source: the reference's BC() restated (bfs_oracle.c)."""
+    n = arr["n"]
+    sigma = np.empty(n, dtype=np.uint32)
+    dep = np.empty(n, dtype=np.float32)
+    cost = np.empty(n, dtype=np.int32)
+    scale = np.empty(n, dtype=np.float64)
+    _ok(lib().orc_bc_single(n, _p(arr["row_start"]), _p(arr["degrees"]), _p(arr["csr_dst"]), int(source),
+                            _p(sigma), dep.ctypes.data_as(C.POINTER(C.c_float)), _p(cost),
+                            scale.ctypes.data_as(C.POINTER(C.c_double))), "bc_single")
+    return sigma, dep, cost, scale
 
 
 def max_threads() -> int:

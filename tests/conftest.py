@@ -73,3 +73,32 @@ def gpu_available() -> bool:
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+BC_RTOL = 1e-4  # float dependencies vs a double or differently ordered float evaluation
+
+
+def bc_case_names():
+    z = np.load(os.path.join(GOLDEN, "bc_networkx.npz"))
+    return [str(x) for x in z["names"]]
+
+
+def load_bc_case(name: str) -> dict:
+    """A graph of the networkx betweenness fixtures with its edge list."""
+    z = np.load(os.path.join(GOLDEN, "bc_networkx.npz"))
+    out = {"n": int(z[name + "__n"]), "sources": z[name + "__sources"], "delta": z[name + "__delta"],
+           "bc": z[name + "__bc"] if name + "__bc" in z.files else None}
+    if name.startswith("hand_"):
+        out["src"], out["dst"] = z[name + "__src"], z[name + "__dst"]
+        out["w"], out["s"] = 4, 2
+    else:
+        c = load_case(name)
+        out["src"], out["dst"], out["w"], out["s"] = c["src"], c["dst"], c["w"], c["s"]
+    return out
+
+
+def bc_close(got, want, scale, rtol: float = BC_RTOL) -> np.ndarray:
+    """Mask of dependencies within rtol of the error scale of their float sums."""
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    return np.abs(got - want) <= rtol * (np.abs(scale) + 1.0)
