@@ -420,6 +420,8 @@ def bench_bc(args, torch, dev, g, sources, flush, arr=None):
         "dependency_kernel_ms_mean": k_ms / len(sts),
         "phase_ms_mean": {k: statistics.mean(st[k] for st in sts) for k in ("sort_ms", "paths_ms", "dependencies_ms")},
         "depth_mean": statistics.mean(st["depth"] for st in sts),
+        "example_levels": {k: sts[0][k] for k in ("level_vertices", "level_big", "level_medium", "level_paths_ms",
+                                                  "level_dependencies_ms")},
         "roofline": {"kernel": "k_bc", "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": ach / peak if peak else None, "algorithmic_bytes_per_launch": alg / len(sts)},
         "e2e": {"value": e2e_edges / e2e_s / 1e9, "unit": "GTEPS", "d2h_bytes_per_step": 4 * n * len(srcs),

@@ -78,6 +78,9 @@ class Options(C.Structure):
     ]
 
 
+BFS_BC_TRACE_LEVELS = 64
+
+
 class BcStats(C.Structure):
     _fields_ = [
         ("num_sources", C.c_uint32),
@@ -93,10 +96,22 @@ class BcStats(C.Structure):
         ("paths_ms", C.c_float),
         ("dependencies_ms", C.c_float),
         ("grid_ctas", C.c_uint32),
+        ("level_paths_ms", C.c_float * BFS_BC_TRACE_LEVELS),
+        ("level_dependencies_ms", C.c_float * BFS_BC_TRACE_LEVELS),
+        ("level_vertices", C.c_uint32 * BFS_BC_TRACE_LEVELS),
+        ("level_big", C.c_uint32 * BFS_BC_TRACE_LEVELS),
+        ("level_medium", C.c_uint32 * BFS_BC_TRACE_LEVELS),
     ]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("level_")}
+        k = min(self.depth + 1, BFS_BC_TRACE_LEVELS)
+        for name in ("level_paths_ms", "level_dependencies_ms"):
+            d[name] = [round(x, 4) for x in getattr(self, name)[:k]]
+        d["level_vertices"] = list(self.level_vertices[:k])
+        d["level_big"] = list(self.level_big[:k])
+        d["level_medium"] = list(self.level_medium[:k])
+        return d
 
 
 class BatchStats(C.Structure):

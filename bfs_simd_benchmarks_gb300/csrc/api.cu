@@ -84,8 +84,9 @@ struct bfs_graph {
 	} mb;
 	// betweenness state, allocated by the first bfs_bc_* call
 	struct Bc {
-		uint32_t *sigma = nullptr, *order = nullptr, *cnt = nullptr, *kstart = nullptr;
-		float *dacc = nullptr, *delta = nullptr, *acc = nullptr;
+		uint32_t *sigma = nullptr, *order = nullptr, *cnt = nullptr, *kstart = nullptr, *partial = nullptr;
+		float *delta = nullptr, *acc = nullptr;
+		uint2 *lvx = nullptr;
 		BcControl *ctl = nullptr;
 		BcControl *h_ctl = nullptr;  // pinned
 		cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
@@ -871,9 +872,10 @@ int bc_prepare(bfs_graph *g) {
 	if (b.ctl) return BFS_OK;
 	int rc;
 	if ((rc = bc_alloc(g, &b.sigma, g->n)) || (rc = bc_alloc(g, &b.order, g->n)) ||
-			(rc = bc_alloc(g, &b.dacc, g->n)) || (rc = bc_alloc(g, &b.delta, g->n)) ||
+			(rc = bc_alloc(g, &b.lvx, g->n)) || (rc = bc_alloc(g, &b.delta, g->n)) ||
 			(rc = bc_alloc(g, &b.acc, g->n)) || (rc = bc_alloc(g, &b.cnt, kBcCntCap)) ||
-			(rc = bc_alloc(g, &b.kstart, 2 * (size_t) kBcMaxLevels + 1)) || (rc = bc_alloc(g, &b.ctl, 1))) {
+			(rc = bc_alloc(g, &b.kstart, kBcClasses * (size_t) kBcMaxLevels + 1)) ||
+			(rc = bc_alloc(g, &b.partial, bc_partial_capacity(g->m))) || (rc = bc_alloc(g, &b.ctl, 1))) {
 		release_bc(g);
 		return rc;
 	}
@@ -918,12 +920,13 @@ int bc_enqueue(bfs_graph *g, uint32_t source, uint32_t *sigma, float *delta, flo
 	a.num_steps = &r.stats->num_steps;
 	a.bfs_status = &r.stats->status;
 	a.sigma = sigma ? sigma : b.sigma;
-	a.dacc = b.dacc;
+	a.lvx = b.lvx;
 	a.delta = delta ? delta : b.delta;
 	a.acc = acc;
 	a.order = b.order;
 	a.cnt = b.cnt;
 	a.kstart = b.kstart;
+	a.partial = b.partial;
 	a.ctl = b.ctl;
 	if ((rc = bc_launch(a, g->num_sms, st, &b.grid))) return rc;
 	if (cudaEventRecord(b.e2, st) != cudaSuccess) return BFS_ECUDA;
@@ -958,6 +961,15 @@ int bc_collect(bfs_graph *g, bfs_bc_stats *out) {
 		if (c.t[1] && c.t[2] >= c.t[1]) s.paths_ms = (float) ((c.t[2] - c.t[1]) * 1e-6);
 		if (c.t[2] && c.t[3] >= c.t[2]) s.dependencies_ms = (float) ((c.t[3] - c.t[2]) * 1e-6);
 		s.grid_ctas = (uint32_t) b.grid;
+		for (uint32_t d = 0; d <= c.depth && d < BFS_BC_TRACE_LEVELS; ++d) {
+			s.level_vertices[d] = c.lv_vertices[d];
+			s.level_big[d] = c.lv_big[d];
+			s.level_medium[d] = c.lv_medium[d];
+			const unsigned long long f0 = d <= 1 ? c.t[1] : c.t_fwd[d - 1], f1 = c.t_fwd[d];
+			if (d > 0 && f0 && f1 >= f0) s.level_paths_ms[d] = (float) ((f1 - f0) * 1e-6);
+			const unsigned long long r0 = d == c.depth || d + 1 >= BFS_BC_TRACE_LEVELS ? c.t[2] : c.t_rev[d + 1], r1 = c.t_rev[d];
+			if (r0 && r1 >= r0) s.level_dependencies_ms[d] = (float) ((r1 - r0) * 1e-6);
+		}
 		*out = s;
 	}
 	return c.err;
@@ -1512,9 +1524,9 @@ int bfs_bc_accumulate(bfs_graph *g, const uint32_t *sources, uint32_t num_source
 		return BFS_ECUDA;
 	}
 	bfs_bc_stats total{};
+	bfs_bc_stats one{};
 	for (uint32_t i = 0; i < num_sources && rc == BFS_OK; ++i) {
 		rc = bc_enqueue(g, sources[i], nullptr, nullptr, b.acc, 0);
-		bfs_bc_stats one{};
 		if (rc == BFS_OK) rc = bc_collect(g, &one);
 		if (rc == BFS_OK) {
 			total.depth = std::max(total.depth, one.depth);
@@ -1535,6 +1547,11 @@ int bfs_bc_accumulate(bfs_graph *g, const uint32_t *sources, uint32_t num_source
 	if (rc) return rc;
 	total.device_ms = ms;
 	total.grid_ctas = (uint32_t) b.grid;
+	std::memcpy(total.level_paths_ms, one.level_paths_ms, sizeof(one.level_paths_ms));
+	std::memcpy(total.level_dependencies_ms, one.level_dependencies_ms, sizeof(one.level_dependencies_ms));
+	std::memcpy(total.level_vertices, one.level_vertices, sizeof(one.level_vertices));
+	std::memcpy(total.level_big, one.level_big, sizeof(one.level_big));
+	std::memcpy(total.level_medium, one.level_medium, sizeof(one.level_medium));
 	if (stats) *stats = total;
 	if (cudaMemcpy(centrality, b.acc, sizeof(float) * g->n, cudaMemcpyDeviceToHost) != cudaSuccess) return BFS_ECUDA;
 	return BFS_OK;

@@ -47,6 +47,8 @@ struct BcShared {
 	unsigned long long e[kBcWarps];
 	uint32_t scan[kBcWarps];
 	uint32_t total;
+	uint32_t chunk_beg, chunk_end;
+	uint32_t cpre[kBcSmemBig + 1];   // chunk prefix of the level's big vertices
 };
 __device__ __shared__ BcShared bsh;
 
@@ -89,10 +91,8 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t *total)
 	return r;
 }
 
-__device__ __forceinline__ float ld_cg_f(const float *p) { return __ldcg(p); }
-
-// Sort key of a vertex: 2*level + (small ? 1 : 0); -1 for unreached and
-// out-of-range ids.
+// Sort key of a vertex: 3*level + class (0 big, 1 medium, 2 small by the
+// larger of its in- and out-degree); -1 for unreached and out-of-range ids.
 __device__ __forceinline__ int vertex_key(const BcArgs &a, uint64_t v, uint32_t depth, int *bad) {
 	if (v >= a.n) return -1;
 	const int lv = a.level[v];
@@ -100,40 +100,128 @@ __device__ __forceinline__ int vertex_key(const BcArgs &a, uint64_t v, uint32_t 
 	if ((uint32_t) lv > depth) { *bad = 1; return -1; }
 	const uint32_t od = a.row_off[v + 1] - a.row_off[v];
 	const uint32_t id = a.in_off[v + 1] - a.in_off[v];
-	return 2 * lv + ((od > kBcBig || id > kBcBig) ? 0 : 1);
+	const uint32_t dmax = od > id ? od : id;
+	return (int) kBcClasses * lv + (dmax > kBcBig ? 0 : (dmax > kBcMedium ? 1 : 2));
 }
 
 template <bool kFwd> struct Dir {
 	using T = typename std::conditional<kFwd, uint32_t, float>::type;
+	static __device__ __forceinline__ uint32_t bits(T x);
 	static __device__ __forceinline__ const uint32_t *off(const BcArgs &a) { return kFwd ? a.in_off : a.row_off; }
 	static __device__ __forceinline__ const uint32_t *adj(const BcArgs &a) { return kFwd ? a.in_src : a.col; }
-	static __device__ __forceinline__ T value(const BcArgs &a, uint32_t u);
+	static __device__ __forceinline__ T value(uint32_t bits);
 };
-template <> __device__ __forceinline__ uint32_t Dir<true>::value(const BcArgs &a, uint32_t u) { return ld_cg(a.sigma + u); }
-template <> __device__ __forceinline__ float Dir<false>::value(const BcArgs &a, uint32_t u) { return ld_cg_f(a.dacc + u); }
+template <> __device__ __forceinline__ uint32_t Dir<true>::value(uint32_t bits) { return bits; }
+template <> __device__ __forceinline__ float Dir<false>::value(uint32_t bits) { return __uint_as_float(bits); }
+template <> __device__ __forceinline__ uint32_t Dir<true>::bits(uint32_t x) { return x; }
+template <> __device__ __forceinline__ uint32_t Dir<false>::bits(float x) { return __float_as_uint(x); }
 
-// Sum over the edge list of one vertex by the whole CTA (result in warp 0).
+// {level, value} of a neighbour in one 8-byte load (written earlier in this launch: via L2)
+__device__ __forceinline__ uint2 ld_lvx(const uint2 *p) { return __ldcg(p); }
+
+// Sum over the edges [beg, end) of one vertex by the whole CTA (result in warp 0).
 template <bool kFwd>
-__device__ __forceinline__ typename Dir<kFwd>::T cta_vertex_sum(const BcArgs &a, uint32_t v, int target) {
+__device__ __forceinline__ typename Dir<kFwd>::T cta_range_sum(const BcArgs &a, uint64_t beg, uint64_t end, int target) {
 	using T = typename Dir<kFwd>::T;
 	const uint32_t *adj = Dir<kFwd>::adj(a);
-	const uint64_t beg = Dir<kFwd>::off(a)[v], end = Dir<kFwd>::off(a)[v + 1];
 	T s = T(0);
 	for (uint64_t e = beg + threadIdx.x; e < end; e += (uint64_t) kBcThreads * kBcUnroll) {
 		uint32_t nb[kBcUnroll];
-		int lv[kBcUnroll];
+		uint2 lx[kBcUnroll];
 #pragma unroll
 		for (int k = 0; k < kBcUnroll; ++k) {
 			const uint64_t ee = e + (uint64_t) k * kBcThreads;
 			nb[k] = ee < end ? __ldg(adj + ee) : 0xFFFFFFFFu;
 		}
 #pragma unroll
-		for (int k = 0; k < kBcUnroll; ++k) lv[k] = nb[k] != 0xFFFFFFFFu ? __ldg(a.level + nb[k]) : -2;
+		for (int k = 0; k < kBcUnroll; ++k) lx[k] = nb[k] != 0xFFFFFFFFu ? ld_lvx(a.lvx + nb[k]) : make_uint2(0xFFFFFFFEu, 0u);
 #pragma unroll
 		for (int k = 0; k < kBcUnroll; ++k)
-			if (lv[k] == target) s += Dir<kFwd>::value(a, nb[k]);
+			if ((int) lx[k].x == target) s += Dir<kFwd>::value(lx[k].y);
 	}
 	return block_sum(s);
+}
+
+template <bool kFwd>
+__device__ __forceinline__ typename Dir<kFwd>::T cta_vertex_sum(const BcArgs &a, uint32_t v, int target) {
+	return cta_range_sum<kFwd>(a, Dir<kFwd>::off(a)[v], Dir<kFwd>::off(a)[v + 1], target);
+}
+
+// Big vertices order[bb .. bb+nbig) (nbig <= kBcSmemBig) cut into chunks of
+// kBcChunk edges: every CTA builds the same chunk prefix in shared memory,
+// then CTA c sums chunks c, c + grid, ... into partial[] (value bits).
+template <bool kFwd>
+__device__ __forceinline__ void big_chunks(const BcArgs &a, uint32_t bb, uint32_t nbig, int target) {
+	const uint32_t *off = Dir<kFwd>::off(a);
+	uint32_t carry = 0;
+	for (uint32_t t0 = 0; t0 < nbig; t0 += kBcThreads) {
+		const uint32_t i = t0 + threadIdx.x;
+		uint32_t c = 0;
+		if (i < nbig) {
+			const uint32_t v = ld_cg(a.order + bb + i);
+			c = (off[v + 1] - off[v] + kBcChunk - 1) / kBcChunk;
+		}
+		uint32_t tot;
+		const uint32_t ex = block_excl_scan(c, &tot);
+		if (i < nbig) bsh.cpre[i] = carry + ex;
+		carry += tot;
+	}
+	if (threadIdx.x == 0) bsh.cpre[nbig] = carry;
+	__syncthreads();
+	for (uint32_t j = blockIdx.x; j < carry; j += gridDim.x) {
+		if (threadIdx.x == 0) {
+			// the largest i with cpre[i] <= j (cpre[nbig] = carry > j)
+			uint32_t lo = 0, hi = nbig;
+			while (lo < hi) {
+				const uint32_t mid = (lo + hi + 1) / 2;
+				if (bsh.cpre[mid] <= j) lo = mid;
+				else hi = mid - 1;
+			}
+			const uint32_t v = ld_cg(a.order + bb + lo);
+			const uint32_t beg = off[v] + (j - bsh.cpre[lo]) * kBcChunk;
+			const uint32_t end = off[v + 1];
+			bsh.chunk_beg = beg;
+			bsh.chunk_end = end - beg > kBcChunk ? beg + kBcChunk : end;
+		}
+		__syncthreads();
+		const uint32_t beg = bsh.chunk_beg, end = bsh.chunk_end;
+		const typename Dir<kFwd>::T s = cta_range_sum<kFwd>(a, beg, end, target);
+		if (threadIdx.x == 0) a.partial[j] = Dir<kFwd>::bits(s);
+	}
+}
+
+// Sum of big vertex i's chunk partials in chunk order, by one warp (all lanes get it).
+template <bool kFwd>
+__device__ __forceinline__ typename Dir<kFwd>::T big_finish_sum(const BcArgs &a, uint32_t i) {
+	using T = typename Dir<kFwd>::T;
+	const uint32_t c0 = bsh.cpre[i], c1 = bsh.cpre[i + 1];
+	T s = T(0);
+	for (uint32_t j = c0 + lane_id(); j < c1; j += 32) s += Dir<kFwd>::value(ld_cg(a.partial + j));
+	return warp_sum(s);
+}
+
+// Sum over the edge list of one vertex by one warp (all lanes get it).
+template <bool kFwd>
+__device__ __forceinline__ typename Dir<kFwd>::T warp_vertex_sum(const BcArgs &a, uint32_t v, int target) {
+	using T = typename Dir<kFwd>::T;
+	const uint32_t *adj = Dir<kFwd>::adj(a);
+	const uint32_t beg = Dir<kFwd>::off(a)[v], end = Dir<kFwd>::off(a)[v + 1];
+	T s = T(0);
+	for (uint32_t e = beg + lane_id(); e < end; e += 32u * kBcUnroll) {
+		uint32_t nb[kBcUnroll];
+		uint2 lx[kBcUnroll];
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k) {
+			const uint32_t ee = e + (uint32_t) k * 32u;
+			nb[k] = ee < end ? __ldg(adj + ee) : 0xFFFFFFFFu;
+		}
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k) lx[k] = nb[k] != 0xFFFFFFFFu ? ld_lvx(a.lvx + nb[k]) : make_uint2(0xFFFFFFFEu, 0u);
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k)
+			if ((int) lx[k].x == target) s += Dir<kFwd>::value(lx[k].y);
+	}
+	return warp_sum(s);
 }
 
 // Sums of the edge lists of 32 vertices order[first .. min(first+32, end))
@@ -157,7 +245,7 @@ __device__ __forceinline__ typename Dir<kFwd>::T warp_group_sum(const BcArgs &a,
 	T acc = T(0);
 	for (uint32_t f0 = 0; f0 < total; f0 += 32u * kBcUnroll) {
 		uint32_t nb[kBcUnroll], own[kBcUnroll];
-		int lv[kBcUnroll];
+		uint2 lx[kBcUnroll];
 		T val[kBcUnroll];
 #pragma unroll
 		for (int k = 0; k < kBcUnroll; ++k) {
@@ -176,9 +264,9 @@ __device__ __forceinline__ typename Dir<kFwd>::T warp_group_sum(const BcArgs &a,
 			nb[k] = on ? __ldg(adj + ob + (f - oe)) : 0u;
 		}
 #pragma unroll
-		for (int k = 0; k < kBcUnroll; ++k) lv[k] = own[k] < 32u ? __ldg(a.level + nb[k]) : -2;
+		for (int k = 0; k < kBcUnroll; ++k) lx[k] = own[k] < 32u ? ld_lvx(a.lvx + nb[k]) : make_uint2(0xFFFFFFFEu, 0u);
 #pragma unroll
-		for (int k = 0; k < kBcUnroll; ++k) val[k] = lv[k] == target ? Dir<kFwd>::value(a, nb[k]) : T(0);
+		for (int k = 0; k < kBcUnroll; ++k) val[k] = (int) lx[k].x == target ? Dir<kFwd>::value(lx[k].y) : T(0);
 #pragma unroll
 		for (int k = 0; k < kBcUnroll; ++k) {
 			T x = val[k];
@@ -204,7 +292,7 @@ __device__ __forceinline__ void finish_dependency(const BcArgs &a, uint32_t v, f
 	const uint32_t sg = ld_cg(a.sigma + v);
 	const float inv = sg ? 1.0f / (float) (int) sg : 0.0f;
 	const float dv = sum + inv;
-	a.dacc[v] = dv;
+	a.lvx[v].y = __float_as_uint(dv);
 	const float del = inv != 0.0f ? (dv - inv) / inv : 0.0f;
 	a.delta[v] = del;
 	if (a.acc && v != a.source) a.acc[v] += del;
@@ -225,7 +313,7 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 		return;
 	}
 	const uint32_t depth = steps - 1;
-	const uint32_t K = 2u * steps;
+	const uint32_t K = kBcClasses * steps;
 	const uint64_t W32 = ((uint64_t) a.n + 31) / 32;
 	uint64_t q = (K * W32 + kBcCntCap - 1) / kBcCntCap;
 	if (q == 0) q = 1;
@@ -250,6 +338,7 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 			if (v < a.n) {
 				a.sigma[v] = v == a.source ? 1u : 0u;
 				a.delta[v] = 0.0f;
+				a.lvx[v] = make_uint2((uint32_t) a.level[v], v == a.source ? 1u : 0u);
 			}
 			if (key >= 0) {
 				++my_reached;
@@ -331,48 +420,110 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 	// ---- 2. path counts, level by level ----------------------------------
 	unsigned long long e_fwd = 0, e_rev = 0;
 	for (uint32_t d = 1; d <= depth; ++d) {
-		const uint32_t bb = ld_cg(a.kstart + 2 * d), be = ld_cg(a.kstart + 2 * d + 1), se = ld_cg(a.kstart + 2 * d + 2);
-		for (uint32_t i = bb + blockIdx.x; i < be; i += gridDim.x) {
+		const uint32_t bb = ld_cg(a.kstart + kBcClasses * d), be = ld_cg(a.kstart + kBcClasses * d + 1);
+		const uint32_t me = ld_cg(a.kstart + kBcClasses * d + 2), se = ld_cg(a.kstart + kBcClasses * d + 3);
+		const uint32_t nbig = be - bb;
+		if (nbig > 0 && nbig <= kBcSmemBig) {
+			big_chunks<true>(a, bb, nbig, (int) d - 1);
+			if (!grid_barrier(ctl->bar, &ctl->err)) return;
+			for (uint32_t i = gw; i < nbig; i += tw) {
+				const uint32_t v = ld_cg(a.order + bb + i);
+				const uint32_t s = big_finish_sum<true>(a, i);
+				if (lane == 0) {
+					a.sigma[v] = s;
+					a.lvx[v].y = s;
+					e_fwd += a.in_off[v + 1] - a.in_off[v];
+				}
+			}
+		} else {
+			for (uint32_t i = bb + blockIdx.x; i < be; i += gridDim.x) {
+				const uint32_t v = ld_cg(a.order + i);
+				const uint32_t s = cta_vertex_sum<true>(a, v, (int) d - 1);
+				if (threadIdx.x == 0) {
+					a.sigma[v] = s;
+					a.lvx[v].y = s;
+					e_fwd += a.in_off[v + 1] - a.in_off[v];
+				}
+			}
+		}
+		for (uint32_t i = be + (tw - 1 - gw); i < me; i += tw) {
 			const uint32_t v = ld_cg(a.order + i);
-			const uint32_t s = cta_vertex_sum<true>(a, v, (int) d - 1);
-			if (threadIdx.x == 0) {
+			const uint32_t s = warp_vertex_sum<true>(a, v, (int) d - 1);
+			if (lane == 0) {
 				a.sigma[v] = s;
+				a.lvx[v].y = s;
 				e_fwd += a.in_off[v + 1] - a.in_off[v];
 			}
 		}
-		const uint32_t groups = (se - be + 31) / 32;
-		for (uint32_t grp = tw - 1 - gw; grp < groups; grp += tw) {
-			const uint32_t idx = be + grp * 32 + lane;
+		const uint32_t groups = (se - me + 31) / 32;
+		for (uint32_t grp = gw; grp < groups; grp += tw) {
+			const uint32_t idx = me + grp * 32 + lane;
 			const bool valid = idx < se;
 			const uint32_t v = valid ? ld_cg(a.order + idx) : 0u;
 			const uint32_t s = warp_group_sum<true>(a, v, valid, (int) d - 1, false, &e_fwd);
-			if (valid) a.sigma[v] = s;
+			if (valid) {
+				a.sigma[v] = s;
+				a.lvx[v].y = s;
+			}
 		}
 		if (!grid_barrier(ctl->bar, &ctl->err)) return;
+		if (blockIdx.x == 0 && threadIdx.x == 0 && d < kBcTraceLevels) ctl->t_fwd[d] = global_timer_ns();
 	}
 	if (blockIdx.x == 0 && threadIdx.x == 0) ctl->t[2] = global_timer_ns();
 
 	// ---- 3. dependency sums, deepest level first ---------------------------
 	for (int d = (int) depth; d >= 0; --d) {
 		const bool deepest = (uint32_t) d == depth;
-		const uint32_t bb = ld_cg(a.kstart + 2 * d), be = ld_cg(a.kstart + 2 * d + 1), se = ld_cg(a.kstart + 2 * d + 2);
-		for (uint32_t i = bb + blockIdx.x; i < be; i += gridDim.x) {
+		const uint32_t bb = ld_cg(a.kstart + kBcClasses * d), be = ld_cg(a.kstart + kBcClasses * d + 1);
+		const uint32_t me = ld_cg(a.kstart + kBcClasses * d + 2), se = ld_cg(a.kstart + kBcClasses * d + 3);
+		const uint32_t nbig = be - bb;
+		if (deepest) {
+			for (uint32_t i = gw; i < nbig; i += tw)
+				if (lane == 0) finish_dependency(a, ld_cg(a.order + bb + i), 0.0f);
+		} else if (nbig > 0 && nbig <= kBcSmemBig) {
+			big_chunks<false>(a, bb, nbig, d + 1);
+			if (!grid_barrier(ctl->bar, &ctl->err)) return;
+			for (uint32_t i = gw; i < nbig; i += tw) {
+				const uint32_t v = ld_cg(a.order + bb + i);
+				const float s = big_finish_sum<false>(a, i);
+				if (lane == 0) {
+					finish_dependency(a, v, s);
+					e_rev += a.row_off[v + 1] - a.row_off[v];
+				}
+			}
+		} else {
+			for (uint32_t i = bb + blockIdx.x; i < be; i += gridDim.x) {
+				const uint32_t v = ld_cg(a.order + i);
+				const float s = cta_vertex_sum<false>(a, v, d + 1);
+				if (threadIdx.x == 0) {
+					finish_dependency(a, v, s);
+					e_rev += a.row_off[v + 1] - a.row_off[v];
+				}
+			}
+		}
+		for (uint32_t i = be + (tw - 1 - gw); i < me; i += tw) {
 			const uint32_t v = ld_cg(a.order + i);
-			const float s = deepest ? 0.0f : cta_vertex_sum<false>(a, v, d + 1);
-			if (threadIdx.x == 0) {
+			const float s = deepest ? 0.0f : warp_vertex_sum<false>(a, v, d + 1);
+			if (lane == 0) {
 				finish_dependency(a, v, s);
 				if (!deepest) e_rev += a.row_off[v + 1] - a.row_off[v];
 			}
 		}
-		const uint32_t groups = (se - be + 31) / 32;
-		for (uint32_t grp = tw - 1 - gw; grp < groups; grp += tw) {
-			const uint32_t idx = be + grp * 32 + lane;
+		const uint32_t groups = (se - me + 31) / 32;
+		for (uint32_t grp = gw; grp < groups; grp += tw) {
+			const uint32_t idx = me + grp * 32 + lane;
 			const bool valid = idx < se;
 			const uint32_t v = valid ? ld_cg(a.order + idx) : 0u;
 			const float s = warp_group_sum<false>(a, v, valid, d + 1, deepest, &e_rev);
 			if (valid) finish_dependency(a, v, s);
 		}
 		if (d > 0 && !grid_barrier(ctl->bar, &ctl->err)) return;
+		if (blockIdx.x == 0 && threadIdx.x == 0 && (uint32_t) d < kBcTraceLevels) {
+			ctl->t_rev[d] = global_timer_ns();
+			ctl->lv_vertices[d] = se - bb;
+			ctl->lv_big[d] = be - bb;
+			ctl->lv_medium[d] = me - be;
+		}
 	}
 	{
 		const unsigned long long ef = block_sum(e_fwd);

@@ -11,7 +11,17 @@ namespace bfsg {
 constexpr uint32_t kBcMaxLevels = 1u << 20;   // deeper traversals are refused (BFS_EUNSUPPORTED)
 constexpr uint32_t kBcCntCap = 1u << 22;      // (level key, vertex range) counters of the level sort
 constexpr uint32_t kBcBig = 1024;             // in- or out-degree above which a whole CTA reduces a vertex
+constexpr uint32_t kBcMedium = 32;            // above this (and up to kBcBig) one warp reduces a vertex;
+                                              // at most this, a warp takes 32 vertices at once
+constexpr uint32_t kBcClasses = 3;            // sort keys per level: big, medium, small
 constexpr uint32_t kBcMaxGrid = 1024;
+constexpr uint32_t kBcTraceLevels = 64;       // per-level timers and sizes kept for the first levels
+constexpr uint32_t kBcChunk = 2048;           // edges of a big vertex one CTA sums in one pass
+constexpr uint32_t kBcSmemBig = 4096;         // big vertices of a level whose chunk list every CTA keeps in shared
+                                              // memory; a level with more gives each big vertex one CTA
+
+// Chunk partial sums a graph of m edges can need in one level.
+inline size_t bc_partial_capacity(uint64_t m) { return kBcSmemBig + m / kBcChunk + 2; }
 
 struct BcControl {
 	unsigned bar[2];            // grid barrier
@@ -23,6 +33,11 @@ struct BcControl {
 	unsigned long long edges_rev;      // out-edges read by the dependency sweep
 	unsigned long long edges_reached;  // sum of out-degrees of reached vertices
 	unsigned long long t[4];           // global timer: start, sorted, path counts done, end
+	unsigned long long t_fwd[kBcTraceLevels];  // end of the path counts of level d
+	unsigned long long t_rev[kBcTraceLevels];  // end of the dependency sums of level d
+	uint32_t lv_vertices[kBcTraceLevels];      // vertices of level d
+	uint32_t lv_big[kBcTraceLevels];           // of which reduced by a whole CTA
+	uint32_t lv_medium[kBcTraceLevels];        // of which reduced by one warp
 	uint32_t blk[kBcMaxGrid];          // per-CTA totals of the counter scan
 };
 
@@ -34,12 +49,14 @@ struct BcArgs {
 	const uint32_t *num_steps;         // the traversal's step count (deepest level + 1)
 	const int *bfs_status;             // the traversal's status word
 	uint32_t *sigma;                   // [n] shortest-path counts (mod 2^32)
-	float *dacc;                       // [n] (1 + dependency) / paths, the reverse sweep's sums
+	uint2 *lvx;                        // [n] {level, value}: the path count in the forward sweep, then the
+	                                   // bits of the float sum (1 + dependency) / paths in the reverse one
 	float *delta;                      // [n] dependencies (output)
 	float *acc;                        // [n] or null: += dependency for every vertex but the source
-	uint32_t *order;                   // [n] reached vertices sorted by (level, big first)
+	uint32_t *order;                   // [n] reached vertices sorted by (level, class: big, medium, small)
 	uint32_t *cnt;                     // [kBcCntCap] counters of the level sort
-	uint32_t *kstart;                  // [2 * kBcMaxLevels + 1] start of every key in `order`
+	uint32_t *kstart;                  // [kBcClasses * kBcMaxLevels + 1] start of every key in `order`
+	uint32_t *partial;                 // [bc_partial_capacity(m)] chunk sums of big vertices (value bits)
 	BcControl *ctl;
 };
 

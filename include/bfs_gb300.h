@@ -452,6 +452,7 @@ int bfs_graph_bfs_order(bfs_graph *g, uint32_t source, uint32_t *vertex_map);
  * 0; the source gets the number of other vertices it reaches (the reference
  * computes it the same way).  Sums are taken in a fixed order: repeated runs
  * give identical bits.  Traversals deeper than 2^20 levels: BFS_EUNSUPPORTED. */
+#define BFS_BC_TRACE_LEVELS 64
 typedef struct bfs_bc_stats {
 	uint32_t num_sources;     /* dependency runs counted here */
 	uint32_t depth;           /* deepest level (the largest over the runs) */
@@ -466,6 +467,15 @@ typedef struct bfs_bc_stats {
 	float paths_ms;
 	float dependencies_ms;
 	uint32_t grid_ctas;
+	/* the (last) run, per level d < BFS_BC_TRACE_LEVELS: path-count and
+	 * dependency times, vertices, and of those the ones whose in- or
+	 * out-degree is above 1024 (reduced by whole CTAs) or above 32 (one warp
+	 * each; the rest are taken 32 to a warp) */
+	float level_paths_ms[BFS_BC_TRACE_LEVELS];
+	float level_dependencies_ms[BFS_BC_TRACE_LEVELS];
+	uint32_t level_vertices[BFS_BC_TRACE_LEVELS];
+	uint32_t level_big[BFS_BC_TRACE_LEVELS];
+	uint32_t level_medium[BFS_BC_TRACE_LEVELS];
 } bfs_bc_stats;
 
 /* dependencies[N] and num_paths[N] are HOST buffers (either may be NULL). */

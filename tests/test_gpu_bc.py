@@ -86,6 +86,27 @@ def test_bc_hubs_take_the_cta_path(native, oracle):
             _check_source(oracle, arr, g, s)
 
 
+def test_bc_many_big_vertices_in_one_level(native, oracle):
+    """A level with more than 4096 big vertices (one CTA each) followed by a
+    level of 1800 big vertices (chunked over the grid)."""
+    import bfs_simd_benchmarks_gb300 as B
+    rng = np.random.default_rng(11)
+    first, pool = 4200, 1800
+    n = 1 + first + pool
+    src = [np.zeros(first, np.uint32)]
+    dst = [np.arange(1, first + 1, dtype=np.uint32)]
+    for v in range(1, first + 1):
+        t = rng.choice(pool, 1100, replace=False).astype(np.uint32) + first + 1
+        src.append(np.full(1100, v, np.uint32))
+        dst.append(t)
+    src = np.concatenate(src)
+    dst = np.concatenate(dst)
+    arr = oracle.arrays_from_edges(n, src, dst, 512, 8)
+    with B.Graph.from_edges(n, src, dst, 512, 8) as g:
+        _, _, st = _check_source(oracle, arr, g, 0)
+        assert st["level_big"][1] == first and st["level_big"][2] == pool
+
+
 def test_bc_deep_chain(native, oracle):
     """5000 levels: the level sort's keys far beyond one per warp range."""
     import bfs_simd_benchmarks_gb300 as B
