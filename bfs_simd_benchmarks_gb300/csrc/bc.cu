@@ -91,8 +91,9 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t *total)
 	return r;
 }
 
-// Sort key of a vertex: 3*level + class (0 big, 1 medium, 2 small by the
-// larger of its in- and out-degree); -1 for unreached and out-of-range ids.
+// Sort key of a vertex: kBcClasses*level + class by the larger of its in- and
+// out-degree d (0: d > 1024; 1..5: d in (512, 1024], (256, 512], (128, 256],
+// (64, 128], (32, 64]; 6: d <= 32); -1 for unreached and out-of-range ids.
 __device__ __forceinline__ int vertex_key(const BcArgs &a, uint64_t v, uint32_t depth, int *bad) {
 	if (v >= a.n) return -1;
 	const int lv = a.level[v];
@@ -101,7 +102,10 @@ __device__ __forceinline__ int vertex_key(const BcArgs &a, uint64_t v, uint32_t 
 	const uint32_t od = a.row_off[v + 1] - a.row_off[v];
 	const uint32_t id = a.in_off[v + 1] - a.in_off[v];
 	const uint32_t dmax = od > id ? od : id;
-	return (int) kBcClasses * lv + (dmax > kBcBig ? 0 : (dmax > kBcMedium ? 1 : 2));
+	int cls = (int) kBcClasses - 1;
+	if (dmax > kBcBig) cls = 0;
+	else if (dmax > kBcMedium) cls = 1 + (31 - __clz(kBcBig - 1)) - (31 - __clz(dmax - 1));
+	return (int) kBcClasses * lv + cls;
 }
 
 template <bool kFwd> struct Dir {
@@ -222,6 +226,38 @@ __device__ __forceinline__ typename Dir<kFwd>::T warp_vertex_sum(const BcArgs &a
 			if ((int) lx[k].x == target) s += Dir<kFwd>::value(lx[k].y);
 	}
 	return warp_sum(s);
+}
+
+// Sum over the edge list of one vertex by a half-warp (16 lanes); v_ok false
+// gives 0.  Both halves call it together (the reduction shuffles the warp).
+template <bool kFwd>
+__device__ __forceinline__ typename Dir<kFwd>::T half_vertex_sum(const BcArgs &a, uint32_t v, bool v_ok, int target) {
+	using T = typename Dir<kFwd>::T;
+	const uint32_t *adj = Dir<kFwd>::adj(a);
+	const uint32_t hl = lane_id() & 15u;
+	uint32_t beg = 0, end = 0;
+	if (v_ok) {
+		beg = Dir<kFwd>::off(a)[v];
+		end = Dir<kFwd>::off(a)[v + 1];
+	}
+	T s = T(0);
+	for (uint32_t e = beg + hl; e < end; e += 16u * kBcUnroll) {
+		uint32_t nb[kBcUnroll];
+		uint2 lx[kBcUnroll];
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k) {
+			const uint32_t ee = e + (uint32_t) k * 16u;
+			nb[k] = ee < end ? __ldg(adj + ee) : 0xFFFFFFFFu;
+		}
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k) lx[k] = nb[k] != 0xFFFFFFFFu ? ld_lvx(a.lvx + nb[k]) : make_uint2(0xFFFFFFFEu, 0u);
+#pragma unroll
+		for (int k = 0; k < kBcUnroll; ++k)
+			if ((int) lx[k].x == target) s += Dir<kFwd>::value(lx[k].y);
+	}
+#pragma unroll
+	for (int d = 8; d > 0; d >>= 1) s += __shfl_xor_sync(kFull, s, d);
+	return s;
 }
 
 // Sums of the edge lists of 32 vertices order[first .. min(first+32, end))
@@ -421,7 +457,8 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 	unsigned long long e_fwd = 0, e_rev = 0;
 	for (uint32_t d = 1; d <= depth; ++d) {
 		const uint32_t bb = ld_cg(a.kstart + kBcClasses * d), be = ld_cg(a.kstart + kBcClasses * d + 1);
-		const uint32_t me = ld_cg(a.kstart + kBcClasses * d + 2), se = ld_cg(a.kstart + kBcClasses * d + 3);
+		const uint32_t me = ld_cg(a.kstart + kBcClasses * d + kBcClasses - 1);
+		const uint32_t se = ld_cg(a.kstart + kBcClasses * d + kBcClasses);
 		const uint32_t nbig = be - bb;
 		if (nbig > 0 && nbig <= kBcSmemBig) {
 			big_chunks<true>(a, bb, nbig, (int) d - 1);
@@ -446,10 +483,12 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 				}
 			}
 		}
-		for (uint32_t i = be + (tw - 1 - gw); i < me; i += tw) {
-			const uint32_t v = ld_cg(a.order + i);
-			const uint32_t s = warp_vertex_sum<true>(a, v, (int) d - 1);
-			if (lane == 0) {
+		for (uint32_t i0 = be + 2 * (tw - 1 - gw); i0 < me; i0 += 2 * tw) {
+			const uint32_t i = i0 + (lane >> 4);
+			const bool ok = i < me;
+			const uint32_t v = ok ? ld_cg(a.order + i) : 0u;
+			const uint32_t s = half_vertex_sum<true>(a, v, ok, (int) d - 1);
+			if (ok && (lane & 15u) == 0) {
 				a.sigma[v] = s;
 				a.lvx[v].y = s;
 				e_fwd += a.in_off[v + 1] - a.in_off[v];
@@ -475,7 +514,8 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 	for (int d = (int) depth; d >= 0; --d) {
 		const bool deepest = (uint32_t) d == depth;
 		const uint32_t bb = ld_cg(a.kstart + kBcClasses * d), be = ld_cg(a.kstart + kBcClasses * d + 1);
-		const uint32_t me = ld_cg(a.kstart + kBcClasses * d + 2), se = ld_cg(a.kstart + kBcClasses * d + 3);
+		const uint32_t me = ld_cg(a.kstart + kBcClasses * d + kBcClasses - 1);
+		const uint32_t se = ld_cg(a.kstart + kBcClasses * d + kBcClasses);
 		const uint32_t nbig = be - bb;
 		if (deepest) {
 			for (uint32_t i = gw; i < nbig; i += tw)
@@ -501,10 +541,12 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 				}
 			}
 		}
-		for (uint32_t i = be + (tw - 1 - gw); i < me; i += tw) {
-			const uint32_t v = ld_cg(a.order + i);
-			const float s = deepest ? 0.0f : warp_vertex_sum<false>(a, v, d + 1);
-			if (lane == 0) {
+		for (uint32_t i0 = be + 2 * (tw - 1 - gw); i0 < me; i0 += 2 * tw) {
+			const uint32_t i = i0 + (lane >> 4);
+			const bool ok = i < me;
+			const uint32_t v = ok ? ld_cg(a.order + i) : 0u;
+			const float s = half_vertex_sum<false>(a, v, ok && !deepest, d + 1);
+			if (ok && (lane & 15u) == 0) {
 				finish_dependency(a, v, s);
 				if (!deepest) e_rev += a.row_off[v + 1] - a.row_off[v];
 			}

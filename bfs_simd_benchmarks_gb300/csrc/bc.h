@@ -8,14 +8,17 @@
 
 namespace bfsg {
 
-constexpr uint32_t kBcMaxLevels = 1u << 20;   // deeper traversals are refused (BFS_EUNSUPPORTED)
+constexpr uint32_t kBcMaxLevels = 1u << 19;   // deeper traversals are refused (BFS_EUNSUPPORTED)
 constexpr uint32_t kBcCntCap = 1u << 22;      // (level key, vertex range) counters of the level sort
 constexpr uint32_t kBcBig = 1024;             // in- or out-degree above which a whole CTA reduces a vertex
 constexpr uint32_t kBcMedium = 32;            // above this (and up to kBcBig) one warp reduces a vertex;
                                               // at most this, a warp takes 32 vertices at once
-constexpr uint32_t kBcClasses = 3;            // sort keys per level: big, medium, small
+constexpr uint32_t kBcClasses = 7;            // sort keys per level: big, five medium degree bands
+                                              // (highest first, so that warps dealt medium vertices in
+                                              // turn get similar work), small
 constexpr uint32_t kBcMaxGrid = 1024;
 constexpr uint32_t kBcTraceLevels = 64;       // per-level timers and sizes kept for the first levels
+static_assert(kBcClasses * kBcMaxLevels <= kBcCntCap, "every sort key needs a counter");
 constexpr uint32_t kBcChunk = 2048;           // edges of a big vertex one CTA sums in one pass
 constexpr uint32_t kBcSmemBig = 4096;         // big vertices of a level whose chunk list every CTA keeps in shared
                                               // memory; a level with more gives each big vertex one CTA

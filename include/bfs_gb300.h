@@ -451,7 +451,7 @@ int bfs_graph_bfs_order(bfs_graph *g, uint32_t source, uint32_t *vertex_map);
  * from the deepest, result (sum - inverse) / inverse.  Unreached vertices get
  * 0; the source gets the number of other vertices it reaches (the reference
  * computes it the same way).  Sums are taken in a fixed order: repeated runs
- * give identical bits.  Traversals deeper than 2^20 levels: BFS_EUNSUPPORTED. */
+ * give identical bits.  Traversals deeper than 2^19 levels: BFS_EUNSUPPORTED. */
 #define BFS_BC_TRACE_LEVELS 64
 typedef struct bfs_bc_stats {
 	uint32_t num_sources;     /* dependency runs counted here */
