@@ -19,7 +19,7 @@ constexpr uint32_t kBcClasses = 7;            // sort keys per level: big, five 
 constexpr uint32_t kBcMaxGrid = 1024;
 constexpr uint32_t kBcTraceLevels = 64;       // per-level timers and sizes kept for the first levels
 static_assert(kBcClasses * kBcMaxLevels <= kBcCntCap, "every sort key needs a counter");
-constexpr uint32_t kBcChunk = 2048;           // edges of a big vertex one CTA sums in one pass
+constexpr uint32_t kBcChunk = 4096;           // edges of a big vertex one CTA sums as one task
 constexpr uint32_t kBcSmemBig = 4096;         // big vertices of a level whose chunk list every CTA keeps in shared
                                               // memory; a level with more gives each big vertex one CTA
 
