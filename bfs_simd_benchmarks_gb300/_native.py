@@ -75,6 +75,7 @@ class Options(C.Structure):
         ("batch_budget_mb", C.c_uint32),
         ("batch_single_max", C.c_uint32),
         ("batch_push_div", C.c_uint32),
+        ("bc_level_bytes", C.c_uint32),
     ]
 
 

@@ -85,8 +85,10 @@ struct bfs_graph {
 	// betweenness state, allocated by the first bfs_bc_* call
 	struct Bc {
 		uint32_t *sigma = nullptr, *order = nullptr, *cnt = nullptr, *kstart = nullptr, *partial = nullptr;
+		uint32_t *cpre = nullptr;
 		float *delta = nullptr, *acc = nullptr;
 		uint2 *lvx = nullptr;
+		uint8_t *lv8 = nullptr;
 		BcControl *ctl = nullptr;
 		BcControl *h_ctl = nullptr;  // pinned
 		cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
@@ -872,10 +874,11 @@ int bc_prepare(bfs_graph *g) {
 	if (b.ctl) return BFS_OK;
 	int rc;
 	if ((rc = bc_alloc(g, &b.sigma, g->n)) || (rc = bc_alloc(g, &b.order, g->n)) ||
-			(rc = bc_alloc(g, &b.lvx, g->n)) || (rc = bc_alloc(g, &b.delta, g->n)) ||
+			(rc = bc_alloc(g, &b.lvx, g->n)) || (rc = bc_alloc(g, &b.lv8, g->n)) || (rc = bc_alloc(g, &b.delta, g->n)) ||
 			(rc = bc_alloc(g, &b.acc, g->n)) || (rc = bc_alloc(g, &b.cnt, kBcCntCap)) ||
 			(rc = bc_alloc(g, &b.kstart, kBcClasses * (size_t) kBcMaxLevels + 1)) ||
-			(rc = bc_alloc(g, &b.partial, bc_partial_capacity(g->m))) || (rc = bc_alloc(g, &b.ctl, 1))) {
+			(rc = bc_alloc(g, &b.partial, bc_partial_capacity(g->n, g->m))) ||
+			(rc = bc_alloc(g, &b.cpre, (size_t) g->n + 1)) || (rc = bc_alloc(g, &b.ctl, 1))) {
 		release_bc(g);
 		return rc;
 	}
@@ -921,12 +924,15 @@ int bc_enqueue(bfs_graph *g, uint32_t source, uint32_t *sigma, float *delta, flo
 	a.bfs_status = &r.stats->status;
 	a.sigma = sigma ? sigma : b.sigma;
 	a.lvx = b.lvx;
+	a.lv8 = b.lv8;
+	a.byte_levels = g->opt.bc_level_bytes == 1 || (g->opt.bc_level_bytes == 0 && g->n >= kBcByteLevelsMinVertices);
 	a.delta = delta ? delta : b.delta;
 	a.acc = acc;
 	a.order = b.order;
 	a.cnt = b.cnt;
 	a.kstart = b.kstart;
 	a.partial = b.partial;
+	a.cpre = b.cpre;
 	a.ctl = b.ctl;
 	if ((rc = bc_launch(a, g->num_sms, st, &b.grid))) return rc;
 	if (cudaEventRecord(b.e2, st) != cudaSuccess) return BFS_ECUDA;
@@ -1338,7 +1344,7 @@ int bfs_set_options(bfs_graph *g, const bfs_options *opt) {
 	if (opt->mode > BFS_MODE_STEPWISE || opt->bottom_up > BFS_BU_STREAM || opt->to_dense_ratio == 0 || opt->to_sparse_ratio == 0 ||
 			opt->warp_max_degree == 0 || opt->cta_max_degree < opt->warp_max_degree || opt->batch_planes == 1 ||
 			opt->batch_planes > kMsMaxLevel + 1 || (opt->batch_planes == 0 && opt->batch_budget_mb == 0) ||
-			opt->batch_push_div == 0)
+			opt->batch_push_div == 0 || opt->bc_level_bytes > 2)
 		return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);
 	g->opt = *opt;

@@ -22,7 +22,9 @@
 //      over out-edges v -> w with level(w) = level(v) + 1; the output is
 //      (D - 1/sigma) / (1/sigma), 0 where sigma is 0 -- the reference's float
 //      formulas, with its signed int -> float conversion of the counts.
-// Per level, big vertices are reduced by a whole CTA each, the rest by warps
+// Per level, the edge lists of big vertices are cut into kBcChunk-edge chunks
+// that CTAs all over the grid sum (partials added in chunk order after a grid
+// barrier), medium vertices are summed by half-warps, and small ones by warps
 // that take 32 vertices and walk their concatenated edge lists 32 edges at a
 // time (owner by a binary search over the warp's degree prefix, segmented
 // shuffle scan per 32 edges).
@@ -123,9 +125,29 @@ template <> __device__ __forceinline__ uint32_t Dir<false>::bits(float x) { retu
 // {level, value} of a neighbour in one 8-byte load (written earlier in this launch: via L2)
 __device__ __forceinline__ uint2 ld_lvx(const uint2 *p) { return __ldcg(p); }
 
+// Level tags and value bits of the neighbours nb[] (0xFFFFFFFF: none): with
+// use8 the byte level first and the value only where it matches `target`,
+// else {level, value} in one 8-byte load.
+template <int U>
+__device__ __forceinline__ void gather_tags(const BcArgs &a, const uint32_t (&nb)[U], uint2 (&lx)[U], bool use8,
+		int target) {
+#pragma unroll
+	for (int k = 0; k < U; ++k) {
+		if (nb[k] == 0xFFFFFFFFu) lx[k] = make_uint2(0xFFFFFFFEu, 0u);
+		else if (use8) lx[k] = make_uint2((uint32_t) ld_cg_u8(a.lv8 + nb[k]), 0u);
+		else lx[k] = ld_lvx(a.lvx + nb[k]);
+	}
+	if (use8) {
+#pragma unroll
+		for (int k = 0; k < U; ++k)
+			if ((int) lx[k].x == target) lx[k].y = ld_cg(reinterpret_cast<const uint32_t *>(a.lvx + nb[k]) + 1);
+	}
+}
+
 // Sum over the edges [beg, end) of one vertex by the whole CTA (result in warp 0).
 template <bool kFwd>
-__device__ __forceinline__ typename Dir<kFwd>::T cta_range_sum(const BcArgs &a, uint64_t beg, uint64_t end, int target) {
+__device__ __forceinline__ typename Dir<kFwd>::T cta_range_sum(const BcArgs &a, uint64_t beg, uint64_t end, int target,
+		bool use8) {
 	using T = typename Dir<kFwd>::T;
 	const uint32_t *adj = Dir<kFwd>::adj(a);
 	T s = T(0);
@@ -137,8 +159,7 @@ __device__ __forceinline__ typename Dir<kFwd>::T cta_range_sum(const BcArgs &a, 
 			const uint64_t ee = e + (uint64_t) k * kBcThreads;
 			nb[k] = ee < end ? __ldg(adj + ee) : 0xFFFFFFFFu;
 		}
-#pragma unroll
-		for (int k = 0; k < kBcUnroll; ++k) lx[k] = nb[k] != 0xFFFFFFFFu ? ld_lvx(a.lvx + nb[k]) : make_uint2(0xFFFFFFFEu, 0u);
+		gather_tags(a, nb, lx, use8, target);
 #pragma unroll
 		for (int k = 0; k < kBcUnroll; ++k)
 			if ((int) lx[k].x == target) s += Dir<kFwd>::value(lx[k].y);
@@ -146,16 +167,12 @@ __device__ __forceinline__ typename Dir<kFwd>::T cta_range_sum(const BcArgs &a, 
 	return block_sum(s);
 }
 
-template <bool kFwd>
-__device__ __forceinline__ typename Dir<kFwd>::T cta_vertex_sum(const BcArgs &a, uint32_t v, int target) {
-	return cta_range_sum<kFwd>(a, Dir<kFwd>::off(a)[v], Dir<kFwd>::off(a)[v + 1], target);
-}
 
 // Big vertices order[bb .. bb+nbig) (nbig <= kBcSmemBig) cut into chunks of
 // kBcChunk edges: every CTA builds the same chunk prefix in shared memory,
 // then CTA c sums chunks c, c + grid, ... into partial[] (value bits).
 template <bool kFwd>
-__device__ __forceinline__ void big_chunks(const BcArgs &a, uint32_t bb, uint32_t nbig, int target) {
+__device__ __forceinline__ void big_chunks(const BcArgs &a, uint32_t bb, uint32_t nbig, int target, bool use8) {
 	const uint32_t *off = Dir<kFwd>::off(a);
 	uint32_t carry = 0;
 	for (uint32_t t0 = 0; t0 < nbig; t0 += kBcThreads) {
@@ -189,49 +206,110 @@ __device__ __forceinline__ void big_chunks(const BcArgs &a, uint32_t bb, uint32_
 		}
 		__syncthreads();
 		const uint32_t beg = bsh.chunk_beg, end = bsh.chunk_end;
-		const typename Dir<kFwd>::T s = cta_range_sum<kFwd>(a, beg, end, target);
+		const typename Dir<kFwd>::T s = cta_range_sum<kFwd>(a, beg, end, target, use8);
 		if (threadIdx.x == 0) a.partial[j] = Dir<kFwd>::bits(s);
 	}
 }
 
-// Sum of big vertex i's chunk partials in chunk order, by one warp (all lanes get it).
+// The same for a level with more than kBcSmemBig big vertices: the chunk
+// prefix is scanned grid-wide into a.cpre (two grid barriers), then CTA c sums
+// the contiguous chunk range [c*per, (c+1)*per).  Returns false when a barrier
+// gave up.
 template <bool kFwd>
-__device__ __forceinline__ typename Dir<kFwd>::T big_finish_sum(const BcArgs &a, uint32_t i) {
-	using T = typename Dir<kFwd>::T;
-	const uint32_t c0 = bsh.cpre[i], c1 = bsh.cpre[i + 1];
-	T s = T(0);
-	for (uint32_t j = c0 + lane_id(); j < c1; j += 32) s += Dir<kFwd>::value(ld_cg(a.partial + j));
-	return warp_sum(s);
+__device__ __forceinline__ bool big_chunks_global(const BcArgs &a, uint32_t bb, uint32_t nbig, int target, bool use8) {
+	const uint32_t *off = Dir<kFwd>::off(a);
+	BcControl *ctl = a.ctl;
+	const uint32_t L = (nbig + gridDim.x - 1) / gridDim.x;
+	const uint32_t lo = blockIdx.x * L < nbig ? blockIdx.x * L : nbig;
+	const uint32_t hi = lo + L < nbig ? lo + L : nbig;
+	{
+		uint32_t s = 0;
+		for (uint32_t i = lo + threadIdx.x; i < hi; i += kBcThreads) {
+			const uint32_t v = ld_cg(a.order + bb + i);
+			s += (off[v + 1] - off[v] + kBcChunk - 1) / kBcChunk;
+		}
+		s = block_sum(s);
+		if (threadIdx.x == 0) ctl->blk[blockIdx.x] = s;
+	}
+	if (!grid_barrier(ctl->bar, &ctl->err)) return false;
+	uint32_t base = 0, total = 0;
+	for (uint32_t c = threadIdx.x; c < gridDim.x; c += kBcThreads) {
+		const uint32_t x = ld_cg(ctl->blk + c);
+		if (c < blockIdx.x) base += x;
+		total += x;
+	}
+	base = block_sum(base);
+	total = block_sum(total);
+	if (threadIdx.x == 0) {
+		bsh.chunk_beg = base;
+		bsh.chunk_end = total;
+	}
+	__syncthreads();
+	base = bsh.chunk_beg;
+	total = bsh.chunk_end;
+	__syncthreads();
+	for (uint32_t t0 = lo; t0 < hi; t0 += kBcThreads) {
+		const uint32_t i = t0 + threadIdx.x;
+		uint32_t c = 0;
+		if (i < hi) {
+			const uint32_t v = ld_cg(a.order + bb + i);
+			c = (off[v + 1] - off[v] + kBcChunk - 1) / kBcChunk;
+		}
+		uint32_t tot;
+		const uint32_t ex = block_excl_scan(c, &tot);
+		if (i < hi) a.cpre[i] = base + ex;
+		base += tot;
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) a.cpre[nbig] = total;
+	if (!grid_barrier(ctl->bar, &ctl->err)) return false;
+	const uint32_t per = (total + gridDim.x - 1) / gridDim.x;
+	const uint32_t j0 = blockIdx.x * per < total ? blockIdx.x * per : total;
+	const uint32_t j1 = j0 + per < total ? j0 + per : total;
+	uint32_t owner = 0;
+	if (j0 < j1 && threadIdx.x == 0) {
+		// the largest i with cpre[i] <= j0 (cpre[nbig] = total > j0)
+		uint32_t l = 0, h = nbig;
+		while (l < h) {
+			const uint32_t mid = (l + h + 1) / 2;
+			if (ld_cg(a.cpre + mid) <= j0) l = mid;
+			else h = mid - 1;
+		}
+		owner = l;
+	}
+	for (uint32_t j = j0; j < j1; ++j) {
+		if (threadIdx.x == 0) {
+			while (ld_cg(a.cpre + owner + 1) <= j) ++owner;
+			const uint32_t v = ld_cg(a.order + bb + owner);
+			const uint32_t beg = off[v] + (j - ld_cg(a.cpre + owner)) * kBcChunk;
+			const uint32_t end = off[v + 1];
+			bsh.chunk_beg = beg;
+			bsh.chunk_end = end - beg > kBcChunk ? beg + kBcChunk : end;
+		}
+		__syncthreads();
+		const uint32_t beg = bsh.chunk_beg, end = bsh.chunk_end;
+		const typename Dir<kFwd>::T s = cta_range_sum<kFwd>(a, beg, end, target, use8);
+		if (threadIdx.x == 0) a.partial[j] = Dir<kFwd>::bits(s);
+	}
+	return true;
 }
 
-// Sum over the edge list of one vertex by one warp (all lanes get it).
+// Sum of big vertex i's chunk partials in chunk order, by one warp (all lanes
+// get it); the chunk prefix is in shared memory (global: in a.cpre).
 template <bool kFwd>
-__device__ __forceinline__ typename Dir<kFwd>::T warp_vertex_sum(const BcArgs &a, uint32_t v, int target) {
+__device__ __forceinline__ typename Dir<kFwd>::T big_finish_sum(const BcArgs &a, uint32_t i, bool global) {
 	using T = typename Dir<kFwd>::T;
-	const uint32_t *adj = Dir<kFwd>::adj(a);
-	const uint32_t beg = Dir<kFwd>::off(a)[v], end = Dir<kFwd>::off(a)[v + 1];
+	const uint32_t c0 = global ? ld_cg(a.cpre + i) : bsh.cpre[i];
+	const uint32_t c1 = global ? ld_cg(a.cpre + i + 1) : bsh.cpre[i + 1];
 	T s = T(0);
-	for (uint32_t e = beg + lane_id(); e < end; e += 32u * kBcUnroll) {
-		uint32_t nb[kBcUnroll];
-		uint2 lx[kBcUnroll];
-#pragma unroll
-		for (int k = 0; k < kBcUnroll; ++k) {
-			const uint32_t ee = e + (uint32_t) k * 32u;
-			nb[k] = ee < end ? __ldg(adj + ee) : 0xFFFFFFFFu;
-		}
-#pragma unroll
-		for (int k = 0; k < kBcUnroll; ++k) lx[k] = nb[k] != 0xFFFFFFFFu ? ld_lvx(a.lvx + nb[k]) : make_uint2(0xFFFFFFFEu, 0u);
-#pragma unroll
-		for (int k = 0; k < kBcUnroll; ++k)
-			if ((int) lx[k].x == target) s += Dir<kFwd>::value(lx[k].y);
-	}
+	for (uint32_t j = c0 + lane_id(); j < c1; j += 32) s += Dir<kFwd>::value(ld_cg(a.partial + j));
 	return warp_sum(s);
 }
 
 // Sum over the edge list of one vertex by a half-warp (16 lanes); v_ok false
 // gives 0.  Both halves call it together (the reduction shuffles the warp).
 template <bool kFwd>
-__device__ __forceinline__ typename Dir<kFwd>::T half_vertex_sum(const BcArgs &a, uint32_t v, bool v_ok, int target) {
+__device__ __forceinline__ typename Dir<kFwd>::T half_vertex_sum(const BcArgs &a, uint32_t v, bool v_ok, int target,
+		bool use8) {
 	using T = typename Dir<kFwd>::T;
 	const uint32_t *adj = Dir<kFwd>::adj(a);
 	const uint32_t hl = lane_id() & 15u;
@@ -249,8 +327,7 @@ __device__ __forceinline__ typename Dir<kFwd>::T half_vertex_sum(const BcArgs &a
 			const uint32_t ee = e + (uint32_t) k * 16u;
 			nb[k] = ee < end ? __ldg(adj + ee) : 0xFFFFFFFFu;
 		}
-#pragma unroll
-		for (int k = 0; k < kBcUnroll; ++k) lx[k] = nb[k] != 0xFFFFFFFFu ? ld_lvx(a.lvx + nb[k]) : make_uint2(0xFFFFFFFEu, 0u);
+		gather_tags(a, nb, lx, use8, target);
 #pragma unroll
 		for (int k = 0; k < kBcUnroll; ++k)
 			if ((int) lx[k].x == target) s += Dir<kFwd>::value(lx[k].y);
@@ -264,7 +341,7 @@ __device__ __forceinline__ typename Dir<kFwd>::T half_vertex_sum(const BcArgs &a
 // by one warp; lane i gets vertex i's sum (0 for lanes past `end`).
 template <bool kFwd>
 __device__ __forceinline__ typename Dir<kFwd>::T warp_group_sum(const BcArgs &a, uint32_t v, bool valid, int target,
-		bool skip, unsigned long long *edges) {
+		bool skip, bool use8, unsigned long long *edges) {
 	using T = typename Dir<kFwd>::T;
 	const unsigned lane = lane_id();
 	uint32_t beg = 0, deg = 0;
@@ -297,10 +374,9 @@ __device__ __forceinline__ typename Dir<kFwd>::T warp_group_sum(const BcArgs &a,
 			const uint32_t oe = __shfl_sync(kFull, excl, o);
 			const bool on = f < total;
 			own[k] = on ? o : 32u;
-			nb[k] = on ? __ldg(adj + ob + (f - oe)) : 0u;
+			nb[k] = on ? __ldg(adj + ob + (f - oe)) : 0xFFFFFFFFu;
 		}
-#pragma unroll
-		for (int k = 0; k < kBcUnroll; ++k) lx[k] = own[k] < 32u ? ld_lvx(a.lvx + nb[k]) : make_uint2(0xFFFFFFFEu, 0u);
+		gather_tags(a, nb, lx, use8, target);
 #pragma unroll
 		for (int k = 0; k < kBcUnroll; ++k) val[k] = (int) lx[k].x == target ? Dir<kFwd>::value(lx[k].y) : T(0);
 #pragma unroll
@@ -349,6 +425,7 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 		return;
 	}
 	const uint32_t depth = steps - 1;
+	const bool use8 = a.byte_levels && depth <= 254;
 	const uint32_t K = kBcClasses * steps;
 	const uint64_t W32 = ((uint64_t) a.n + 31) / 32;
 	uint64_t q = (K * W32 + kBcCntCap - 1) / kBcCntCap;
@@ -374,7 +451,9 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 			if (v < a.n) {
 				a.sigma[v] = v == a.source ? 1u : 0u;
 				a.delta[v] = 0.0f;
-				a.lvx[v] = make_uint2((uint32_t) a.level[v], v == a.source ? 1u : 0u);
+				const int lv = a.level[v];
+				a.lvx[v] = make_uint2((uint32_t) lv, v == a.source ? 1u : 0u);
+				a.lv8[v] = (uint8_t) (lv < 0 || lv > 254 ? 255 : lv);
 			}
 			if (key >= 0) {
 				++my_reached;
@@ -460,23 +539,18 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 		const uint32_t me = ld_cg(a.kstart + kBcClasses * d + kBcClasses - 1);
 		const uint32_t se = ld_cg(a.kstart + kBcClasses * d + kBcClasses);
 		const uint32_t nbig = be - bb;
-		if (nbig > 0 && nbig <= kBcSmemBig) {
-			big_chunks<true>(a, bb, nbig, (int) d - 1);
+		if (nbig > 0) {
+			const bool global = nbig > kBcSmemBig;
+			if (global) {
+				if (!big_chunks_global<true>(a, bb, nbig, (int) d - 1, use8)) return;
+			} else {
+				big_chunks<true>(a, bb, nbig, (int) d - 1, use8);
+			}
 			if (!grid_barrier(ctl->bar, &ctl->err)) return;
 			for (uint32_t i = gw; i < nbig; i += tw) {
 				const uint32_t v = ld_cg(a.order + bb + i);
-				const uint32_t s = big_finish_sum<true>(a, i);
+				const uint32_t s = big_finish_sum<true>(a, i, global);
 				if (lane == 0) {
-					a.sigma[v] = s;
-					a.lvx[v].y = s;
-					e_fwd += a.in_off[v + 1] - a.in_off[v];
-				}
-			}
-		} else {
-			for (uint32_t i = bb + blockIdx.x; i < be; i += gridDim.x) {
-				const uint32_t v = ld_cg(a.order + i);
-				const uint32_t s = cta_vertex_sum<true>(a, v, (int) d - 1);
-				if (threadIdx.x == 0) {
 					a.sigma[v] = s;
 					a.lvx[v].y = s;
 					e_fwd += a.in_off[v + 1] - a.in_off[v];
@@ -487,7 +561,7 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 			const uint32_t i = i0 + (lane >> 4);
 			const bool ok = i < me;
 			const uint32_t v = ok ? ld_cg(a.order + i) : 0u;
-			const uint32_t s = half_vertex_sum<true>(a, v, ok, (int) d - 1);
+			const uint32_t s = half_vertex_sum<true>(a, v, ok, (int) d - 1, use8);
 			if (ok && (lane & 15u) == 0) {
 				a.sigma[v] = s;
 				a.lvx[v].y = s;
@@ -499,7 +573,7 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 			const uint32_t idx = me + grp * 32 + lane;
 			const bool valid = idx < se;
 			const uint32_t v = valid ? ld_cg(a.order + idx) : 0u;
-			const uint32_t s = warp_group_sum<true>(a, v, valid, (int) d - 1, false, &e_fwd);
+			const uint32_t s = warp_group_sum<true>(a, v, valid, (int) d - 1, false, use8, &e_fwd);
 			if (valid) {
 				a.sigma[v] = s;
 				a.lvx[v].y = s;
@@ -520,22 +594,18 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 		if (deepest) {
 			for (uint32_t i = gw; i < nbig; i += tw)
 				if (lane == 0) finish_dependency(a, ld_cg(a.order + bb + i), 0.0f);
-		} else if (nbig > 0 && nbig <= kBcSmemBig) {
-			big_chunks<false>(a, bb, nbig, d + 1);
+		} else if (nbig > 0) {
+			const bool global = nbig > kBcSmemBig;
+			if (global) {
+				if (!big_chunks_global<false>(a, bb, nbig, d + 1, use8)) return;
+			} else {
+				big_chunks<false>(a, bb, nbig, d + 1, use8);
+			}
 			if (!grid_barrier(ctl->bar, &ctl->err)) return;
 			for (uint32_t i = gw; i < nbig; i += tw) {
 				const uint32_t v = ld_cg(a.order + bb + i);
-				const float s = big_finish_sum<false>(a, i);
+				const float s = big_finish_sum<false>(a, i, global);
 				if (lane == 0) {
-					finish_dependency(a, v, s);
-					e_rev += a.row_off[v + 1] - a.row_off[v];
-				}
-			}
-		} else {
-			for (uint32_t i = bb + blockIdx.x; i < be; i += gridDim.x) {
-				const uint32_t v = ld_cg(a.order + i);
-				const float s = cta_vertex_sum<false>(a, v, d + 1);
-				if (threadIdx.x == 0) {
 					finish_dependency(a, v, s);
 					e_rev += a.row_off[v + 1] - a.row_off[v];
 				}
@@ -545,7 +615,7 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 			const uint32_t i = i0 + (lane >> 4);
 			const bool ok = i < me;
 			const uint32_t v = ok ? ld_cg(a.order + i) : 0u;
-			const float s = half_vertex_sum<false>(a, v, ok && !deepest, d + 1);
+			const float s = half_vertex_sum<false>(a, v, ok && !deepest, d + 1, use8);
 			if (ok && (lane & 15u) == 0) {
 				finish_dependency(a, v, s);
 				if (!deepest) e_rev += a.row_off[v + 1] - a.row_off[v];
@@ -556,7 +626,7 @@ __global__ void __launch_bounds__(kBcThreads, 2) k_bc(BcArgs a) {
 			const uint32_t idx = me + grp * 32 + lane;
 			const bool valid = idx < se;
 			const uint32_t v = valid ? ld_cg(a.order + idx) : 0u;
-			const float s = warp_group_sum<false>(a, v, valid, d + 1, deepest, &e_rev);
+			const float s = warp_group_sum<false>(a, v, valid, d + 1, deepest, use8, &e_rev);
 			if (valid) finish_dependency(a, v, s);
 		}
 		if (d > 0 && !grid_barrier(ctl->bar, &ctl->err)) return;

@@ -19,12 +19,14 @@ constexpr uint32_t kBcClasses = 7;            // sort keys per level: big, five 
 constexpr uint32_t kBcMaxGrid = 1024;
 constexpr uint32_t kBcTraceLevels = 64;       // per-level timers and sizes kept for the first levels
 static_assert(kBcClasses * kBcMaxLevels <= kBcCntCap, "every sort key needs a counter");
+constexpr uint32_t kBcByteLevelsMinVertices = 1u << 22;  // default: byte levels from here (the 8-byte
+                                                         // {level, value} array outgrows L2)
 constexpr uint32_t kBcChunk = 4096;           // edges of a big vertex one CTA sums as one task
 constexpr uint32_t kBcSmemBig = 4096;         // big vertices of a level whose chunk list every CTA keeps in shared
-                                              // memory; a level with more gives each big vertex one CTA
+                                              // memory; a level with more builds it in global memory
 
-// Chunk partial sums a graph of m edges can need in one level.
-inline size_t bc_partial_capacity(uint64_t m) { return kBcSmemBig + m / kBcChunk + 2; }
+// Chunk partial sums a graph of n vertices and m edges can need in one level.
+inline size_t bc_partial_capacity(uint64_t n, uint64_t m) { return n + kBcSmemBig + m / kBcChunk + 2; }
 
 struct BcControl {
 	unsigned bar[2];            // grid barrier
@@ -46,12 +48,15 @@ struct BcControl {
 
 struct BcArgs {
 	uint32_t n, source;
+	uint32_t byte_levels;              // 1: test lv8 first (used when the traversal is at most 254 deep)
 	const uint32_t *row_off, *col;     // CSR
 	const uint32_t *in_off, *in_src;   // in-edge lists (the reverse graph)
 	const int32_t *level;              // levels of the traversal from `source`, -1 unreached
 	const uint32_t *num_steps;         // the traversal's step count (deepest level + 1)
 	const int *bfs_status;             // the traversal's status word
 	uint32_t *sigma;                   // [n] shortest-path counts (mod 2^32)
+	uint8_t *lv8;                      // [n] levels as bytes (255: unreached or deeper than 254), checked
+	                                   // first when the traversal is at most 254 levels deep (fits in L2)
 	uint2 *lvx;                        // [n] {level, value}: the path count in the forward sweep, then the
 	                                   // bits of the float sum (1 + dependency) / paths in the reverse one
 	float *delta;                      // [n] dependencies (output)
@@ -59,7 +64,8 @@ struct BcArgs {
 	uint32_t *order;                   // [n] reached vertices sorted by (level, class: big, medium, small)
 	uint32_t *cnt;                     // [kBcCntCap] counters of the level sort
 	uint32_t *kstart;                  // [kBcClasses * kBcMaxLevels + 1] start of every key in `order`
-	uint32_t *partial;                 // [bc_partial_capacity(m)] chunk sums of big vertices (value bits)
+	uint32_t *partial;                 // [bc_partial_capacity(n, m)] chunk sums of big vertices (value bits)
+	uint32_t *cpre;                    // [n + 1] chunk prefix of a level with more than kBcSmemBig big vertices
 	BcControl *ctl;
 };
 

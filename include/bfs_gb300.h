@@ -141,6 +141,9 @@ typedef struct bfs_options {
 	                              single-source traversals (default 4; 0 = always bit-sliced) */
 	uint32_t batch_push_div;   /* bfs_run_batch: a level is pushed top-down while its frontier's out-edges
 	                              < E / batch_push_div, pulled bottom-up after (default 16) */
+	uint32_t bc_level_bytes;   /* bfs_bc_*: test neighbour levels in a byte array before fetching values
+	                              (traversals of at most 254 levels): 0 = for graphs of at least 2^22
+	                              vertices (default), 1 = always, 2 = never; results are identical */
 } bfs_options;
 
 /* Bottom-up step variants.  PULL: every unvisited destination of a column

@@ -51,15 +51,21 @@ def test_bc_matches_oracle_and_networkx(native, oracle, name):
 
 @pytest.mark.parametrize("name", golden_case_names())
 def test_bc_golden_graphs_deterministic(native, oracle, name):
-    """Every golden graph (duplicate edges included) and a repeat run bit-identical."""
+    """Every golden graph (duplicate edges included), a repeat run bit-identical,
+    and the byte-level gathers (bc_level_bytes = 1) giving the same bits as the
+    8-byte ones (2)."""
     import bfs_simd_benchmarks_gb300 as B
     c = load_case(name)
     arr = oracle.arrays_from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"])
     with B.Graph.from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"]) as g:
         for s in c["sources"]:
+            g.set_options(bc_level_bytes=2)
             dep, sig, _ = _check_source(oracle, arr, g, s)
             dep2, sig2, _ = g.bc(int(s))
             assert dep.tobytes() == dep2.tobytes() and sig.tobytes() == sig2.tobytes()
+            g.set_options(bc_level_bytes=1)
+            dep3, sig3, _ = g.bc(int(s))
+            assert dep.tobytes() == dep3.tobytes() and sig.tobytes() == sig3.tobytes()
 
 
 def test_bc_hubs_take_the_cta_path(native, oracle):
@@ -103,8 +109,10 @@ def test_bc_many_big_vertices_in_one_level(native, oracle):
     dst = np.concatenate(dst)
     arr = oracle.arrays_from_edges(n, src, dst, 512, 8)
     with B.Graph.from_edges(n, src, dst, 512, 8) as g:
-        _, _, st = _check_source(oracle, arr, g, 0)
-        assert st["level_big"][1] == first and st["level_big"][2] == pool
+        for mode in (1, 2):
+            g.set_options(bc_level_bytes=mode)
+            _, _, st = _check_source(oracle, arr, g, 0)
+            assert st["level_big"][1] == first and st["level_big"][2] == pool
 
 
 def test_bc_deep_chain(native, oracle):
@@ -118,6 +126,7 @@ def test_bc_deep_chain(native, oracle):
     dst = np.concatenate([dst, np.array([12, 102, 2002], np.uint32)])
     arr = oracle.arrays_from_edges(n, src, dst, 64, 4)
     with B.Graph.from_edges(n, src, dst, 64, 4) as g:
+        g.set_options(bc_level_bytes=1)   # deeper than 254 levels: the 8-byte gathers are used anyway
         _check_source(oracle, arr, g, 0)
         _check_source(oracle, arr, g, 1500)
 
@@ -129,8 +138,10 @@ def test_bc_rmat18_permuted(native, oracle):
     arr = oracle.arrays_from_edges(n, src, dst, 1024, 16)
     deg = arr["degrees"]
     with B.Graph.from_edges(n, src, dst, 1024, 16) as g:
-        for s in np.flatnonzero(deg > 0)[[3, 999]]:
-            _check_source(oracle, arr, g, int(s))
+        for mode in (1, 2):
+            g.set_options(bc_level_bytes=mode)
+            for s in np.flatnonzero(deg > 0)[[3, 999]]:
+                _check_source(oracle, arr, g, int(s))
 
 
 def test_bc_accumulate_matches_networkx_and_oracle(native, oracle):
