@@ -34,8 +34,13 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
+from bfs_simd_benchmarks_gb300 import workloads  # noqa: E402  (numpy only: loads no library)
+
 L2_FLUSH_BYTES = 256 << 20
 DEVICE_BUILD_EDGES = 1 << 26  # graphs this large build their layout on the GPU (BFS_LOAD_DEVICE_BUILD)
+
+
+METRIC = "BFS GTEPS (1-src & 4096-src batched), query p50/p99 ms; vs plain GPU BFS"
 
 
 def parse():
@@ -151,29 +156,91 @@ def algorithmic_bytes(st: dict, n: int, sw: int, pull: bool) -> int:
             + 8 * st["reached"] + 8 * n + st["num_steps"] * 2 * ((n + 7) // 8))
 
 
-def cpu_baseline(wl, src, dst, sources, seconds: float, per_call=None):
-    """The oracle (the reference's algorithm restated, OpenMP on all host cores) on a bounded sample."""
+def host_cpu_info() -> dict:
+    """The host cores the CPU legs run on: count, model and ISA."""
+    import platform
+    info = {"machine": platform.machine(), "nproc": os.cpu_count(),
+            "cores_usable": len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()}
+    model, flags, impl, part = None, "", None, None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                k, v = k.strip().lower(), v.strip()
+                if k == "model name" and model is None:
+                    model = v
+                elif k in ("flags", "features") and not flags:
+                    flags = v
+                elif k == "cpu implementer" and impl is None:
+                    impl = v
+                elif k == "cpu part" and part is None:
+                    part = v
+    except OSError:
+        pass
+    arm_parts = {("0x41", "0xd4f"): "Arm Neoverse V2 (NVIDIA Grace)", ("0x41", "0xd40"): "Arm Neoverse V1",
+                 ("0x41", "0xd0c"): "Arm Neoverse N1", ("0x41", "0xd8e"): "Arm Neoverse N3",
+                 ("0x41", "0xd84"): "Arm Neoverse V3"}
+    if model is None and impl is not None:
+        model = arm_parts.get((impl.lower(), (part or "").lower()), f"Arm implementer {impl} part {part}")
+    fl = set(flags.split())
+    simd = [x for x in ("avx512f", "avx512bw", "avx2", "sve2", "sve", "asimd") if x in fl]
+    info["model"] = model
+    info["isa"] = info["machine"] + (" + " + ", ".join(simd) if simd else "")
+    info["oracle_build"] = "plain C + OpenMP, gcc -O2 (scalar loops; no explicit SIMD)"
+    if "avx512f" not in fl:
+        info["note"] = "no AVX-512 on this host: the reference's bfs_simd (AVX-512 intrinsics) cannot run here"
+    return info
+
+
+def bench_config(wl, num_sources: int) -> dict:
+    """The workload both arms (GPU and reference) measure: same keys, same values."""
+    return dict(wl.describe(), sources=num_sources, step=f"{num_sources} single-source traversals",
+                l2="GPU arm: flushed (256 MiB write) before every traversal; graph far above L2")
+
+
+def oracle_workload(wl, limit: int = 0):
+    """The workload's graph and sources built on the checker's side only
+    (oracle/: generator, tool orders, CSR); no product library is loaded."""
     from oracle import oracle as O
     O.build(with_reference=False)
+    src, dst = O.gen_rmat(wl.n, wl.m, wl.a, wl.b, wl.c, seed=wl.seed, permute=wl.permute)
     arr = O.arrays_from_edges(wl.n, src, dst, wl.w, wl.s)
+    sources = wl.sources(arr["degrees"])
+    if limit:
+        sources = sources[:limit]
+    return O, arr, [int(s) for s in sources]
+
+
+def cpu_leg(args, wl, keep_levels: int = 8):
+    """cpu_baseline: the oracle (the reference's algorithm restated, OpenMP on
+    all host cores) timed on a bounded sample of the same workload.  It runs
+    before torch or CUDA are touched in this process, with a warm-up, so its
+    rate is the reference arm's."""
+    O, arr, sources = oracle_workload(wl, args.sources)
     deg = arr["degrees"].astype(np.uint64)
     threads = O.max_threads()
-    edges = 0
-    secs = 0.0
-    done = []
+    for s in sources[:4]:  # warm-up: thread pool, page faults of the per-run arrays
+        O.bfs_hybrid(arr, s, threads=threads)
+    edges, secs, runs, passes = 0, 0.0, 0, 0
     levels = {}
     t0 = time.perf_counter()
-    for s in sources:
-        cost, _, _, t = O.bfs_hybrid(arr, int(s), threads=threads)
-        edges += int(deg[cost >= 0].sum())
-        secs += t
-        done.append(int(s))
-        levels[int(s)] = cost
-        if time.perf_counter() - t0 > seconds:
+    while True:
+        for s in sources:
+            cost, _, _, t = O.bfs_hybrid(arr, s, threads=threads)
+            edges += int(deg[cost >= 0].sum())
+            secs += t
+            runs += 1
+            if passes == 0 and len(levels) < keep_levels:
+                levels[s] = cost
+        passes += 1
+        if time.perf_counter() - t0 > args.cpu_seconds:
             break
     return {"value": edges / secs / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
-            "sample": f"{len(done)} of {len(sources)} sources of the same graph, the reference's timed region "
-                      f"(traversal only), oracle/bfs_oracle.c OpenMP build"}, levels, arr
+            "sample": f"{passes} pass(es) over all {len(sources)} sources of the same graph ({runs} traversals) "
+                      "after a 4-traversal warm-up, the reference's timed region (traversal only, "
+                      "apps/bfs_simd/bfs.cpp:806-913), oracle/bfs_oracle.c OpenMP build, run before any "
+                      "CUDA work in this process",
+            "host": host_cpu_info()}, levels
 
 
 def aggregate_replicas(torch, total_ms: float, edges: int, dev, world: int):
@@ -188,29 +255,21 @@ def aggregate_replicas(torch, total_ms: float, edges: int, dev, world: int):
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU algorithm (oracle/bfs_oracle.c,
+    OpenMP on all host cores; bfs_simd itself needs AVX-512) on the same
+    workload, config and metric as the GPU arm.  One step = every source once,
+    like the GPU arm's step.  Only the checker's library is loaded."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from bfs_simd_benchmarks_gb300 import workloads
-    import bfs_simd_benchmarks_gb300 as B
-    B.load_library(build_if_missing=True)
     wl = workloads.get(args.workload)
-    src, dst = wl.edges()
-    from oracle import oracle as O
-    O.build(with_reference=False)
-    arr = O.arrays_from_edges(wl.n, src, dst, wl.w, wl.s)
+    O, arr, sources = oracle_workload(wl, args.sources)
     deg = arr["degrees"].astype(np.uint64)
-    sources = wl.sources(arr["degrees"])
     threads = O.max_threads()
-    per_step = 4
-    it = 0
 
     def step():
-        nonlocal it
         e, t = 0, 0.0
-        for _ in range(per_step):
-            s = int(sources[it % len(sources)])
-            it += 1
+        for s in sources:
             cost, _, _, sec = O.bfs_hybrid(arr, s, threads=threads)
             e += int(deg[cost >= 0].sum())
             t += sec
@@ -224,34 +283,38 @@ def run_reference(args):
         E += e
         T += t
     val = E / T / 1e9
-    line = {"metric": "BFS GTEPS (1-src & 4096-src batched), query p50/p99 ms; vs plain GPU BFS",
-            "impl": "reference", "value": val, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": T / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded R-MAT)",
-            "config": dict(wl.describe(), step=f"{per_step} single-source traversals on the host cores"),
+    line = {"metric": METRIC, "impl": "reference", "value": val, "unit": "GTEPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": T / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded R-MAT stand-in, see config)", "config": bench_config(wl, len(sources)),
             "cpu_baseline": {"value": val, "unit": "GTEPS", "cores": threads, "kind": "port",
-                             "sample": f"{per_step} sources per step, {args.steps} steps, the reference's "
-                                       "timed region, oracle/bfs_oracle.c OpenMP build"},
+                             "sample": f"all {len(sources)} sources per step, {args.steps} steps after "
+                                       f"{args.warmup} warm-up steps, the reference's timed region "
+                                       "(apps/bfs_simd/bfs.cpp:806-913), oracle/bfs_oracle.c OpenMP build",
+                             "host": host_cpu_info()},
             "e2e": {"value": val, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def bench_batched(args, torch, dev, graph=None, build_s=0.0):
+def bench_batched(args, torch, dev, graph=None, build_s=0.0, edges=None):
     """Batched multi-source BFS (bfs_run_batch): every step traverses all the
     sources at once and writes uint8 levels [sources][N] into HBM.  Compared
-    with the single-source kernel on the same graph (the plain GPU BFS).
-    `graph` is the single-source workload's graph when both are the same."""
+    with the single-source kernel on the same graph (the plain GPU BFS);
+    sampled rows are checked against the oracle.  `graph` (and its `edges`)
+    is the single-source workload's graph when both are the same."""
     import bfs_simd_benchmarks_gb300 as B
-    from bfs_simd_benchmarks_gb300 import workloads
+    from oracle import oracle as O
     wl = workloads.get(args.batch_workload)
     if graph is None:
         t0 = time.perf_counter()
         src, dst = wl.edges()
         g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s, device_build=wl.m >= DEVICE_BUILD_EDGES)
         build_s = time.perf_counter() - t0
-        del src, dst
     else:
         g = graph
+        src, dst = edges
+    oarr = O.csr_arrays(wl.n, src, dst)
+    del src, dst
     g.set_options(batch_budget_mb=args.batch_budget_mb)
     deg = g.degrees()
     sources = wl.sources(deg, args.batch_sources)
@@ -320,18 +383,15 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
         single_ms.append(e0.elapsed_time(e1))
         single_edges += st["edges_traversed"]
     for i in check:
-        with torch.cuda.stream(stream):
-            g.run_device(int(sources[i]), lev.data_ptr(), 0, stream.cuda_stream)
-        g.last_stats()
-        ref = lev.cpu().numpy()
+        ref = O.bfs_levels(oarr, int(sources[i]))
         ref = np.where(ref < 0, 255, ref).astype(np.uint8)
         row = host[i].numpy() if host is not None else out[i].cpu().numpy()
         rows_ok += int(np.array_equal(row, ref))
     single_gteps = single_edges / (sum(single_ms) / 1e3) / 1e9
     st = runs[-1][1]
     # algorithmic bytes of a batch: every level writes its N x K-word plane, every
-    # frontier word a pull reads is 8 B (above 512 sources the device counts one
-    # word per row read, so this is a lower bound), the output is N bytes per source
+    # 64-bit frontier word a pull gathers is 8 B (counted on the device), the
+    # output is N bytes per source
     alg = st["depth"] * 8 * st["words_per_vertex"] * wl.n + 8 * st["words_gathered"] + len(sources) * wl.n
     peak, peak_kind = peaks()
     achieved = alg / (statistics.mean(ms) / 1e3) / 1e9
@@ -352,7 +412,8 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0):
         "autotune": tuned,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "kernels": "k_ms_bfs + k_ms_emit", "peak_kind": peak_kind, "algorithmic_bytes_per_batch": alg},
-        "parity": f"batched rows equal single-source levels on {rows_ok}/{len(check)} sources checked",
+        "parity": f"batched rows bit-exact to the oracle's levels (oracle/bfs_oracle.c orc_bfs_levels) on "
+                  f"{rows_ok}/{len(check)} sampled sources",
         "steps": len(ms), "l2": "flushed (256 MiB write) before every batch; batch state far above L2",
     }
     if graph is None:
@@ -456,15 +517,16 @@ def bench_serving(args, torch, dev):
     factor 16) under a 40 GB HBM admission budget; open-loop Poisson arrivals
     of (graph, source) queries drawn uniformly, coalesced per graph into
     batches of up to 1024 sources; levels are computed and left on the device
-    (BFS_DST_NONE) so that latency measures the traversal path."""
+    (BFS_DST_NONE) so that latency measures the traversal path.  Then a burst
+    of queries whose levels are delivered to host memory (BFS_DST_HOST), with
+    a sample of them checked against the oracle."""
     import bfs_simd_benchmarks_gb300 as B
-    from bfs_simd_benchmarks_gb300 import workloads
     t0 = time.perf_counter()
-    graphs = []
+    graphs, edges = [], []
     for wl in workloads.serve_graphs():
         src, dst = wl.edges()
         graphs.append((wl, B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s, device_build=wl.m >= DEVICE_BUILD_EDGES)))
-        del src, dst
+        edges.append((src, dst))
     build_s = time.perf_counter() - t0
     srv = B.Server(budget_bytes=40 * 10**9)
     for _, g in graphs:
@@ -495,10 +557,13 @@ def bench_serving(args, torch, dev):
                           "max_ms": st["max_ms"], "mean_batch": st["mean_batch"], "batches": int(st["batches"]),
                           "gteps": st["edges_traversed"] / wall / 1e9, "wall_s": wall,
                           "slots_in_flight_mean": st["device_ms"] / 1e3 / wall})
+    host = serve_host_check(srv, graphs, edges, pools)
     res = {"graphs": [{"workload": wl.name, "vertices": wl.n, "edges": wl.m} for wl, _ in graphs],
            "budget_bytes": 40 * 10**9, "admitted_bytes": srv.stats()["device_bytes"], "graph_build_s": round(build_s, 1),
-           "max_batch": 1024, "slots": 3, "results": "left on the device (BFS_DST_NONE)",
-           "latency": "submit -> traversal and output pass complete, host clock", "rates": rates,
+           "max_batch": 1024, "slots": 3, "results": "rates: left on the device (BFS_DST_NONE); host_delivery: "
+                                                      "uint8 levels copied to host memory (BFS_DST_HOST)",
+           "latency": "submit -> traversal and output pass complete (rates) / levels in host memory (host_delivery), "
+                      "host clock", "rates": rates, "host_delivery": host,
            "clocks": clk.summary()}
     srv.close()
     for _, g in graphs:
@@ -507,12 +572,49 @@ def bench_serving(args, torch, dev):
     return res
 
 
+def serve_host_check(srv, graphs, edges, pools, count: int = 256, per_graph: int = 2):
+    """A burst of `count` queries over all graphs with levels delivered to
+    host memory; `per_graph` results of every graph compared with the oracle."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(99)
+    gids = rng.integers(0, len(graphs), count)
+    picks = rng.integers(0, 4096, count)
+    outs = [np.empty(graphs[gi][0].n, np.uint8) for gi in gids]
+    srv.reset_stats()
+    t0 = time.perf_counter()
+    tickets = [srv.submit_host(int(gi), int(pools[gi][k]), outs[i]) for i, (gi, k) in enumerate(zip(gids, picks))]
+    lat = [srv.wait(t)["latency_ms"] for t in tickets]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    ok = checked = 0
+    for gi, (wl, _) in enumerate(graphs):
+        idx = [i for i in range(count) if gids[i] == gi][:per_graph]
+        if not idx:
+            continue
+        oarr = O.csr_arrays(wl.n, *edges[gi])
+        for i in idx:
+            ref = O.bfs_levels(oarr, int(pools[gi][picks[i]]))
+            ok += int(np.array_equal(outs[i], np.where(ref < 0, 255, ref).astype(np.uint8)))
+            checked += 1
+        del oarr
+    return {"queries": count, "submitted": "as one burst from the host thread", "wall_s": wall,
+            "achieved_qps": count / wall, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "mean_batch": st["mean_batch"],
+            "d2h_bytes": int(sum(o.nbytes for o in outs)),
+            "parity": f"{ok}/{checked} sampled results bit-exact to the oracle's levels "
+                      f"(oracle/bfs_oracle.c orc_bfs_levels), {per_graph} per graph"}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
         return
     rank, world, local = dist_env()
+    wl = workloads.get(args.workload)
+    cpu, cpu_levels = None, {}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, cpu_levels = cpu_leg(args, wl)  # before torch and CUDA are touched
     import torch
     torch.cuda.set_device(local)
     if world > 1:
@@ -520,9 +622,7 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     import bfs_simd_benchmarks_gb300 as B
     from bfs_simd_benchmarks_gb300 import _native as N
-    from bfs_simd_benchmarks_gb300 import workloads
     B.load_library(build_if_missing=True)
-    wl = workloads.get(args.workload)
     t_gen = time.perf_counter()
     src, dst = wl.edges()
     g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s, device_build=wl.m >= DEVICE_BUILD_EDGES)
@@ -612,16 +712,14 @@ def main():
     batched = None
     if args.batch_workload != "none" and world == 1:
         same = args.batch_workload == args.workload
-        batched = bench_batched(args, torch, dev, g if same else None, t_gen if same else 0.0)
+        batched = bench_batched(args, torch, dev, g if same else None, t_gen if same else 0.0,
+                                (src, dst) if same else None)
     serving = None
     if args.serve != "none" and world == 1:
         serving = bench_serving(args, torch, dev)
 
-    cpu = None
     parity = None
-    cpu_arr = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu, cpu_levels, cpu_arr = cpu_baseline(wl, src, dst, sources, args.cpu_seconds)
+    if cpu_levels:
         ok = 0
         for s, ref in cpu_levels.items():
             got, _, _ = g.run(s, parents=False)
@@ -629,21 +727,24 @@ def main():
         parity = f"levels bit-exact on {ok}/{len(cpu_levels)} sources checked against the oracle"
     bc = None
     if args.bc_sources > 0 and world == 1:
-        bc = bench_bc(args, torch, dev, g, sources, flush, cpu_arr)
+        bc_arr = None
+        if not args.no_cpu_baseline:
+            from oracle import oracle as O
+            bc_arr = O.csr_arrays(wl.n, src, dst)
+        bc = bench_bc(args, torch, dev, g, sources, flush, bc_arr)
     if rank == 0:
         clocks = clk.summary()
         line = {
-            "metric": "BFS GTEPS (1-src & 4096-src batched), query p50/p99 ms; vs plain GPU BFS",
+            "metric": METRIC,
             "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded R-MAT stand-in, see config)",
-            "config": dict(wl.describe(), step=f"{len(sources)} single-source traversals",
-                           parallelism="replicas" if world > 1 else "single GPU", mode=args.mode,
-                           bottom_up=args.bottom_up,
-                           l2=f"flushed (256 MiB write) before every traversal; graph {info['device_bytes'] / 1e6:.0f} MB > L2",
-                           grid_ctas=timed[0][2]["grid_ctas"], column_groups=info["num_groups"],
-                           autotune=tuned,
-                           graph_build_s=round(t_gen, 2)),
+            "config": bench_config(wl, len(sources)),
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "gpu_config": {"mode": args.mode, "bottom_up": args.bottom_up,
+                           "graph_device_bytes": info["device_bytes"], "grid_ctas": timed[0][2]["grid_ctas"],
+                           "column_groups": info["num_groups"], "autotune": tuned,
+                           "graph_build_s": round(t_gen, 2)},
             "single_source": {"gteps": value, "ms_per_traversal_mean": statistics.mean(trav_ms),
                               "ms_per_traversal_p50": statistics.median(trav_ms),
                               "ms_per_traversal_p99": float(np.percentile(trav_ms, 99)),

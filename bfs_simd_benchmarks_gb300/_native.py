@@ -173,15 +173,19 @@ class Stats(C.Structure):
         ("sparse_ms", C.c_double),
         ("to_sparse_ms", C.c_double),
         ("step_ms", C.c_float * BFS_TRACE_MAX),
+        ("step_work_min_ms", C.c_float * BFS_TRACE_MAX),
+        ("step_work_max_ms", C.c_float * BFS_TRACE_MAX),
         ("bu_cycles", C.c_uint64 * 8),
     ]
 
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("trace", "step_ms", "bu_cycles")}
+        arrays = ("trace", "step_ms", "step_work_min_ms", "step_work_max_ms", "bu_cycles")
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in arrays}
         d["bu_cycles"] = list(self.bu_cycles[:6])
         k = min(self.num_steps, BFS_TRACE_MAX)
         d["trace"] = list(self.trace[:k])
-        d["step_ms"] = [round(x, 5) for x in self.step_ms[:k]]
+        for name in ("step_ms", "step_work_min_ms", "step_work_max_ms"):
+            d[name] = [round(x, 5) for x in getattr(self, name)[:k]]
         return d
 
 

@@ -589,6 +589,9 @@ int collect_stats(bfs_graph *g, bfs_stats *out) {
 			double total = (t1 - t0) * 1e-6, conv = 0;
 			if (d.t_conv[i] >= t0 && d.t_conv[i] <= t1 && d.t_conv[i]) conv = (d.t_conv[i] - t0) * 1e-6;
 			s.step_ms[i] = (float) total;
+			const unsigned long long wmax = d.t_work_max[i], wmin = ~d.t_work_min_inv[i];
+			if (d.t_work_max[i] >= t0) s.step_work_max_ms[i] = (float) ((wmax - t0) * 1e-6);
+			if (d.t_work_min_inv[i] && wmin >= t0) s.step_work_min_ms[i] = (float) ((wmin - t0) * 1e-6);
 			if (s.trace[i]) { s.dense_ms += total - conv; s.to_dense_ms += conv; }
 			else { s.sparse_ms += total - conv; s.to_sparse_ms += conv; }
 		}
@@ -973,7 +976,11 @@ int bc_collect(bfs_graph *g, bfs_bc_stats *out) {
 			s.level_medium[d] = c.lv_medium[d];
 			const unsigned long long f0 = d <= 1 ? c.t[1] : c.t_fwd[d - 1], f1 = c.t_fwd[d];
 			if (d > 0 && f0 && f1 >= f0) s.level_paths_ms[d] = (float) ((f1 - f0) * 1e-6);
-			const unsigned long long r0 = d == c.depth || d + 1 >= BFS_BC_TRACE_LEVELS ? c.t[2] : c.t_rev[d + 1], r1 = c.t_rev[d];
+			// the sweep of level d starts where level d + 1 ended (the deepest
+			// level starts at the end of the path counts); past the recorded
+			// levels the start is unknown and the entry stays 0
+			if (d != c.depth && d + 1 >= BFS_BC_TRACE_LEVELS) continue;
+			const unsigned long long r0 = d == c.depth ? c.t[2] : c.t_rev[d + 1], r1 = c.t_rev[d];
 			if (r0 && r1 >= r0) s.level_dependencies_ms[d] = (float) ((r1 - r0) * 1e-6);
 		}
 		*out = s;

@@ -61,6 +61,10 @@ struct DevStats {
 	// every step and the end of its queue<->bitmap conversion (if any)
 	unsigned long long t_step[257];
 	unsigned long long t_conv[256];
+	// per step, over the CTAs: the latest and (bit-inverted) the earliest
+	// globaltimer stamp at which a CTA had finished the step's work
+	unsigned long long t_work_max[256];
+	unsigned long long t_work_min_inv[256];
 	// SM cycles summed over CTAs inside the bottom-up step: group setup,
 	// window lists, consumer wait, consumer work, producer wait, publish
 	unsigned long long bu_cycles[8];

@@ -1161,6 +1161,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 			phase_expand(g, r, p, step, smem, acc);
 		}
 		flush_step(acc, r, step % 3);
+		if (threadIdx.x == 0 && step < 256) {
+			const unsigned long long t = global_timer_ns();
+			atomicMax(&r.stats->t_work_max[step], t);
+			atomicMax(&r.stats->t_work_min_inv[step], ~t);
+		}
 		if (blockIdx.x == 0 && threadIdx.x == 0) {
 			if (step < 256) r.stats->trace[step] = dense ? 1 : 0;
 			if (dense) r.stats->dense_steps++;

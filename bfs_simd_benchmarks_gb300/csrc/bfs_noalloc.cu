@@ -20,7 +20,10 @@
 //     threads) race on the shared scratch: serialise them;
 //   - the first call on a device does a one-time set-up (it looks up the
 //     device address of the scratch array); make that first call before any
-//     stream capture.
+//     stream capture;
+//   - the CSR is checked as it is read: a column id >= num_vertices is
+//     skipped and the call's status becomes BFS_EARG (the offsets themselves
+//     must be non-decreasing and end inside the column array).
 //
 // The kernel is a top-down-only variant of the traversal kernel: one
 // cooperative launch runs every level, separated by a bounded-spin grid
@@ -62,6 +65,8 @@ __global__ void __launch_bounds__(kNaThreads) k_noalloc_bfs(const uint32_t *__re
 		s->tail[0] = s->tail[1] = s->tail[2] = 0;
 		s->err = 0;
 	}
+	// *status was zeroed by the host before the launch; every CTA that ends
+	// on an error raises it below, so no CTA's late error is lost.
 	bool ok = grid_barrier(s->bar, &s->err);
 	if (ok && t0 == 0) {
 		level[source] = 0;
@@ -89,9 +94,13 @@ __global__ void __launch_bounds__(kNaThreads) k_noalloc_bfs(const uint32_t *__re
 				uint32_t v = 0;
 				if (e < end) {
 					v = __ldg(col + e);
-					const uint32_t bit = 1u << (v & 31);
-					if (!(ld_cg(s->vis + (v >> 5)) & bit))
-						claimed = !(atomicOr(s->vis + (v >> 5), bit) & bit);
+					if (v < n) {
+						const uint32_t bit = 1u << (v & 31);
+						if (!(ld_cg(s->vis + (v >> 5)) & bit))
+							claimed = !(atomicOr(s->vis + (v >> 5), bit) & bit);
+					} else {
+						atomicExch(&s->err, 4 /* BFS_EARG: a column id out of range */);
+					}
 				}
 				const unsigned mask = __ballot_sync(kFull, claimed);
 				if (!mask) continue;
@@ -107,7 +116,12 @@ __global__ void __launch_bounds__(kNaThreads) k_noalloc_bfs(const uint32_t *__re
 		}
 		ok = grid_barrier(s->bar, &s->err);
 	}
-	if (t0 == 0 && status) *status = *(volatile int *) &s->err;
+	// Every CTA reports what it saw: a CTA whose barrier gave up after CTA 0
+	// had finished still raises the status (codes are positive, BFS_OK is 0).
+	if (threadIdx.x == 0 && status) {
+		const int e = *(volatile int *) &s->err;
+		if (e) atomicMax(status, e);
+	}
 }
 
 struct DeviceSetup {
@@ -148,8 +162,10 @@ extern "C" int bfs_run_noalloc(uint32_t num_vertices, const uint32_t *row_offset
 		su = d;
 	}
 	cudaStream_t st = (cudaStream_t) stream;
-	// The grid barrier's words must be zero when the launch starts.
+	// The grid barrier's words must be zero when the launch starts, and so
+	// must the status, which the kernel's CTAs only raise.
 	if (cudaMemsetAsync(su.scratch->bar, 0, sizeof(su.scratch->bar), st) != cudaSuccess) return BFS_ECUDA;
+	if (status && cudaMemsetAsync(status, 0, sizeof(int32_t), st) != cudaSuccess) return BFS_ECUDA;
 	uint32_t n = num_vertices;
 	NoAllocScratch *sp = su.scratch;
 	void *args[] = {(void *) &row_offsets, (void *) &columns, &n, &source, &levels, &status, &sp};

@@ -268,18 +268,19 @@ __device__ __forceinline__ bool ms_gather(const MsArgs &a, const uint64_t *cur, 
 					lm &= lm - 1;
 					ut = __shfl_sync(kFull, u, src_lane);
 					mt = shfl64(um, src_lane);
-					++loads;  // rows (counted as one word each)
 				}
 				const uint64_t *r = cur + (size_t) ut * K;
-				g0[t] = (need0 && ((mt >> lane) & 1ull)) ? ld_cg64(r + lane) : 0ull;
-				g1[t] = (need1 && ((mt >> (lane + 32)) & 1ull)) ? ld_cg64(r + lane + 32) : 0ull;
+				const bool l0 = need0 && ((mt >> lane) & 1ull), l1 = need1 && ((mt >> (lane + 32)) & 1ull);
+				g0[t] = l0 ? ld_cg64(r + lane) : 0ull;
+				g1[t] = l1 ? ld_cg64(r + lane + 32) : 0ull;
+				loads += (uint32_t) l0 + (uint32_t) l1;  // words read by this lane
 			}
 #pragma unroll
 			for (int t = 0; t < kMsGather; ++t) { acc0 |= g0[t]; acc1 |= g1[t]; }
 			done = fm.complete(acc0 | vis0, acc1 | vis1);
 		}
 	}
-	if (lane_id() == 0) gathered += loads;
+	gathered += loads;
 	return done;
 }
 

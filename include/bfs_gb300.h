@@ -184,6 +184,10 @@ typedef struct bfs_stats {
 	 * device between grid barriers (persistent mode only; 0 otherwise). */
 	double dense_ms, to_dense_ms, sparse_ms, to_sparse_ms;
 	float step_ms[BFS_TRACE_MAX]; /* duration of each step, conversion included */
+	/* from the start of each step to the first / the last CTA done with the
+	 * step's work (the rest of step_ms is the grid barrier and the totals) */
+	float step_work_min_ms[BFS_TRACE_MAX];
+	float step_work_max_ms[BFS_TRACE_MAX];
 	/* Bottom-up step profile: SM cycles summed over CTAs spent in group setup,
 	 * segment lists, consumer wait, consumer work, producer wait and publish. */
 	uint64_t bu_cycles[8];
@@ -216,8 +220,7 @@ typedef struct bfs_batch_stats {
 	uint32_t push_levels;      /* levels expanded top-down (the others pulled bottom-up) */
 	int32_t status;            /* BFS_OK, BFS_ETIMEOUT, or BFS_EUNSUPPORTED (a level above 254) */
 	uint64_t edges_traversed;  /* sum over the sources of the out-degrees of the vertices each reached */
-	uint64_t words_gathered;   /* frontier words read by pull levels (batches of more than 512 sources
-	                              count one per in-neighbour row read: a lower bound) */
+	uint64_t words_gathered;   /* 64-bit frontier words read by the pull levels' gathers */
 	uint32_t planes;           /* level planes held (levels kept before an early output pass) */
 	uint32_t spills;           /* early output passes (traversal deeper than the planes) */
 	uint32_t words_per_vertex; /* 64-bit words per vertex, ceil(num_sources / 64) */
@@ -397,8 +400,11 @@ int bfs_server_destroy(bfs_server *s);
  * memory (row_offsets[num_vertices+1], columns[row_offsets[num_vertices]],
  * 0-based), writing int32 levels (-1 unreached) into the caller's device
  * buffer levels[num_vertices] on `stream` (a cudaStream_t, NULL for the
- * default stream).  If `status` (a device int) is not NULL it receives
- * BFS_OK or BFS_ETIMEOUT when the traversal ends.  Asynchronous.
+ * default stream).  If `status` (a device int) is not NULL it is set to
+ * BFS_OK on the stream before the launch and raised to BFS_ETIMEOUT (a grid
+ * barrier gave up) or BFS_EARG (a column id >= num_vertices, which is then
+ * skipped) by the traversal.  The row offsets must be non-decreasing and end
+ * inside the column array; they are not checked.  Asynchronous.
  *
  * This entry point allocates nothing, for callers that cannot call
  * cudaMalloc: plug-ins whose host framework reserves the device memory and

@@ -22,11 +22,18 @@ _i32p = C.POINTER(C.c_int32)
 _lib = None
 
 
+def reference_dir() -> str | None:
+    """The reference checkout named by BFS_REFERENCE_DIR, if it holds the sources."""
+    d = os.environ.get("BFS_REFERENCE_DIR", "")
+    return d if d and os.path.isdir(os.path.join(d, "apps")) else None
+
+
 def build(with_reference: bool = True) -> None:
-    """Compiles liboracle.so and, where the reference sources exist, oracle/_ref."""
+    """Compiles liboracle.so and, where the reference sources exist (BFS_REFERENCE_DIR), oracle/_ref."""
     subprocess.run(["make", "-s", "-C", HERE, "lib"], check=True, capture_output=True)
-    if with_reference and os.path.isdir("/root/reference/apps"):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, capture_output=True)
+    ref = reference_dir()
+    if with_reference and ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True, capture_output=True)
 
 
 def lib() -> C.CDLL:
@@ -60,6 +67,8 @@ def lib() -> C.CDLL:
             "orc_bc_single": [C.c_uint, _u32p, _u32p, _u32p, C.c_uint, _u32p, C.POINTER(C.c_float), _i32p,
                               C.POINTER(C.c_double)],
             "orc_max_threads": [],
+            "orc_gen_rmat": [C.c_uint, C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.c_ulonglong, C.c_uint,
+                             _u32p, _u32p],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -122,6 +131,17 @@ def arrays_from_edges(n: int, src, dst, w: int, s_len: int) -> dict:
             "csr_src": cs, "csr_dst": cd, "heads": hs, "tails": tl, "tile_offsets": noff}
 
 
+def csr_arrays(n: int, src, dst) -> dict:
+    """Only the CSR arrays (what bfs_levels, check_parents and bc_single read):
+    cheaper than arrays_from_edges on large graphs."""
+    cs, cd, deg = csr_order(n, src, dst)
+    del cs
+    row = np.zeros(n, dtype=np.uint32)
+    if n > 1:
+        row[1:] = np.cumsum(deg[:-1], dtype=np.uint64).astype(np.uint32)
+    return {"n": n, "m": int(cd.size), "degrees": deg, "row_start": row, "csr_dst": cd}
+
+
 # ---- traversal -------------------------------------------------------------
 def bfs_hybrid(arr: dict, source: int, t_ratio: int = 20, threads: int = 0, trace_cap: int = 256):
     """Levels, parents, direction trace and seconds of the restated graph_prepare."""
@@ -168,6 +188,18 @@ def bc_single(arr: dict, source: int):
 
 def max_threads() -> int:
     return int(lib().orc_max_threads())
+
+
+def gen_rmat(num_vertices: int, num_edges: int, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 1, dedup: bool = True, no_self_loops: bool = True, permute: bool = False):
+    """The bench's seeded R-MAT edge list generated on the checker's side
+    (bfs_oracle.c orc_gen_rmat): the same list as the product's generator,
+    without loading the product library."""
+    src = np.empty(num_edges, dtype=np.uint32)
+    dst = np.empty(num_edges, dtype=np.uint32)
+    flags = (1 if no_self_loops else 0) | (2 if dedup else 0) | (4 if permute else 0)
+    _ok(lib().orc_gen_rmat(num_vertices, num_edges, a, b, c, seed, flags, _p(src), _p(dst)), "gen_rmat")
+    return src, dst
 
 
 # ---- files -------------------------------------------------------------------

@@ -17,7 +17,7 @@ into oracle/_ref by `make -C oracle ref`).  For every case it
 The fixtures keep the edge lists of small cases and, for the scale-16 case,
 only the generator parameters plus a digest of the edge list.
 
-    python tests/golden/make_golden.py
+    BFS_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -39,7 +39,7 @@ from oracle import oracle as O  # noqa: E402
 import bfs_simd_benchmarks_gb300 as B  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+REF = os.environ.get("BFS_REFERENCE_DIR", "")  # the reference checkout; no default path
 
 
 def sha_files(paths: list[str]) -> str:
@@ -160,8 +160,9 @@ def cases():
 
 
 def main():
-    if not os.path.isdir(os.path.join(REF, "apps", "bfs_simd")):
-        sys.exit("reference sources not present: the golden fixtures can only be regenerated where they are")
+    if not REF or not os.path.isdir(os.path.join(REF, "apps", "bfs_simd")):
+        sys.exit("set BFS_REFERENCE_DIR to the reference checkout: the golden fixtures can only be regenerated "
+                 "where its sources are")
     O.build(with_reference=True)
     summary = {}
     with tempfile.TemporaryDirectory() as work:

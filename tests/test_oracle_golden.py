@@ -98,3 +98,17 @@ def test_oracle_switch_rule_goes_dense_on_big_frontier(oracle):
     _, _, trace_td, _ = oracle.bfs_hybrid(arr, int(c["sources"][0]), t_ratio=1)
     # frontier + out_degree > E never holds: every step is top-down
     assert set(trace_td) == {0}
+
+
+@pytest.mark.parametrize("n,m,permute,dedup,loops", [(1 << 10, 16 << 10, False, True, False),
+                                                     (3000, 40000, True, True, False),
+                                                     (1 << 12, 1 << 16, True, False, True),
+                                                     (5, 20, False, True, False)])
+def test_oracle_generator_equals_product_generator(native, oracle, n, m, permute, dedup, loops):
+    """The checker's R-MAT generator (used where the product library must not
+    be loaded) gives the product generator's edge list, element for element."""
+    import bfs_simd_benchmarks_gb300 as B
+    a = oracle.gen_rmat(n, m, seed=77, permute=permute, dedup=dedup, no_self_loops=not loops)
+    b = B.gen_rmat(n, m, seed=77, permute=permute, dedup=dedup, no_self_loops=not loops)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])

@@ -60,3 +60,22 @@ def test_reference_arm_line_on_rank0():
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["host"]["isa"] and line["cpu_baseline"]["host"]["nproc"] >= 1
+    # the same config object as the GPU arm's line
+    sys.path.insert(0, ROOT)
+    import bench
+    from bfs_simd_benchmarks_gb300 import workloads
+    assert line["config"] == bench.bench_config(workloads.get("rmat16"), 1)
+
+
+@pytest.mark.timeout(600)
+def test_reference_arm_loads_no_product_library():
+    """The reference arm maps the checker's library only, never libbfs_gb300.so."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'rmat16', "
+            "'--steps', '1', '--warmup', '0']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPS', int('libbfs_gb300' in maps), int('liboracle.so' in maps))")
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().splitlines()[-1] == "MAPS 0 1"
