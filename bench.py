@@ -753,7 +753,9 @@ def main():
                               "steps_mean": statistics.mean(st["num_steps"] for _, _, st in timed),
                               "phase_ms_mean": {k: statistics.mean(st[k] for _, _, st in timed)
                                                 for k in ("dense_ms", "to_dense_ms", "sparse_ms", "to_sparse_ms")},
-                              "example_steps": {"trace": timed[0][2]["trace"], "step_ms": timed[0][2]["step_ms"]},
+                              "example_steps": {k: timed[0][2][k] for k in ("trace", "step_ms", "step_work_min_ms",
+                                                                               "step_work_max_ms")},
+                              "init_ms_mean": statistics.mean(st["device_ms"] - st["kernel_ms"] for _, _, st in timed),
                               "bu_cycles_per_cta_mean": [round(statistics.mean(st["bu_cycles"][i] for _, _, st in timed)
                                                                / max(1, timed[0][2]["grid_ctas"])) for i in range(6)]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -546,10 +546,12 @@ int run_impl(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, 
 	p.to_dense_threshold = g->m / std::max<uint32_t>(1, g->opt.to_dense_ratio);
 	p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
 	int rc;
-	if (cudaEventRecord(g->ev0, st) != cudaSuccess) return BFS_ECUDA;
-	if ((rc = launch_init(g->dg, r, st, g->num_sms))) return rc;
-	if (cudaEventRecord(g->evm, st) != cudaSuccess) return BFS_ECUDA;
 	g->stepwise_last = g->opt.mode == BFS_MODE_STEPWISE;
+	if (cudaEventRecord(g->ev0, st) != cudaSuccess) return BFS_ECUDA;
+	// the persistent kernel starts from a source seeded by the clearing pass;
+	// the stepwise host loop seeds with its own launch
+	if ((rc = launch_init(g->dg, r, st, g->num_sms, g->stepwise_last ? nullptr : &p))) return rc;
+	if (cudaEventRecord(g->evm, st) != cudaSuccess) return BFS_ECUDA;
 	if (g->stepwise_last) {
 		if ((rc = run_stepwise(g, r, p, st))) return rc;
 	} else {
@@ -773,7 +775,7 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 		p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
 		for (uint32_t i = 0; i < ns; ++i) {
 			p.source = sources[i];
-			if ((rc = launch_init(g->dg, r, st, g->num_sms))) return rc;
+			if ((rc = launch_init(g->dg, r, st, g->num_sms, &p))) return rc;
 			if ((rc = launch_persistent(g->dg, r, p, g->batch, g->grid, g->smem, st))) return rc;
 			k_levels_u8<<<g->num_sms * 4, 512, 0, st>>>(g->level_buf, levels + (size_t) i * g->n, g->n, r.stats, a.ctl);
 		}
@@ -912,7 +914,7 @@ int bc_enqueue(bfs_graph *g, uint32_t source, uint32_t *sigma, float *delta, flo
 	p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
 	int rc;
 	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
-	if ((rc = launch_init(g->dg, r, st, g->num_sms))) return rc;
+	if ((rc = launch_init(g->dg, r, st, g->num_sms, &p))) return rc;
 	if ((rc = launch_persistent(g->dg, r, p, g->batch, g->grid, g->smem, st))) return rc;
 	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
 	BcArgs a{};

@@ -38,6 +38,17 @@ namespace bfsg {
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 
+// Per-CTA phase stamps for profiling builds (nvcc -DBFS_CTA_TIMERS): thread 0
+// of every CTA records the globaltimer at fixed points of the first 16 steps.
+#ifdef BFS_CTA_TIMERS
+constexpr int kProfPoints = 10;
+__device__ unsigned long long g_cta_prof[16][kProfPoints][kMaxGrid];
+#define CTA_STAMP(step, k) \
+	do { if (threadIdx.x == 0 && (step) < 16) g_cta_prof[step][k][blockIdx.x] = global_timer_ns(); } while (0)
+#else
+#define CTA_STAMP(step, k) do { } while (0)
+#endif
+
 struct ThreadAcc {
 	unsigned long long count, degsum, td_edges, td_vertices, bu_words, bu_slices, bu_groups, bu_vertices;
 };
@@ -86,15 +97,24 @@ __device__ __forceinline__ void wq_flush_all(WarpQ &wq) {
 // visited pre-load (it keeps already-visited hub destinations off the atomic
 // unit), the claiming atomicOr, the degree load of the claimed -- is issued
 // for all candidates before any result is used, so a lane waits for three
-// round trips per batch of edges, not per edge.
-// Claimed vertices get their level and parent and are staged for the next
-// queue bucket of their out-degree.
+// round trips per batch of edges, not per edge.  Lanes holding the same
+// destination in the same slot leave the claim to the lowest of them (R-MAT
+// frontiers send many edges to a few hub destinations, and claims of one
+// address are serialised at L2).
+// Claimed vertices get their level and parent, their bit in the next
+// frontier's bitmap `nbm` (so that a bottom-up step after this one needs no
+// queue -> bitmap conversion) and are staged for the next queue bucket of
+// their out-degree.
 __device__ __forceinline__ void visit_and_append(const bool (&has)[kTdPerLane], const uint32_t (&u)[kTdPerLane],
-		const uint32_t (&v)[kTdPerLane], int32_t next_level, const DevGraph &g, const RunCtx &r, WarpQ &wq,
-		const StepParams &p, ThreadAcc &acc) {
+		const uint32_t (&v)[kTdPerLane], int32_t next_level, const DevGraph &g, const RunCtx &r, uint32_t *nbm,
+		WarpQ &wq, const StepParams &p, ThreadAcc &acc) {
 	uint32_t word[kTdPerLane];
 #pragma unroll
-	for (int q = 0; q < kTdPerLane; ++q) word[q] = has[q] ? ld_cg(r.vis + (v[q] >> 5)) : ~0u;
+	for (int q = 0; q < kTdPerLane; ++q) {
+		const unsigned peers = __match_any_sync(kFull, has[q] ? v[q] : 0xFFFFFFFFu);
+		const bool lead = has[q] && (peers & lanemask_lt()) == 0;
+		word[q] = lead ? ld_cg(r.vis + (v[q] >> 5)) : ~0u;
+	}
 	// The claim is a compare-and-swap on the destination's own level (-1 ->
 	// next level): only edges to the same destination contend, not the 32
 	// destinations of a bitmap word.  The visited bit follows with a
@@ -109,7 +129,10 @@ __device__ __forceinline__ void visit_and_append(const bool (&has)[kTdPerLane], 
 	uint32_t deg[kTdPerLane];
 #pragma unroll
 	for (int q = 0; q < kTdPerLane; ++q) {
-		if (claimed[q]) atomicOr(r.vis + (v[q] >> 5), 1u << (v[q] & 31));
+		if (claimed[q]) {
+			atomicOr(r.vis + (v[q] >> 5), 1u << (v[q] & 31));
+			atomicOr(nbm + (v[q] >> 5), 1u << (v[q] & 31));
+		}
 		deg[q] = claimed[q] ? __ldg(g.row_off + v[q] + 1) - __ldg(g.row_off + v[q]) : 0u;
 	}
 	uint32_t cnt[3] = {0, 0, 0};
@@ -165,19 +188,20 @@ __device__ __forceinline__ uint32_t block_incl_scan(uint32_t x) {
 // ---------------------------------------------------------------------------
 // Top-down step (BFS_kernel_sparse + update_sparse, apps/bfs_simd/bfs.cpp:467-711)
 // ---------------------------------------------------------------------------
+// The frontier's queue sizes nS, nM, nL (small, medium, large out-degree)
+// come from the caller, which loads them together with the step totals.
 __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t step,
-		uint32_t *smem, ThreadAcc &acc) {
+		uint32_t nS, uint32_t nM, uint32_t nL, uint32_t *smem, ThreadAcc &acc) {
 	const uint32_t cur = step & 1, nxt = (step + 1) & 1;
-	const StepCounters *in = r.ctr + (step + 2) % 3;
 	StepCounters *out = r.ctr + step % 3;
-	const uint32_t nS = ld_volatile(&in->tail[0]);
-	const uint32_t nM = ld_volatile(&in->tail[1]);
-	const uint32_t nL = ld_volatile(&in->tail[2]);
+	uint32_t *nbm = r.bm[step % 3];
 	const uint32_t *qS = r.q[cur][0], *qM = r.q[cur][1], *qL = r.q[cur][2];
 	uint32_t *const qn[3] = {r.q[nxt][0], r.q[nxt][1], r.q[nxt][2]};
 	const int32_t nl = (int32_t) step + 1;
 	const unsigned lane = lane_id(), wid = warp_id();
-	const uint64_t gwarp = (uint64_t) blockIdx.x * kWarps + wid;
+	// warps numbered across CTAs first, so that a small amount of work is
+	// spread over all SMs rather than the first CTAs' warps
+	const uint64_t gwarp = (uint64_t) wid * gridDim.x + blockIdx.x;
 	const uint64_t nwarps = (uint64_t) gridDim.x * kWarps;
 	constexpr uint32_t kSpan = 32 * kTdPerLane;  // edges per warp iteration
 	WarpQ wq{smem + (size_t) wid * 3 * kWqCap, {0, 0, 0}, qn, out->tail};
@@ -206,7 +230,7 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 		xsh.pre[threadIdx.x] = incl;
 		__syncthreads();
 		const uint32_t total = xsh.pre[cn - 1];
-		const uint64_t per = ((total + nwarps - 1) / nwarps + kSpan - 1) / kSpan * kSpan;
+		const uint64_t per = (total + nwarps - 1) / nwarps;
 		const uint64_t lo = min((uint64_t) total, gwarp * per), hi = min((uint64_t) total, lo + per);
 		for (uint64_t f0 = lo; f0 < hi; f0 += kSpan) {
 #pragma unroll
@@ -224,11 +248,12 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 				uu[q] = xsh.u[jj];
 				vv[q] = has[q] ? __ldg(g.col + xsh.beg[jj] + (uint32_t) (f - prev)) : 0u;
 			}
-			visit_and_append(has, uu, vv, nl, g, r, wq, p, acc);
+			visit_and_append(has, uu, vv, nl, g, r, nbm, wq, p, acc);
 		}
 		if (blockIdx.x == 0 && threadIdx.x == 0) { acc.td_edges += total; acc.td_vertices += cn; }
 		__syncthreads();
 	}
+	CTA_STAMP(step, 6);
 	// Medium out-degree, many vertices: a CTA expands a chunk of up to 32
 	// vertices as one flat edge list.  Chunks (about 8 per CTA) are handed out
 	// by a counter, the next one fetched while this one runs: medium degrees
@@ -274,7 +299,7 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 					uu[q] = xsh.u[jj];
 					vv[q] = has[q] ? __ldg(g.col + xsh.beg[jj] + (uint32_t) (f - prev)) : 0u;
 				}
-				visit_and_append(has, uu, vv, nl, g, r, wq, p, acc);
+				visit_and_append(has, uu, vv, nl, g, r, nbm, wq, p, acc);
 			}
 			if (threadIdx.x == 0) {
 				acc.td_edges += total;
@@ -285,11 +310,15 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 			ci = s_next;
 		}
 	}
-	// Small out-degree: one warp expands 32 vertices together; lanes take
-	// consecutive edges of the warp's combined edge list.
-	for (uint64_t base = gwarp * 32; base < nS; base += nwarps * 32) {
+	CTA_STAMP(step, 7);
+	// Small out-degree: one warp expands up to 32 vertices together; lanes
+	// take consecutive edges of the warp's combined edge list.  A small
+	// frontier is spread thinner (down to one vertex per warp), so that its
+	// chain of dependent loads runs on many warps at once.
+	const uint32_t vpw = nS >= nwarps * 32 ? 32u : (uint32_t) max((uint64_t) 1, (nS + nwarps - 1) / nwarps);
+	for (uint64_t base = gwarp * vpw; base < nS; base += nwarps * vpw) {
 		const uint64_t i = base + lane;
-		const bool valid = i < nS;
+		const bool valid = lane < vpw && i < nS;
 		const uint32_t u = valid ? ld_cg(qS + i) : 0u;
 		const uint32_t beg = valid ? __ldg(g.row_off + u) : 0u;
 		const uint32_t deg = valid ? __ldg(g.row_off + u + 1) - beg : 0u;
@@ -313,7 +342,7 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 				const uint32_t oe = __shfl_sync(kFull, excl, lo);
 				vv[q] = has[q] ? __ldg(g.col + ob + (f - oe)) : 0u;
 			}
-			visit_and_append(has, uu, vv, nl, g, r, wq, p, acc);
+			visit_and_append(has, uu, vv, nl, g, r, nbm, wq, p, acc);
 		}
 		const unsigned nvalid = (unsigned) __popc(__ballot_sync(kFull, valid));
 		if (lane == 0) {
@@ -321,6 +350,7 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 			acc.td_vertices += nvalid;
 		}
 	}
+	CTA_STAMP(step, 8);
 	wq_flush_all(wq);
 }
 
@@ -416,19 +446,25 @@ __device__ __shared__ TmaMeta tma_meta[kTmaStages];
 __device__ __shared__ alignas(8) uint64_t tma_bar[kTmaStages];    // stage filled
 __device__ __shared__ alignas(8) uint64_t tma_empty[kTmaStages];  // stage released by every consumer warp
 
-// Claims the next column group; loads its visited bits into vis_s and a copy
-// into nxt_s, and counts the vertices with an in-edge that are still unvisited.
-// Returns false when no group is left.  Uniform across the CTA.
+// Claims the next work item -- a column group, or with `split` > 1 one of
+// `split` equal parts (in 32-vertex words) of a column group -- loads its
+// visited bits into vis_s and a copy into nxt_s, and counts the vertices
+// with an in-edge that are still unvisited.  Returns false when no item is
+// left.  Uniform across the CTA.
 __device__ __forceinline__ bool dense_group_begin(const DevGraph &g, const RunCtx &r, StepCounters *out, uint32_t *vis_s,
-		uint32_t *nxt_s, DenseGroup &gr, uint32_t *hin_s = nullptr) {
+		uint32_t *nxt_s, DenseGroup &gr, uint32_t *hin_s = nullptr, uint32_t split = 1) {
 	__syncthreads();
 	if (threadIdx.x == 0) { dsh.group = atomicAdd(&out->work, 1u); dsh.unsettled = 0; dsh.stop = 0; }
 	__syncthreads();
-	gr.gi = dsh.group;
-	if (gr.gi >= g.num_groups) return false;
+	const uint32_t item = dsh.group;
+	if (item >= g.num_groups * split) return false;
+	gr.gi = item / split;
+	const uint32_t part = item % split;
 	const uint32_t c0 = __ldg(g.group_col + gr.gi), c1 = __ldg(g.group_col + gr.gi + 1);
-	gr.v0 = (uint64_t) c0 * g.w;
-	gr.v1 = min((uint64_t) c1 * g.w, (uint64_t) g.n);
+	const uint64_t a = (uint64_t) c0 * g.w, b = min((uint64_t) c1 * g.w, (uint64_t) g.n);
+	const uint64_t words = (b - a + 31) / 32;
+	gr.v0 = min(b, a + 32 * (words * part / split));
+	gr.v1 = min(b, a + 32 * (words * (part + 1) / split));
 	gr.gw = (uint32_t) ((gr.v1 - gr.v0 + 31) / 32);
 	uint32_t uns = 0;
 	for (uint32_t j = threadIdx.x; j < gr.gw; j += kThreads) {
@@ -853,6 +889,10 @@ __device__ __forceinline__ void phase_dense_tma(const DevGraph &g, const RunCtx 
 // settled by then go to a shared-memory queue that whole warps scan 32 edges
 // at a time with a ballot to stop at the first hit.
 constexpr uint32_t kPullShort = 4;
+// Work items of a pull step: each column group in this many parts, handed
+// out dynamically (whole groups left a few CTAs with most of the work: the
+// early exit makes a group's cost depend on where its frontier sources are).
+constexpr uint32_t kPullSplit = 4;
 
 __device__ __forceinline__ bool frontier_bit(const uint32_t *cur, uint32_t u) {
 	return (ld_cg(cur + (u >> 5)) >> (u & 31)) & 1u;
@@ -875,7 +915,7 @@ __device__ __forceinline__ void phase_pull(const DevGraph &g, const RunCtx &r, u
 	DenseGroup gr;
 	unsigned long long cyc[4] = {0, 0, 0, 0};
 	long long t0 = clock64();
-	while (dense_group_begin(g, r, out, vis_s, vis0_s, gr, hin_s)) {
+	while (dense_group_begin(g, r, out, vis_s, vis0_s, gr, hin_s, kPullSplit)) {
 		{ long long t1 = clock64(); cyc[0] += t1 - t0; t0 = t1; }
 		if (dsh.unsettled == 0) continue;
 		if (threadIdx.x == 0) { acc.bu_groups++; dsh.nlist = 0; }
@@ -1024,12 +1064,16 @@ __device__ __forceinline__ void flush_step(ThreadAcc &acc, const RunCtx &r, uint
 	acc.degsum = 0;
 }
 
-// Sums the partials of `slot` over the grid (all threads call).
+// Sums the partials of `slot` over the grid (all threads call), and loads
+// the slot's three queue tails in the same round trip.
 __device__ __forceinline__ void step_totals(const RunCtx &r, uint32_t slot, uint32_t *count,
-		unsigned long long *degsum) {
+		unsigned long long *degsum, uint32_t (&tails)[3]) {
 	// every thread loads at most a few partials (one L2 round trip), then a
-	// block reduction
+	// block reduction; three threads load the tails (every thread loading
+	// them put hundreds of thousands of requests on one hot line)
 	__shared__ unsigned long long red[2][kWarps];
+	__shared__ uint32_t s_tails[3];
+	if (threadIdx.x < 3) s_tails[threadIdx.x] = __ldcg(&r.ctr[slot].tail[threadIdx.x]);
 	unsigned long long c = 0, d = 0;
 	const unsigned long long *pc = part_at(r, slot, 0), *pd = part_at(r, slot, 1);
 	for (uint32_t i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
@@ -1045,6 +1089,9 @@ __device__ __forceinline__ void step_totals(const RunCtx &r, uint32_t slot, uint
 	for (int w = 0; w < kWarps; ++w) { tc += red[0][w]; td += red[1][w]; }
 	*count = (uint32_t) tc;
 	*degsum = td;
+	tails[0] = s_tails[0];
+	tails[1] = s_tails[1];
+	tails[2] = s_tails[2];
 	__syncthreads();
 }
 
@@ -1095,22 +1142,44 @@ __device__ void seed_source(const DevGraph &g, const RunCtx &r, const StepParams
 // ---------------------------------------------------------------------------
 // Kernels
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_init(DevGraph g, RunCtx r) {
+// Clears the run state and, when `seed`, seeds the source in the same
+// writes (the values written at the source's indices are the seeded ones),
+// so the traversal kernel needs no seeding step and no barrier after it.
+__global__ void __launch_bounds__(kThreads) k_init(DevGraph g, RunCtx r, StepParams p, int seed) {
 	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
 	const uint64_t t0 = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
+	const uint32_t s = p.source;
 	for (uint64_t i = t0; i < g.n; i += stride) {
-		r.level[i] = -1;
-		if (r.parent) r.parent[i] = kUnvisitedWord;
+		const bool src = seed && i == s;
+		r.level[i] = src ? 0 : -1;
+		if (r.parent) r.parent[i] = src ? s : kUnvisitedWord;
 	}
-	for (uint64_t i = t0; i < g.nwords; i += stride) r.vis[i] = 0;
+	for (uint64_t i = t0; i < g.nwords; i += stride) r.vis[i] = (seed && i == (s >> 5)) ? 1u << (s & 31) : 0u;
 	for (uint64_t i = t0; i < g.bm_words; i += stride) {
 		r.bm[0][i] = 0;
 		r.bm[1][i] = 0;
 		r.bm[2][i] = 0;
 	}
 	for (uint64_t i = t0; i < g.num_stripes; i += stride) { r.sf[0][i] = 0; r.sf[1][i] = 0; r.sf[2][i] = 0; }
-	if (t0 < 3 * sizeof(StepCounters) / 4) ((uint32_t *) r.ctr)[t0] = 0;
-	for (uint64_t i = t0; i < 6ull * kMaxGrid; i += stride) r.part[i] = 0;
+	// the source is the frontier "produced by step -1": the queue bucket of
+	// its out-degree, counter slot 2, CTA 0's partials of slot 2
+	constexpr uint64_t kCtrWords = 3 * sizeof(StepCounters) / 4;
+	uint32_t deg = 0, bk = 0;
+	if (seed && t0 <= kCtrWords) {
+		deg = __ldg(g.row_off + s + 1) - __ldg(g.row_off + s);
+		bk = bucket_of(deg, p);
+	}
+	if (t0 < kCtrWords) {
+		const uint64_t tail_idx = (2 * sizeof(StepCounters) + bk * sizeof(unsigned)) / 4;
+		((uint32_t *) r.ctr)[t0] = (seed && t0 == tail_idx) ? 1u : 0u;
+	}
+	if (seed && t0 == kCtrWords) r.q[0][bk][0] = s;
+	for (uint64_t i = t0; i < 6ull * kMaxGrid; i += stride) {
+		unsigned long long x = 0;
+		if (seed && i == (2 * 2 + 0) * (uint64_t) kMaxGrid) x = 1;
+		if (seed && i == (2 * 2 + 1) * (uint64_t) kMaxGrid) x = __ldg(g.row_off + s + 1) - __ldg(g.row_off + s);
+		r.part[i] = x;
+	}
 	if (t0 < sizeof(DevStats) / 4) ((uint32_t *) r.stats)[t0] = 0;
 	if (t0 < 2) r.bar[t0] = 0;
 	if (t0 == 0) *r.err = 0;
@@ -1120,22 +1189,30 @@ __global__ void k_seed(DevGraph g, RunCtx r, StepParams p) {
 	if (blockIdx.x == 0 && threadIdx.x == 0) seed_source(g, r, p);
 }
 
+// All steps of one traversal in one cooperative launch.  k_init has seeded
+// the source, so step 0 starts at once.  The run statistics that only CTA 0
+// keeps are held in its registers and written once at the end, so CTA 0
+// (which every light step waits for) takes no extra round trips.
 __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunCtx r, StepParams p, uint32_t batch) {
 	extern __shared__ __align__(128) uint32_t smem[];
+	__shared__ uint32_t s_conv_tails[3];
 	ThreadAcc acc{0, 0, 0, 0, 0, 0, 0, 0};
 	bool ok = true;
 	dense_tma_init();
-	if (blockIdx.x == 0 && threadIdx.x == 0) seed_source(g, r, p);
-	ok = grid_barrier(r.bar, r.err);
+	const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+	unsigned long long st_reached = 0, st_edges = 0;
+	uint32_t st_dense = 0;
 	bool last_dense = false;
 	uint32_t step = 0;
 	for (; ok; ++step) {
-		uint32_t fsize;
+		uint32_t fsize, tails[3];
 		unsigned long long dsum;
-		step_totals(r, (step + 2) % 3, &fsize, &dsum);
-		if (blockIdx.x == 0 && threadIdx.x == 0) {
-			r.stats->reached += fsize;
-			r.stats->edges_traversed += dsum;
+		CTA_STAMP(step, 0);
+		step_totals(r, (step + 2) % 3, &fsize, &dsum, tails);
+		CTA_STAMP(step, 1);
+		if (leader) {
+			st_reached += fsize;
+			st_edges += dsum;
 			if (step < 257) r.stats->t_step[step] = global_timer_ns();
 		}
 		if (fsize == 0) break;
@@ -1145,36 +1222,51 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 			dense = (unsigned long long) fsize + dsum > thr;
 		}
 		clear_slot(g, r, (step + 1) % 3);
+		CTA_STAMP(step, 2);
 		if (dense) {
-			if (!last_dense) {
-				phase_to_dense(g, r, step, p.bottom_up != 0);
+			// the top-down step that produced this frontier also set its
+			// bitmap; only the streaming variant needs the stripe flags built
+			if (!last_dense && p.bottom_up != 0) {
+				phase_to_dense(g, r, step, true);
 				if (!(ok = grid_barrier(r.bar, r.err))) break;
-				if (blockIdx.x == 0 && threadIdx.x == 0 && step < 256) r.stats->t_conv[step] = global_timer_ns();
+				if (leader && step < 256) r.stats->t_conv[step] = global_timer_ns();
 			}
+			CTA_STAMP(step, 3);
 			phase_dense(g, r, p, step, batch, smem, acc);
 		} else {
 			if (last_dense) {
 				phase_to_sparse(g, r, p, step);
 				if (!(ok = grid_barrier(r.bar, r.err))) break;
-				if (blockIdx.x == 0 && threadIdx.x == 0 && step < 256) r.stats->t_conv[step] = global_timer_ns();
+				if (leader && step < 256) r.stats->t_conv[step] = global_timer_ns();
+				if (threadIdx.x < 3) s_conv_tails[threadIdx.x] = __ldcg(&r.ctr[(step + 2) % 3].tail[threadIdx.x]);
+				__syncthreads();
+				tails[0] = s_conv_tails[0];
+				tails[1] = s_conv_tails[1];
+				tails[2] = s_conv_tails[2];
 			}
-			phase_expand(g, r, p, step, smem, acc);
+			CTA_STAMP(step, 3);
+			phase_expand(g, r, p, step, tails[0], tails[1], tails[2], smem, acc);
 		}
+		CTA_STAMP(step, 4);
 		flush_step(acc, r, step % 3);
+		CTA_STAMP(step, 5);
 		if (threadIdx.x == 0 && step < 256) {
 			const unsigned long long t = global_timer_ns();
 			atomicMax(&r.stats->t_work_max[step], t);
 			atomicMax(&r.stats->t_work_min_inv[step], ~t);
 		}
-		if (blockIdx.x == 0 && threadIdx.x == 0) {
+		if (leader) {
 			if (step < 256) r.stats->trace[step] = dense ? 1 : 0;
-			if (dense) r.stats->dense_steps++;
+			st_dense += dense;
 		}
 		last_dense = dense;
 		ok = grid_barrier(r.bar, r.err);
 	}
 	flush_stats(acc, r.stats);
-	if (blockIdx.x == 0 && threadIdx.x == 0) {
+	if (leader) {
+		r.stats->reached = st_reached;
+		r.stats->edges_traversed = st_edges;
+		r.stats->dense_steps = st_dense;
 		r.stats->num_steps = step;
 		r.stats->status = *(volatile int *) r.err;
 	}
@@ -1193,7 +1285,9 @@ __global__ void __launch_bounds__(kThreads) k_step_to_sparse(DevGraph g, RunCtx 
 __global__ void __launch_bounds__(kThreads) k_step_expand(DevGraph g, RunCtx r, StepParams p, uint32_t step) {
 	extern __shared__ __align__(128) uint32_t smem[];
 	ThreadAcc acc{0, 0, 0, 0, 0, 0, 0, 0};
-	phase_expand(g, r, p, step, smem, acc);
+	const StepCounters *in = r.ctr + (step + 2) % 3;
+	phase_expand(g, r, p, step, ld_volatile(&in->tail[0]), ld_volatile(&in->tail[1]), ld_volatile(&in->tail[2]),
+			smem, acc);
 	flush_step(acc, r, step % 3);
 	flush_stats(acc, r.stats);
 }
@@ -1238,8 +1332,10 @@ int persistent_grid(const DevGraph &g, uint32_t batch, int num_sms, int *grid, s
 	return BFS_OK;
 }
 
-int launch_init(const DevGraph &g, const RunCtx &r, cudaStream_t st, int num_sms) {
-	k_init<<<num_sms * 4, kThreads, 0, st>>>(g, r);
+int launch_init(const DevGraph &g, const RunCtx &r, cudaStream_t st, int num_sms, const StepParams *seed) {
+	StepParams p{};
+	if (seed) p = *seed;
+	k_init<<<num_sms * 4, kThreads, 0, st>>>(g, r, p, seed != nullptr);
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }
 
@@ -1269,5 +1365,11 @@ int launch_step(int kind, const DevGraph &g, const RunCtx &r, const StepParams &
 }
 
 int kernel_threads() { return kThreads; }
+
+#ifdef BFS_CTA_TIMERS
+extern "C" int bfs_debug_cta_profile(unsigned long long *host) {
+	return cudaMemcpyFromSymbol(host, g_cta_prof, sizeof(g_cta_prof)) == cudaSuccess ? 0 : BFS_ECUDA;
+}
+#endif
 
 } // namespace bfsg
