@@ -94,13 +94,11 @@ __device__ __forceinline__ void wq_flush_all(WarpQ &wq) {
 
 // All 32 lanes of the warp call this with up to kTdPerLane candidate edges
 // u[q] -> v[q] each (has[q] false for an empty slot).  Each stage -- the
-// visited pre-load (it keeps already-visited hub destinations off the atomic
-// unit), the claiming atomicOr, the degree load of the claimed -- is issued
-// for all candidates before any result is used, so a lane waits for three
-// round trips per batch of edges, not per edge.  Lanes holding the same
-// destination in the same slot leave the claim to the lowest of them (R-MAT
-// frontiers send many edges to a few hub destinations, and claims of one
-// address are serialised at L2).
+// claiming compare-and-swap, the degree load of the claimed -- is issued for
+// all candidates before any result is used, so a lane waits for two round
+// trips per batch of edges, not per edge.  (A visited-bitmap pre-load before
+// the claim kept visited destinations off the atomic unit but cost a round
+// trip per batch: measured slower on R-MAT frontiers.)
 // Claimed vertices get their level and parent, their bit in the next
 // frontier's bitmap `nbm` (so that a bottom-up step after this one needs no
 // queue -> bitmap conversion) and are staged for the next queue bucket of
@@ -108,24 +106,14 @@ __device__ __forceinline__ void wq_flush_all(WarpQ &wq) {
 __device__ __forceinline__ void visit_and_append(const bool (&has)[kTdPerLane], const uint32_t (&u)[kTdPerLane],
 		const uint32_t (&v)[kTdPerLane], int32_t next_level, const DevGraph &g, const RunCtx &r, uint32_t *nbm,
 		WarpQ &wq, const StepParams &p, ThreadAcc &acc) {
-	uint32_t word[kTdPerLane];
-#pragma unroll
-	for (int q = 0; q < kTdPerLane; ++q) {
-		const unsigned peers = __match_any_sync(kFull, has[q] ? v[q] : 0xFFFFFFFFu);
-		const bool lead = has[q] && (peers & lanemask_lt()) == 0;
-		word[q] = lead ? ld_cg(r.vis + (v[q] >> 5)) : ~0u;
-	}
 	// The claim is a compare-and-swap on the destination's own level (-1 ->
 	// next level): only edges to the same destination contend, not the 32
 	// destinations of a bitmap word.  The visited bit follows with a
 	// reduction whose result nobody waits for.
 	bool claimed[kTdPerLane];
 #pragma unroll
-	for (int q = 0; q < kTdPerLane; ++q) {
-		claimed[q] = false;
-		if (!(word[q] & (1u << (v[q] & 31))))
-			claimed[q] = atomicCAS((int *) r.level + v[q], -1, next_level) == -1;
-	}
+	for (int q = 0; q < kTdPerLane; ++q)
+		claimed[q] = has[q] && atomicCAS((int *) r.level + v[q], -1, next_level) == -1;
 	uint32_t deg[kTdPerLane];
 #pragma unroll
 	for (int q = 0; q < kTdPerLane; ++q) {
@@ -452,9 +440,16 @@ __device__ __shared__ alignas(8) uint64_t tma_empty[kTmaStages];  // stage relea
 // with an in-edge that are still unvisited.  Returns false when no item is
 // left.  Uniform across the CTA.
 __device__ __forceinline__ bool dense_group_begin(const DevGraph &g, const RunCtx &r, StepCounters *out, uint32_t *vis_s,
-		uint32_t *nxt_s, DenseGroup &gr, uint32_t *hin_s = nullptr, uint32_t split = 1) {
+		uint32_t *nxt_s, DenseGroup &gr, uint32_t *hin_s = nullptr, uint32_t split = 1, bool first = false) {
 	__syncthreads();
-	if (threadIdx.x == 0) { dsh.group = atomicAdd(&out->work, 1u); dsh.unsettled = 0; dsh.stop = 0; }
+	if (threadIdx.x == 0) {
+		// with `first`, a CTA's first item is its own index (no atomic: the
+		// whole grid asking at once queued on one line); later items are
+		// counted from gridDim.x
+		dsh.group = first ? blockIdx.x : (split > 1 ? gridDim.x : 0u) + atomicAdd(&out->work, 1u);
+		dsh.unsettled = 0;
+		dsh.stop = 0;
+	}
 	__syncthreads();
 	const uint32_t item = dsh.group;
 	if (item >= g.num_groups * split) return false;
@@ -915,7 +910,9 @@ __device__ __forceinline__ void phase_pull(const DevGraph &g, const RunCtx &r, u
 	DenseGroup gr;
 	unsigned long long cyc[4] = {0, 0, 0, 0};
 	long long t0 = clock64();
-	while (dense_group_begin(g, r, out, vis_s, vis0_s, gr, hin_s, kPullSplit)) {
+	bool first = true;
+	while (dense_group_begin(g, r, out, vis_s, vis0_s, gr, hin_s, kPullSplit, first)) {
+		first = false;
 		{ long long t1 = clock64(); cyc[0] += t1 - t0; t0 = t1; }
 		if (dsh.unsettled == 0) continue;
 		if (threadIdx.x == 0) { acc.bu_groups++; dsh.nlist = 0; }
@@ -1202,6 +1199,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 	const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
 	unsigned long long st_reached = 0, st_edges = 0;
 	uint32_t st_dense = 0;
+	unsigned epoch = 0;  // grid barriers this CTA has passed
 	bool last_dense = false;
 	uint32_t step = 0;
 	for (; ok; ++step) {
@@ -1228,7 +1226,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 			// bitmap; only the streaming variant needs the stripe flags built
 			if (!last_dense && p.bottom_up != 0) {
 				phase_to_dense(g, r, step, true);
-				if (!(ok = grid_barrier(r.bar, r.err))) break;
+				if (!(ok = grid_sync(r.bar, epoch, r.err))) break;
 				if (leader && step < 256) r.stats->t_conv[step] = global_timer_ns();
 			}
 			CTA_STAMP(step, 3);
@@ -1236,7 +1234,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 		} else {
 			if (last_dense) {
 				phase_to_sparse(g, r, p, step);
-				if (!(ok = grid_barrier(r.bar, r.err))) break;
+				if (!(ok = grid_sync(r.bar, epoch, r.err))) break;
 				if (leader && step < 256) r.stats->t_conv[step] = global_timer_ns();
 				if (threadIdx.x < 3) s_conv_tails[threadIdx.x] = __ldcg(&r.ctr[(step + 2) % 3].tail[threadIdx.x]);
 				__syncthreads();
@@ -1260,7 +1258,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 			st_dense += dense;
 		}
 		last_dense = dense;
-		ok = grid_barrier(r.bar, r.err);
+		ok = grid_sync(r.bar, epoch, r.err);
 	}
 	flush_stats(acc, r.stats);
 	if (leader) {

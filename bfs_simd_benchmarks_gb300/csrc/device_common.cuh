@@ -113,6 +113,42 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
 	return s_ok != 0;
 }
 
+// Grid barrier over a monotonic arrival counter (*count is 0 when the launch
+// starts; `epoch` is the number of these barriers the CTA has passed, the
+// same in every CTA).  Arrival is a fire-and-forget add after a fence; the
+// barrier is complete when the counter reaches gridDim.x * (epoch + 1), which
+// every CTA sees by polling the counter itself -- no generation word to read
+// before arriving, no reset, no separate release write.  Bounded like
+// grid_barrier: gives up after kWaitLimitNs, records BFS_ETIMEOUT.
+__device__ __forceinline__ bool grid_sync(unsigned *count, unsigned &epoch, int *err) {
+	__shared__ int s_sync_ok;
+	__syncthreads();
+	++epoch;
+	if (threadIdx.x == 0) {
+		int ok = 1;
+		const unsigned target = gridDim.x * epoch;
+		__threadfence();
+		atomicAdd(count, 1u);
+		uint64_t t0 = 0;
+		for (uint32_t it = 0;; ++it) {
+			if (ld_volatile(count) >= target) break;
+			if (*(volatile int *) err) { ok = 0; break; }
+			if (it == 0) t0 = global_timer_ns();
+			else if (it > kWaitLimitIters || global_timer_ns() - t0 > kWaitLimitNs) {
+				atomicExch(err, 6 /* BFS_ETIMEOUT */);
+				ok = 0;
+				break;
+			}
+			if (it > 16) __nanosleep(it < 256 ? 32 : 128);
+		}
+		__threadfence();
+		if (*(volatile int *) err) ok = 0;
+		s_sync_ok = ok;
+	}
+	__syncthreads();
+	return s_sync_ok != 0;
+}
+
 // ---- shared-memory barriers and 1-D bulk copies (TMA) ---------------------
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
 	return (uint32_t) __cvta_generic_to_shared(p);
