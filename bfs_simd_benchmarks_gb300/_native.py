@@ -76,6 +76,8 @@ class Options(C.Structure):
         ("batch_single_max", C.c_uint32),
         ("batch_push_div", C.c_uint32),
         ("bc_level_bytes", C.c_uint32),
+        ("wait_limit_us", C.c_uint32),
+        ("test_hold_barrier", C.c_uint32),
     ]
 
 

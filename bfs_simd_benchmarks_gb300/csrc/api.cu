@@ -104,6 +104,11 @@ namespace {
 
 int cuda_ok(cudaError_t e) { return e == cudaSuccess ? BFS_OK : BFS_ECUDA; }
 
+// Bound of the device-side waits of a run, from the options (0 = default).
+uint64_t wait_limit_ns(const bfs_options &o) {
+	return o.wait_limit_us ? (uint64_t) o.wait_limit_us * 1000ull : 2000000000ull;  // default 2 s
+}
+
 template <class T> int dev_alloc(bfs_graph *g, T **out, size_t count) {
 	size_t bytes = std::max<size_t>(sizeof(T) * count, 16);
 	void *p = nullptr;
@@ -258,6 +263,9 @@ int alloc_run(bfs_graph *g) {
 	if ((st = dev_alloc(g, &r.stats, 1))) return st;
 	if ((st = dev_alloc(g, &r.bar, 2))) return st;
 	if ((st = dev_alloc(g, &r.err, 1))) return st;
+	// the persistent kernel expects its barrier and status words zero at launch
+	if (cudaMemset(r.bar, 0, 2 * sizeof(unsigned)) != cudaSuccess || cudaMemset(r.err, 0, sizeof(int)) != cudaSuccess)
+		return BFS_ECUDA;
 	if ((st = dev_alloc(g, &g->level_buf, g->n))) return st;
 	if ((st = dev_alloc(g, &g->parent_buf, g->n))) return st;
 	if (cudaMallocHost(&g->h_stats, sizeof(DevStats)) != cudaSuccess) return BFS_ENOMEM;
@@ -545,12 +553,14 @@ int run_impl(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, 
 	p.bottom_up = g->opt.bottom_up;
 	p.to_dense_threshold = g->m / std::max<uint32_t>(1, g->opt.to_dense_ratio);
 	p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
+	p.wait_limit_ns = wait_limit_ns(g->opt);
+	p.hold_barrier = g->opt.test_hold_barrier;
 	int rc;
 	g->stepwise_last = g->opt.mode == BFS_MODE_STEPWISE;
 	if (cudaEventRecord(g->ev0, st) != cudaSuccess) return BFS_ECUDA;
-	// the persistent kernel starts from a source seeded by the clearing pass;
-	// the stepwise host loop seeds with its own launch
-	if ((rc = launch_init(g->dg, r, st, g->num_sms, g->stepwise_last ? nullptr : &p))) return rc;
+	// the persistent kernel clears the run state and seeds the source itself;
+	// the stepwise host loop clears and seeds with launches of their own
+	if (g->stepwise_last && (rc = launch_init(g->dg, r, st, g->num_sms))) return rc;
 	if (cudaEventRecord(g->evm, st) != cudaSuccess) return BFS_ECUDA;
 	if (g->stepwise_last) {
 		if ((rc = run_stepwise(g, r, p, st))) return rc;
@@ -747,6 +757,8 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 	a.last_bits = ns - 64 * (K - 1);
 	a.planes = planes;
 	a.push_div = std::max<uint32_t>(1, g->opt.batch_push_div);
+	a.wait_limit_ns = wait_limit_ns(g->opt);
+	a.hold_barrier = g->opt.test_hold_barrier;
 	a.row_off = g->dg.row_off;
 	a.col = g->dg.col;
 	a.in_off = g->dg.in_off;
@@ -773,9 +785,10 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 		p.bottom_up = g->opt.bottom_up;
 		p.to_dense_threshold = g->m / std::max<uint32_t>(1, g->opt.to_dense_ratio);
 		p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
+		p.wait_limit_ns = wait_limit_ns(g->opt);
+		p.hold_barrier = g->opt.test_hold_barrier;
 		for (uint32_t i = 0; i < ns; ++i) {
 			p.source = sources[i];
-			if ((rc = launch_init(g->dg, r, st, g->num_sms, &p))) return rc;
 			if ((rc = launch_persistent(g->dg, r, p, g->batch, g->grid, g->smem, st))) return rc;
 			k_levels_u8<<<g->num_sms * 4, 512, 0, st>>>(g->level_buf, levels + (size_t) i * g->n, g->n, r.stats, a.ctl);
 		}
@@ -912,9 +925,10 @@ int bc_enqueue(bfs_graph *g, uint32_t source, uint32_t *sigma, float *delta, flo
 	p.bottom_up = g->opt.bottom_up;
 	p.to_dense_threshold = g->m / std::max<uint32_t>(1, g->opt.to_dense_ratio);
 	p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
+	p.wait_limit_ns = wait_limit_ns(g->opt);
+	p.hold_barrier = g->opt.test_hold_barrier;
 	int rc;
 	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
-	if ((rc = launch_init(g->dg, r, st, g->num_sms, &p))) return rc;
 	if ((rc = launch_persistent(g->dg, r, p, g->batch, g->grid, g->smem, st))) return rc;
 	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
 	BcArgs a{};

@@ -81,7 +81,7 @@ struct RunCtx {
 	StepCounters *ctr;     // [3]
 	unsigned long long *part;  // [3 slots][2 (count, degsum)][kMaxGrid] per-CTA step totals
 	DevStats *stats;
-	unsigned *bar;         // [2] grid barrier
+	unsigned *bar;         // [2] grid barrier: arrival count, exits (0 between launches)
 	int *err;              // device status word
 };
 
@@ -92,6 +92,8 @@ struct StepParams {
 	uint32_t bottom_up;   // 0: pull over in-edge lists, 1: stream the packed tiles
 	unsigned long long to_dense_threshold;   // dense when frontier + degsum > this
 	unsigned long long to_sparse_threshold;  // stay dense while frontier + degsum > this
+	unsigned long long wait_limit_ns;        // bound of every grid-barrier wait
+	uint32_t hold_barrier;                   // tests: CTA 0 skips its arrival at this barrier (0 = off)
 };
 
 } // namespace bfsg

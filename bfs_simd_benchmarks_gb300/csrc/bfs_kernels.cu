@@ -1141,8 +1141,10 @@ __device__ void seed_source(const DevGraph &g, const RunCtx &r, const StepParams
 // ---------------------------------------------------------------------------
 // Clears the run state and, when `seed`, seeds the source in the same
 // writes (the values written at the source's indices are the seeded ones),
-// so the traversal kernel needs no seeding step and no barrier after it.
-__global__ void __launch_bounds__(kThreads) k_init(DevGraph g, RunCtx r, StepParams p, int seed) {
+// so the traversal needs no seeding step.  Grid-strided over the launch.
+// The barrier words and the status word are not touched: the persistent
+// kernel leaves them zero when it exits.
+__device__ __forceinline__ void init_run(const DevGraph &g, const RunCtx &r, const StepParams &p, bool seed) {
 	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
 	const uint64_t t0 = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
 	const uint32_t s = p.source;
@@ -1177,7 +1179,13 @@ __global__ void __launch_bounds__(kThreads) k_init(DevGraph g, RunCtx r, StepPar
 		if (seed && i == (2 * 2 + 1) * (uint64_t) kMaxGrid) x = __ldg(g.row_off + s + 1) - __ldg(g.row_off + s);
 		r.part[i] = x;
 	}
-	if (t0 < sizeof(DevStats) / 4) ((uint32_t *) r.stats)[t0] = 0;
+	for (uint64_t i = t0; i < sizeof(DevStats) / 4; i += stride) ((uint32_t *) r.stats)[i] = 0;
+}
+
+// The stepwise mode's clearing launch (the host loop seeds with k_seed).
+__global__ void __launch_bounds__(kThreads) k_init(DevGraph g, RunCtx r, StepParams p) {
+	init_run(g, r, p, false);
+	const uint64_t t0 = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
 	if (t0 < 2) r.bar[t0] = 0;
 	if (t0 == 0) *r.err = 0;
 }
@@ -1186,10 +1194,13 @@ __global__ void k_seed(DevGraph g, RunCtx r, StepParams p) {
 	if (blockIdx.x == 0 && threadIdx.x == 0) seed_source(g, r, p);
 }
 
-// All steps of one traversal in one cooperative launch.  k_init has seeded
-// the source, so step 0 starts at once.  The run statistics that only CTA 0
-// keeps are held in its registers and written once at the end, so CTA 0
-// (which every light step waits for) takes no extra round trips.
+// All steps of one traversal in one cooperative launch, the clearing of the
+// run state and the seeding of the source included (one grid barrier after
+// them).  The run statistics that only CTA 0 keeps are held in its
+// registers and written once at the end, so CTA 0 (which every light step
+// waits for) takes no extra round trips.  The grid barrier's arrival count,
+// the exit count and the status word are zero when the launch starts: the
+// last CTA to exit resets them.
 __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunCtx r, StepParams p, uint32_t batch) {
 	extern __shared__ __align__(128) uint32_t smem[];
 	__shared__ uint32_t s_conv_tails[3];
@@ -1202,6 +1213,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 	unsigned epoch = 0;  // grid barriers this CTA has passed
 	bool last_dense = false;
 	uint32_t step = 0;
+	init_run(g, r, p, true);
+	ok = grid_sync(r.bar, epoch, r.err, p.wait_limit_ns, p.hold_barrier);
 	for (; ok; ++step) {
 		uint32_t fsize, tails[3];
 		unsigned long long dsum;
@@ -1226,7 +1239,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 			// bitmap; only the streaming variant needs the stripe flags built
 			if (!last_dense && p.bottom_up != 0) {
 				phase_to_dense(g, r, step, true);
-				if (!(ok = grid_sync(r.bar, epoch, r.err))) break;
+				if (!(ok = grid_sync(r.bar, epoch, r.err, p.wait_limit_ns, p.hold_barrier))) break;
 				if (leader && step < 256) r.stats->t_conv[step] = global_timer_ns();
 			}
 			CTA_STAMP(step, 3);
@@ -1234,7 +1247,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 		} else {
 			if (last_dense) {
 				phase_to_sparse(g, r, p, step);
-				if (!(ok = grid_sync(r.bar, epoch, r.err))) break;
+				if (!(ok = grid_sync(r.bar, epoch, r.err, p.wait_limit_ns, p.hold_barrier))) break;
 				if (leader && step < 256) r.stats->t_conv[step] = global_timer_ns();
 				if (threadIdx.x < 3) s_conv_tails[threadIdx.x] = __ldcg(&r.ctr[(step + 2) % 3].tail[threadIdx.x]);
 				__syncthreads();
@@ -1258,7 +1271,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 			st_dense += dense;
 		}
 		last_dense = dense;
-		ok = grid_sync(r.bar, epoch, r.err);
+		ok = grid_sync(r.bar, epoch, r.err, p.wait_limit_ns, p.hold_barrier);
 	}
 	flush_stats(acc, r.stats);
 	if (leader) {
@@ -1267,6 +1280,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 		r.stats->dense_steps = st_dense;
 		r.stats->num_steps = step;
 		r.stats->status = *(volatile int *) r.err;
+	}
+	// the last CTA out resets the barrier and status words for the next launch
+	// (every CTA has left every barrier and read the status by then)
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		__threadfence();
+		if (atomicAdd(&r.bar[1], 1u) == gridDim.x - 1) {
+			atomicExch(&r.bar[0], 0u);
+			atomicExch(&r.bar[1], 0u);
+			atomicExch(r.err, 0);
+		}
 	}
 }
 
@@ -1330,10 +1354,9 @@ int persistent_grid(const DevGraph &g, uint32_t batch, int num_sms, int *grid, s
 	return BFS_OK;
 }
 
-int launch_init(const DevGraph &g, const RunCtx &r, cudaStream_t st, int num_sms, const StepParams *seed) {
+int launch_init(const DevGraph &g, const RunCtx &r, cudaStream_t st, int num_sms) {
 	StepParams p{};
-	if (seed) p = *seed;
-	k_init<<<num_sms * 4, kThreads, 0, st>>>(g, r, p, seed != nullptr);
+	k_init<<<num_sms * 4, kThreads, 0, st>>>(g, r, p);
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }
 

@@ -120,7 +120,10 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
 // every CTA sees by polling the counter itself -- no generation word to read
 // before arriving, no reset, no separate release write.  Bounded like
 // grid_barrier: gives up after kWaitLimitNs, records BFS_ETIMEOUT.
-__device__ __forceinline__ bool grid_sync(unsigned *count, unsigned &epoch, int *err) {
+// `limit_ns` bounds the wait; `hold` (tests only) = the epoch at which CTA 0
+// does not arrive, so that every CTA's wait runs out (0 = never).
+__device__ __forceinline__ bool grid_sync(unsigned *count, unsigned &epoch, int *err,
+		uint64_t limit_ns = kWaitLimitNs, unsigned hold = 0) {
 	__shared__ int s_sync_ok;
 	__syncthreads();
 	++epoch;
@@ -128,13 +131,13 @@ __device__ __forceinline__ bool grid_sync(unsigned *count, unsigned &epoch, int 
 		int ok = 1;
 		const unsigned target = gridDim.x * epoch;
 		__threadfence();
-		atomicAdd(count, 1u);
+		if (!(hold == epoch && blockIdx.x == 0)) atomicAdd(count, 1u);
 		uint64_t t0 = 0;
 		for (uint32_t it = 0;; ++it) {
 			if (ld_volatile(count) >= target) break;
 			if (*(volatile int *) err) { ok = 0; break; }
 			if (it == 0) t0 = global_timer_ns();
-			else if (it > kWaitLimitIters || global_timer_ns() - t0 > kWaitLimitNs) {
+			else if (it > kWaitLimitIters || global_timer_ns() - t0 > limit_ns) {
 				atomicExch(err, 6 /* BFS_ETIMEOUT */);
 				ok = 0;
 				break;

@@ -24,9 +24,9 @@ enum StepKind { kStepSeed = 0, kStepClear, kStepToDense, kStepToSparse, kStepExp
 
 size_t dense_smem_bytes(const DevGraph &g, uint32_t batch);
 int persistent_grid(const DevGraph &g, uint32_t batch, int num_sms, int *grid, size_t *smem);
-// Clears the run state; with `seed`, also seeds seed->source (the persistent
-// kernel then starts at step 0 without a seeding step).
-int launch_init(const DevGraph &g, const RunCtx &r, cudaStream_t st, int num_sms, const StepParams *seed);
+// Clears the run state for the stepwise mode (the persistent kernel clears
+// and seeds by itself).
+int launch_init(const DevGraph &g, const RunCtx &r, cudaStream_t st, int num_sms);
 int launch_persistent(const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t batch, int grid,
 		size_t smem, cudaStream_t st);
 int launch_step(int kind, const DevGraph &g, const RunCtx &r, const StepParams &p, uint32_t step,

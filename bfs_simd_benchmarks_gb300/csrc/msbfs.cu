@@ -714,6 +714,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 	const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
 	const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
 	const size_t nK = (size_t) a.n * a.K;
+	unsigned epoch = 0;  // grid barriers passed (the control block, and its arrival count, start zeroed)
 	if (leader) ctl->stats.t_start = global_timer_ns();
 	// clear (the control block was zeroed by the host)
 	for (size_t i = t0; i < nK; i += stride) { a.vis[i] = 0; a.hist[i] = 0; }
@@ -723,7 +724,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 		a.touched[i] = 0;
 		a.seed_flag[i] = 0;
 	}
-	bool ok = grid_barrier(ctl->bar, &ctl->err);
+	bool ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
 	// plane 0: every source reaches itself
 	if (ok) {
 		for (uint32_t i = t0; i < ns; i += stride) {
@@ -744,7 +745,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 				atomicAdd(&ctl->ctr[0].act_deg, (unsigned long long) d);
 			}
 		}
-		ok = grid_barrier(ctl->bar, &ctl->err);
+		ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
 	}
 	if (leader) ctl->stats.t_levels0 = global_timer_ns();
 	unsigned long long gathered = 0;
@@ -762,14 +763,14 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 		if (lvl + 1 - base >= a.planes) {
 			// planes full: write them out, keep the frontier's plane as plane 0
 			ms_emit(a, levels, ns, base, base == 0 ? 0 : 1, lvl - base, base != 0, lev);
-			if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
+			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 			const uint64_t *src = a.hist + (size_t) (lvl - base) * nK;
 			for (size_t i = t0; i < nK; i += stride) a.hist[i] = ld_cg64(src + i);
 			const uint64_t *msrc = a.pmask + (size_t) (lvl - base) * a.n;
 			for (uint32_t i = t0; i < a.n; i += stride) a.pmask[i] = ld_cg64(msrc + i);
 			base = lvl;
 			if (leader) ctl->stats.spills++;
-			if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
+			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 		}
 		// the counters of the level after next are free again
 		if (leader) {
@@ -793,19 +794,19 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 		if (push) {
 			if (blockIdx.x == 0 && nb) ms_push_chunk_list(a, lvl, nb, wq);
 			for (size_t i = t0; i < nK; i += stride) nxt[i] = 0;
-			if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
+			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 			if (leader && tph) tph[0] = global_timer_ns();
 			ms_push(a, lvl, cur, actc, nxt, nq, nb);
-			if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
+			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 			if (leader && tph) tph[1] = global_timer_ns();
 			ms_push_finish(a, lvl, nxt, actn, actdeg);
 		} else {
 			ms_pull(a, lvl, cur, actc, nxt, actn, actdeg, gathered, wq);
 			if (a.nbig_in) {
-				if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
+				if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 				if (leader && tph) tph[0] = global_timer_ns();
 				ms_pull_chunks(a, cur, actc, nxt, gathered);
-				if (!(ok = grid_barrier(ctl->bar, &ctl->err))) break;
+				if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 				if (leader && tph) tph[1] = global_timer_ns();
 				ms_pull_chunks_finish(a, lvl, nxt, actn, actdeg);
 			}
@@ -824,7 +825,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 			}
 		}
 		__syncthreads();
-		ok = grid_barrier(ctl->bar, &ctl->err);
+		ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
 	}
 	if (leader) {
 		ctl->stats.t_levels1 = global_timer_ns();

@@ -67,6 +67,8 @@ struct MsArgs {
 	uint32_t *seed_flag;  // [n]
 	uint32_t *queue[2];   // [n] frontier vertices by level parity (small front, big back)
 	MsControl *ctl;
+	unsigned long long wait_limit_ns;  // bound of every grid-barrier wait
+	uint32_t hold_barrier;             // tests: CTA 0 skips its arrival at this barrier (0 = off)
 };
 
 // Enqueues the whole batched traversal (one cooperative launch and the

@@ -131,7 +131,10 @@ class Graph:
         o = N.Options()
         lib = N.load()
         N.check(lib.bfs_get_options(self._h, C.byref(o)), "bfs_get_options")
+        names = {f for f, _ in N.Options._fields_}
         for k, v in kw.items():
+            if k not in names:
+                raise ValueError(f"unknown option {k!r}")
             if k == "mode" and isinstance(v, str):
                 v = {"persistent": N.BFS_MODE_PERSISTENT, "stepwise": N.BFS_MODE_STEPWISE}[v]
             if k == "bottom_up" and isinstance(v, str):

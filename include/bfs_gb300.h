@@ -144,6 +144,12 @@ typedef struct bfs_options {
 	uint32_t bc_level_bytes;   /* bfs_bc_*: test neighbour levels in a byte array before fetching values
 	                              (traversals of at most 254 levels): 0 = for graphs of at least 2^22
 	                              vertices (default), 1 = always, 2 = never; results are identical */
+	uint32_t wait_limit_us;    /* bound of every device-side wait of bfs_run / bfs_run_batch (grid barriers):
+	                              past it the kernel gives up, returns and the run reports BFS_ETIMEOUT
+	                              (0 = the default, 2 s) */
+	uint32_t test_hold_barrier; /* TESTS ONLY: k > 0 makes CTA 0 skip its arrival at the k-th grid barrier of
+	                              the next runs, so that the other CTAs' bounded waits run out (the failure
+	                              path of the wait limit, exercised without a GPU fault); 0 = off */
 } bfs_options;
 
 /* Bottom-up step variants.  PULL: every unvisited destination of a column
