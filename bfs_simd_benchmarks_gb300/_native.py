@@ -78,6 +78,10 @@ class Options(C.Structure):
         ("bc_level_bytes", C.c_uint32),
         ("wait_limit_us", C.c_uint32),
         ("test_hold_barrier", C.c_uint32),
+        ("switch_rule", C.c_uint32),
+        ("bu_alpha", C.c_uint32),
+        ("td_beta", C.c_uint32),
+        ("ctas_per_sm", C.c_uint32),
     ]
 
 

@@ -46,6 +46,7 @@ struct bfs_graph {
 	RunCtx rc{};
 	uint32_t batch = 1;
 	int grid = 0;
+	int grid_max = 0;  // CTAs of the cooperative grid at full occupancy (grid: as the options ask)
 	size_t smem = 0;
 	std::vector<DevBuf> bufs;
 	size_t device_bytes = 0;
@@ -184,6 +185,10 @@ void default_options(bfs_options *o) {
 	o->batch_budget_mb = 40960;
 	o->batch_single_max = 4;
 	o->batch_push_div = 16;
+	o->switch_rule = BFS_SWITCH_REFERENCE;
+	o->bu_alpha = 14;
+	o->td_beta = 24;
+	o->ctas_per_sm = 0;
 }
 
 int device_setup(bfs_graph *g) {
@@ -274,7 +279,9 @@ int alloc_run(bfs_graph *g) {
 			cudaEventCreate(&g->evm) != cudaSuccess)
 		return BFS_ECUDA;
 	g->batch = std::max<uint32_t>(1, std::min<uint32_t>(kMaxSliceBatch, kSliceBudgetWords / std::max<uint32_t>(1, d.slice_words)));
-	return persistent_grid(d, g->batch, g->num_sms, &g->grid, &g->smem);
+	st = persistent_grid(d, g->batch, g->num_sms, &g->grid, &g->smem);
+	g->grid_max = g->grid;
+	return st;
 }
 
 // Builds the device copy of a validated host graph.
@@ -502,6 +509,7 @@ int run_stepwise(bfs_graph *g, const RunCtx &r, const StepParams &p, cudaStream_
 	bfs_stats &hs = g->host_stats;
 	std::memset(&hs, 0, sizeof(hs));
 	bool last_dense = false;
+	unsigned long long seen = 0;  // out-edges of the vertices reached so far
 	uint32_t step = 0;
 	for (;; ++step) {
 		// the step totals: sum of the per-CTA partials of the frontier's slot
@@ -518,8 +526,12 @@ int run_stepwise(bfs_graph *g, const RunCtx &r, const StepParams &p, cudaStream_
 		hs.reached += (uint32_t) count;
 		hs.edges_traversed += degsum;
 		if (count == 0) break;
+		seen += degsum;
 		bool dense = false;
-		if (step > 0) {
+		if (step > 0 && p.switch_rule != 0) {
+			const unsigned long long unseen = g->m > seen ? g->m - seen : 0ull;
+			dense = last_dense ? count * p.beta >= g->n : degsum * p.alpha > unseen;
+		} else if (step > 0) {
 			unsigned long long thr = last_dense ? p.to_sparse_threshold : p.to_dense_threshold;
 			dense = count + degsum > thr;
 		}
@@ -555,6 +567,9 @@ int run_impl(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, 
 	p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
 	p.wait_limit_ns = wait_limit_ns(g->opt);
 	p.hold_barrier = g->opt.test_hold_barrier;
+	p.switch_rule = g->opt.switch_rule;
+	p.alpha = g->opt.bu_alpha;
+	p.beta = g->opt.td_beta;
 	int rc;
 	g->stepwise_last = g->opt.mode == BFS_MODE_STEPWISE;
 	if (cudaEventRecord(g->ev0, st) != cudaSuccess) return BFS_ECUDA;
@@ -759,6 +774,7 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 	a.push_div = std::max<uint32_t>(1, g->opt.batch_push_div);
 	a.wait_limit_ns = wait_limit_ns(g->opt);
 	a.hold_barrier = g->opt.test_hold_barrier;
+	a.ctas_per_sm = g->opt.ctas_per_sm;
 	a.row_off = g->dg.row_off;
 	a.col = g->dg.col;
 	a.in_off = g->dg.in_off;
@@ -787,6 +803,9 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 		p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
 		p.wait_limit_ns = wait_limit_ns(g->opt);
 		p.hold_barrier = g->opt.test_hold_barrier;
+		p.switch_rule = g->opt.switch_rule;
+		p.alpha = g->opt.bu_alpha;
+		p.beta = g->opt.td_beta;
 		for (uint32_t i = 0; i < ns; ++i) {
 			p.source = sources[i];
 			if ((rc = launch_persistent(g->dg, r, p, g->batch, g->grid, g->smem, st))) return rc;
@@ -927,6 +946,9 @@ int bc_enqueue(bfs_graph *g, uint32_t source, uint32_t *sigma, float *delta, flo
 	p.to_sparse_threshold = g->m / std::max<uint32_t>(1, g->opt.to_sparse_ratio);
 	p.wait_limit_ns = wait_limit_ns(g->opt);
 	p.hold_barrier = g->opt.test_hold_barrier;
+	p.switch_rule = g->opt.switch_rule;
+	p.alpha = g->opt.bu_alpha;
+	p.beta = g->opt.td_beta;
 	int rc;
 	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
 	if ((rc = launch_persistent(g->dg, r, p, g->batch, g->grid, g->smem, st))) return rc;
@@ -1367,10 +1389,14 @@ int bfs_set_options(bfs_graph *g, const bfs_options *opt) {
 	if (opt->mode > BFS_MODE_STEPWISE || opt->bottom_up > BFS_BU_STREAM || opt->to_dense_ratio == 0 || opt->to_sparse_ratio == 0 ||
 			opt->warp_max_degree == 0 || opt->cta_max_degree < opt->warp_max_degree || opt->batch_planes == 1 ||
 			opt->batch_planes > kMsMaxLevel + 1 || (opt->batch_planes == 0 && opt->batch_budget_mb == 0) ||
-			opt->batch_push_div == 0 || opt->bc_level_bytes > 2)
+			opt->batch_push_div == 0 || opt->bc_level_bytes > 2 || opt->switch_rule > BFS_SWITCH_UNVISITED ||
+			opt->bu_alpha == 0 || opt->td_beta == 0 || opt->ctas_per_sm > 2)
 		return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);
 	g->opt = *opt;
+	// the cooperative grid: the occupancy bound found at set-up, or fewer CTAs per SM
+	if (!g->host_only && g->grid_max)
+		g->grid = opt->ctas_per_sm ? std::min(g->grid_max, (int) opt->ctas_per_sm * g->num_sms) : g->grid_max;
 	return BFS_OK;
 }
 

@@ -110,11 +110,13 @@ uint64_t fnv1a(uint64_t h, const void *p, size_t n) {
 }
 
 const char *kFields[] = {"mode", "to_dense_ratio", "to_sparse_ratio", "warp_max_degree", "cta_max_degree",
-		"bottom_up", "batch_planes", "batch_budget_mb", "batch_single_max", "batch_push_div"};
-constexpr int kNumFields = 10;
+		"bottom_up", "batch_planes", "batch_budget_mb", "batch_single_max", "batch_push_div", "switch_rule",
+		"bu_alpha", "td_beta", "ctas_per_sm"};
+constexpr int kNumFields = 14;
 uint32_t *field_ptr(bfs_options &o, int i) {
 	uint32_t *f[] = {&o.mode, &o.to_dense_ratio, &o.to_sparse_ratio, &o.warp_max_degree, &o.cta_max_degree,
-			&o.bottom_up, &o.batch_planes, &o.batch_budget_mb, &o.batch_single_max, &o.batch_push_div};
+			&o.bottom_up, &o.batch_planes, &o.batch_budget_mb, &o.batch_single_max, &o.batch_push_div,
+			&o.switch_rule, &o.bu_alpha, &o.td_beta, &o.ctas_per_sm};
 	return f[i];
 }
 
@@ -174,8 +176,12 @@ int tune(Tuner &t, uint32_t flags, bfs_options *best_out, double *single_out, do
 		time_single(t, o);  // warm-up
 		const std::vector<Axis> axes = {
 				{&bfs_options::bottom_up, {BFS_BU_PULL, BFS_BU_STREAM}},
+				{&bfs_options::ctas_per_sm, {0, 1}},
+				{&bfs_options::switch_rule, {BFS_SWITCH_REFERENCE, BFS_SWITCH_UNVISITED}},
 				{&bfs_options::to_dense_ratio, {5, 10, 20, 40, 80, 160}},
 				{&bfs_options::to_sparse_ratio, {5, 10, 20, 40, 80, 160}},
+				{&bfs_options::bu_alpha, {2, 4, 8, 14, 32, 64}},
+				{&bfs_options::td_beta, {8, 24, 64, 256}},
 				{&bfs_options::warp_max_degree, {8, 16, 32, 64}},
 				{&bfs_options::cta_max_degree, {512, 1024, 4096, 16384}},
 		};
@@ -191,7 +197,8 @@ int tune(Tuner &t, uint32_t flags, bfs_options *best_out, double *single_out, do
 			return BFS_ENOMEM;
 		}
 		time_batch(t, o);  // warm-up (allocates the batch state)
-		const std::vector<Axis> axes = {{&bfs_options::batch_push_div, {4, 8, 16, 32, 64, 128}}};
+		const std::vector<Axis> axes = {{&bfs_options::batch_push_div, {4, 8, 16, 32, 64, 128}},
+				{&bfs_options::ctas_per_sm, {0, 1}}};
 		const uint32_t first = t.res->num_trials;
 		*batch_out = descend(t, o, axes, time_batch, BFS_TUNE_BATCH);
 		if (def_batch && first < t.res->num_trials) *def_batch = t.res->trials[first].gteps;

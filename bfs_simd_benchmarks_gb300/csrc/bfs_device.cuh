@@ -94,6 +94,8 @@ struct StepParams {
 	unsigned long long to_sparse_threshold;  // stay dense while frontier + degsum > this
 	unsigned long long wait_limit_ns;        // bound of every grid-barrier wait
 	uint32_t hold_barrier;                   // tests: CTA 0 skips its arrival at this barrier (0 = off)
+	uint32_t switch_rule;                    // 0: thresholds above; 1: out-edges of the unvisited (alpha, beta)
+	uint32_t alpha, beta;
 };
 
 } // namespace bfsg

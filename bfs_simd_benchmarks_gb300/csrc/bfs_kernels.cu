@@ -61,6 +61,9 @@ constexpr int kTdPerLane = 4;  // candidate edges a lane handles per top-down it
 // Medium-degree buckets up to this size join the grid-flat expansion of the
 // large ones (a few chunks); larger ones are spread over CTAs in chunks.
 constexpr uint32_t kFlatMediumMax = 4 * kThreads;
+// Flat-expansion vertices staged per chunk (in dynamic shared memory after
+// the warps' append buffers).
+constexpr uint32_t kFlatChunk = 4 * kThreads;
 
 // Next-frontier appends of one warp are staged in a shared-memory buffer per
 // degree bucket and moved to the global queue in blocks, so the queue tails
@@ -198,26 +201,42 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 
 	// Large out-degree vertices -- and medium ones when there are few of them
 	// -- are expanded as one flat edge range that every warp of the grid
-	// shares evenly.  Each CTA stages a chunk of up to kThreads such vertices
-	// with the inclusive prefix of their degrees in shared memory; a lane
-	// finds the owner of its edge by binary search.
+	// shares evenly.  Each CTA stages a chunk of up to kFlatChunk such
+	// vertices (usually all of them: every chunk costs each warp a setup and
+	// a partial edge batch) with the inclusive prefix of their degrees in
+	// shared memory; a lane finds the owner of its edge by binary search.
 	const bool flat_medium = nM <= kFlatMediumMax;
 	const uint32_t nflat = nL + (flat_medium ? nM : 0u);
-	for (uint32_t c0 = 0; c0 < nflat; c0 += kThreads) {
-		const uint32_t cn = min((uint32_t) kThreads, nflat - c0);
-		uint32_t deg = 0, u = 0, beg = 0;
-		if (threadIdx.x < cn) {
-			const uint32_t x = c0 + threadIdx.x;
-			u = ld_cg(x < nL ? qL + x : qM + (x - nL));
-			beg = __ldg(g.row_off + u);
-			deg = __ldg(g.row_off + u + 1) - beg;
+	uint32_t *fu = smem + (size_t) kWarps * 3 * kWqCap, *fbeg = fu + kFlatChunk, *fpre = fbeg + kFlatChunk;
+	for (uint32_t c0 = 0; c0 < nflat; c0 += kFlatChunk) {
+		const uint32_t cn = min(kFlatChunk, nflat - c0);
+		constexpr int kPer = kFlatChunk / kThreads;  // entries per thread, consecutive
+		uint32_t u[kPer], beg[kPer], deg[kPer];
+#pragma unroll
+		for (int k = 0; k < kPer; ++k) {
+			const uint32_t x = threadIdx.x * kPer + k, y = c0 + x;
+			u[k] = x < cn ? ld_cg(y < nL ? qL + y : qM + (y - nL)) : 0u;
 		}
-		const uint32_t incl = block_incl_scan(deg);
-		xsh.u[threadIdx.x] = u;
-		xsh.beg[threadIdx.x] = beg;
-		xsh.pre[threadIdx.x] = incl;
+#pragma unroll
+		for (int k = 0; k < kPer; ++k) {
+			const bool in = threadIdx.x * kPer + k < cn;
+			beg[k] = in ? __ldg(g.row_off + u[k]) : 0u;
+			deg[k] = in ? __ldg(g.row_off + u[k] + 1) - beg[k] : 0u;
+		}
+		uint32_t sum = 0;
+#pragma unroll
+		for (int k = 0; k < kPer; ++k) sum += deg[k];
+		uint32_t run = block_incl_scan(sum) - sum;
+#pragma unroll
+		for (int k = 0; k < kPer; ++k) {
+			const uint32_t x = threadIdx.x * kPer + k;
+			run += deg[k];
+			fu[x] = u[k];
+			fbeg[x] = beg[k];
+			fpre[x] = run;
+		}
 		__syncthreads();
-		const uint32_t total = xsh.pre[cn - 1];
+		const uint32_t total = fpre[cn - 1];
 		const uint64_t per = (total + nwarps - 1) / nwarps;
 		const uint64_t lo = min((uint64_t) total, gwarp * per), hi = min((uint64_t) total, lo + per);
 		for (uint64_t f0 = lo; f0 < hi; f0 += kSpan) {
@@ -228,13 +247,13 @@ __device__ __forceinline__ void phase_expand(const DevGraph &g, const RunCtx &r,
 				uint32_t j = 0;  // owner: the number of entries whose inclusive prefix is <= f
 				if (has[q]) {
 #pragma unroll
-					for (uint32_t sp = kThreads / 2; sp >= 1; sp >>= 1)
-						if (j + sp < cn && xsh.pre[j + sp - 1] <= f) j += sp;
+					for (uint32_t sp = kFlatChunk / 2; sp >= 1; sp >>= 1)
+						if (j + sp < cn && fpre[j + sp - 1] <= f) j += sp;
 				}
 				const uint32_t jj = min(j, cn - 1);
-				const uint32_t prev = jj ? xsh.pre[jj - 1] : 0u;
-				uu[q] = xsh.u[jj];
-				vv[q] = has[q] ? __ldg(g.col + xsh.beg[jj] + (uint32_t) (f - prev)) : 0u;
+				const uint32_t prev = jj ? fpre[jj - 1] : 0u;
+				uu[q] = fu[jj];
+				vv[q] = has[q] ? __ldg(g.col + fbeg[jj] + (uint32_t) (f - prev)) : 0u;
 			}
 			visit_and_append(has, uu, vv, nl, g, r, nbm, wq, p, acc);
 		}
@@ -1211,10 +1230,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 	unsigned long long st_reached = 0, st_edges = 0;
 	uint32_t st_dense = 0;
 	unsigned epoch = 0;  // grid barriers this CTA has passed
+	unsigned long long seen = 0;  // out-edges of the vertices reached so far (frontiers included)
 	bool last_dense = false;
 	uint32_t step = 0;
+	CTA_STAMP(15, 0);  // profiling builds: the prologue in the slot of step 15
 	init_run(g, r, p, true);
+	CTA_STAMP(15, 1);
 	ok = grid_sync(r.bar, epoch, r.err, p.wait_limit_ns, p.hold_barrier);
+	CTA_STAMP(15, 2);
 	for (; ok; ++step) {
 		uint32_t fsize, tails[3];
 		unsigned long long dsum;
@@ -1227,10 +1250,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_bfs_persistent(DevGraph g, RunC
 			if (step < 257) r.stats->t_step[step] = global_timer_ns();
 		}
 		if (fsize == 0) break;
+		seen += dsum;
 		bool dense = false;
 		if (step > 0) {
-			unsigned long long thr = last_dense ? p.to_sparse_threshold : p.to_dense_threshold;
-			dense = (unsigned long long) fsize + dsum > thr;
+			if (p.switch_rule == 0) {
+				unsigned long long thr = last_dense ? p.to_sparse_threshold : p.to_dense_threshold;
+				dense = (unsigned long long) fsize + dsum > thr;
+			} else {
+				const unsigned long long unseen = g.m > seen ? g.m - seen : 0ull;
+				dense = last_dense ? (unsigned long long) fsize * p.beta >= g.n : dsum * p.alpha > unseen;
+			}
 		}
 		clear_slot(g, r, (step + 1) % 3);
 		CTA_STAMP(step, 2);
@@ -1331,7 +1360,7 @@ size_t dense_smem_bytes(const DevGraph &g, uint32_t batch) {
 	if (g.tma) words += (size_t) kTmaStages * (kTmaEdgeWords + (size_t) g.tma_batch * g.slice_words);
 	else words += (size_t) batch * g.slice_words;
 	const size_t pull = (size_t) 3 * (g.max_group_words + 1) + g.pull_long_cap;
-	const size_t expand = (size_t) kWarps * 3 * kWqCap;
+	const size_t expand = (size_t) kWarps * 3 * kWqCap + 3 * (size_t) kFlatChunk;
 	size_t need = words > pull ? words : pull;
 	need = need > expand ? need : expand;
 	return sizeof(uint32_t) * need;

@@ -875,6 +875,7 @@ int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *
 	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ms_bfs, kMsThreads, 0) != cudaSuccess || per_sm < 1)
 		return BFS_ECUDA;
 	per_sm = std::min(per_sm, 2);
+	if (a.ctas_per_sm) per_sm = std::min(per_sm, (int) a.ctas_per_sm);
 	if (grid) *grid = num_sms * per_sm;
 	if (cudaMemsetAsync(a.ctl, 0, sizeof(MsControl), st) != cudaSuccess) return BFS_ECUDA;
 	MsArgs aa = a;

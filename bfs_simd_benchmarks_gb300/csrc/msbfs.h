@@ -69,6 +69,7 @@ struct MsArgs {
 	MsControl *ctl;
 	unsigned long long wait_limit_ns;  // bound of every grid-barrier wait
 	uint32_t hold_barrier;             // tests: CTA 0 skips its arrival at this barrier (0 = off)
+	uint32_t ctas_per_sm;              // 0 = as many as fit (at most 2)
 };
 
 // Enqueues the whole batched traversal (one cooperative launch and the

@@ -150,7 +150,18 @@ typedef struct bfs_options {
 	uint32_t test_hold_barrier; /* TESTS ONLY: k > 0 makes CTA 0 skip its arrival at the k-th grid barrier of
 	                              the next runs, so that the other CTAs' bounded waits run out (the failure
 	                              path of the wait limit, exercised without a GPU fault); 0 = off */
+	uint32_t switch_rule;      /* BFS_SWITCH_REFERENCE (default): the thresholds above; BFS_SWITCH_UNVISITED:
+	                              go bottom-up when the frontier's out-edges * bu_alpha exceed the out-edges
+	                              of the vertices not reached yet, back top-down when frontier * td_beta < N
+	                              (Beamer's rule); levels are identical, only the step directions differ */
+	uint32_t bu_alpha;         /* BFS_SWITCH_UNVISITED: alpha (default 14) */
+	uint32_t td_beta;          /* BFS_SWITCH_UNVISITED: beta (default 24) */
+	uint32_t ctas_per_sm;      /* CTAs per SM of the cooperative traversal grids: 0 = as many as fit (at most
+	                              2), or 1 or 2 */
 } bfs_options;
+
+#define BFS_SWITCH_REFERENCE 0u
+#define BFS_SWITCH_UNVISITED 1u
 
 /* Bottom-up step variants.  PULL: every unvisited destination of a column
  * group scans its in-edges (the column's tiles sorted by destination) and

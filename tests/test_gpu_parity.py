@@ -136,6 +136,32 @@ def test_direction_thresholds_do_not_change_levels(native, oracle):
         assert len(seen) > 1, "the options should change the direction trace"
 
 
+def test_unvisited_edge_switch_rule_and_grid_shape_do_not_change_levels(native, oracle):
+    """Beamer's direction rule (switch_rule=1) and one CTA per SM: other step
+    directions and another grid, the same levels, in both execution modes."""
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 15
+    src, dst = B.gen_rmat(n, 16 * n, seed=78, permute=True)
+    arr = oracle.arrays_from_edges(n, src, dst, 1024, 16)
+    srcs = [int(s) for s in B.pick_sources(arr["degrees"], 3, seed=9)]
+    with B.Graph.from_edges(n, src, dst, 1024, 16) as g:
+        traces = set()
+        for mode in ("persistent", "stepwise"):
+            for alpha, beta, cps in [(14, 24, 0), (2, 8, 1), (64, 256, 0), (4, 64, 1)]:
+                g.set_options(mode=mode, switch_rule=1, bu_alpha=alpha, td_beta=beta, ctas_per_sm=cps)
+                for s in srcs:
+                    lev, par, st = g.run(s)
+                    np.testing.assert_array_equal(lev, oracle.bfs_levels(arr, s))
+                    assert oracle.check_parents(arr, s, lev, par) == 0
+                    traces.add((mode, alpha, beta, s, tuple(st["trace"])))
+        # both modes decide the same directions for the same options
+        per = {}
+        for mode, a, b, s, tr in traces:
+            per.setdefault((a, b, s), set()).add(tr)
+        assert all(len(v) == 1 for v in per.values())
+        assert len({tr for *_, tr in traces}) > 1
+
+
 def test_edge_cases(native, oracle):
     import bfs_simd_benchmarks_gb300 as B
     # no edges at all
