@@ -640,7 +640,8 @@ def main():
         t_t = time.perf_counter()
         r = g.tune(sources, single=True)
         tuned = {"options": {k: r["options"][k] for k in ("bottom_up", "to_dense_ratio", "to_sparse_ratio",
-                                                           "warp_max_degree", "cta_max_degree")},
+                                                           "warp_max_degree", "cta_max_degree", "switch_rule",
+                                                           "bu_alpha", "td_beta", "ctas_per_sm")},
                  "tuned_gteps_kernel": r["single_gteps"], "default_gteps_kernel": r["default_single_gteps"],
                  "trials": r["num_trials"], "seconds": round(time.perf_counter() - t_t, 2)}
     dev = torch.device("cuda", local)

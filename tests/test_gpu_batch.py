@@ -243,3 +243,28 @@ def test_device_sources_and_cuda_graph(native, oracle):
             g.run_batch_sources_device(d_src.data_ptr(), 150, out.data_ptr())
             g.last_batch_stats()
         assert ei.value.status == 4
+
+
+@pytest.mark.timeout(900)
+def test_rmat22_4096_sources_against_the_oracle(native, oracle):
+    """The batched configuration at full size: R-MAT scale 22 (4,194,304
+    vertices, 67,108,864 edges), 4096 seeded sources in one launch (64 words
+    per vertex); 12 rows spread over the batch (first and last words
+    included) bit-exact against the oracle."""
+    torch = pytest.importorskip("torch")
+    import bfs_simd_benchmarks_gb300 as B
+    from bfs_simd_benchmarks_gb300 import workloads
+    wl = workloads.get("rmat22")
+    src, dst = wl.edges()
+    arr = oracle.csr_arrays(wl.n, src, dst)
+    with B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s, device_build=True) as g:
+        del src, dst
+        sources = wl.sources(g.degrees(), 4096)
+        out = torch.empty((4096, wl.n), dtype=torch.uint8, device="cuda")
+        st = g.run_batch_device(sources, out.data_ptr(), torch.cuda.current_stream().cuda_stream, stats=True)
+        assert st["status"] == 0 and st["words_per_vertex"] == 64
+        for i in (0, 1, 63, 64, 1000, 2047, 2048, 3000, 4031, 4032, 4094, 4095):
+            ref = oracle.bfs_levels(arr, int(sources[i]))
+            np.testing.assert_array_equal(out[i].cpu().numpy(), np.where(ref < 0, 255, ref).astype(np.uint8))
+        del out
+        torch.cuda.empty_cache()
