@@ -10,6 +10,7 @@ from .graph import (  # noqa: F401
     autotune,
     tile_size_range,
     gen_rmat,
+    gen_rmat_device,
     pick_sources,
     tool_column_major,
     tool_coo_tiling,
@@ -20,6 +21,6 @@ from .graph import (  # noqa: F401
 )
 
 __all__ = [
-    "BfsError", "Graph", "Server", "autotune", "tile_size_range", "gen_rmat", "load_library", "pick_sources", "tool_column_major",
+    "BfsError", "Graph", "Server", "autotune", "tile_size_range", "gen_rmat", "gen_rmat_device", "load_library", "pick_sources", "tool_column_major",
     "tool_coo_tiling", "tool_csr_tiling", "tool_vertex_remap", "write_edge_list", "write_level_dump",
 ]

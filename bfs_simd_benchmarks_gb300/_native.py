@@ -348,6 +348,7 @@ _SIGNATURES = [
     ("bfs_tool_column_major", C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
     ("bfs_tool_vertex_remap", C.c_int, [C.c_char_p, C.c_uint32]),
     ("bfs_gen_rmat", C.c_int, [C.POINTER(RmatParams), _u32p, _u32p, C.c_uint64]),
+    ("bfs_gen_rmat_device", C.c_int, [C.POINTER(RmatParams), C.c_void_p, C.c_void_p, C.c_uint64]),
 ]
 
 _lib = None

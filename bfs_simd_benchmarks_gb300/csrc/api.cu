@@ -371,8 +371,9 @@ int upload_device_build(bfs_graph *g, uint32_t n, uint64_t m, const uint32_t *sr
 			(st = tmp.alloc(&in_deg, n)) || (st = tmp.alloc(&cursor, (size_t) n + 1)) ||
 			(st = tmp.alloc(&scan_tmp, dbuild_scan_tmp_words(n))) || (st = tmp.alloc(&d_err, 1)))
 		return st;
-	if (m && (cudaMemcpy(d_src, src, m * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-			cudaMemcpy(d_dst, dst, m * 4, cudaMemcpyHostToDevice) != cudaSuccess))
+	// host or device edge arrays (unified addressing tells them apart)
+	if (m && (cudaMemcpy(d_src, src, m * 4, cudaMemcpyDefault) != cudaSuccess ||
+			cudaMemcpy(d_dst, dst, m * 4, cudaMemcpyDefault) != cudaSuccess))
 		return BFS_ECUDA;
 	if (cudaMemset(out_deg, 0, (size_t) n * 4) != cudaSuccess || cudaMemset(in_deg, 0, (size_t) n * 4) != cudaSuccess ||
 			cudaMemset(d_err, 0, 4) != cudaSuccess)

@@ -2,55 +2,23 @@
 // reference's datasets; no counterpart in the reference, which downloads
 // KONECT files, README.md:15-24).
 //
-// Each candidate edge i draws its quadrant bits from a counter-based hash
-// (splitmix64 of seed and i), so the list does not depend on the thread
-// count or the platform.  With d = 1-a-b-c, one level picks
-//   (u,v) bits (0,0) with a, (0,1) with b, (1,0) with c, (1,1) with d.
-// The scale is ceil(log2 N); ids >= N are rejected.  Self loops and duplicates
-// are dropped on request (keeping the first occurrence), and candidates are
-// drawn until exactly num_edges survive.  BFS_RMAT_PERMUTE relabels vertices
-// with a seeded Fisher-Yates permutation.
+// The candidate edges are defined in rmat_common.h (shared with the device
+// generator, rmat_device.cu).  Self loops and duplicates are dropped on
+// request (keeping the first occurrence), and candidates are drawn until
+// exactly num_edges survive.  BFS_RMAT_PERMUTE relabels vertices with a
+// seeded Fisher-Yates permutation.
 #include <algorithm>
 #include <atomic>
 #include <cstring>
 
 #include "internal.h"
+#include "rmat_common.h"
 
 namespace {
 
-inline uint64_t splitmix64(uint64_t x) {
-	x += 0x9E3779B97F4A7C15ull;
-	x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
-	x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-	return x ^ (x >> 31);
-}
-
-struct Thresholds {
-	uint32_t ta, tab, tabc;
-};
-
-// Candidate `i`: returns false when rejected (id out of range or self loop).
-inline bool candidate(uint64_t seed, uint64_t i, uint32_t scale, uint32_t n, const Thresholds &t,
-		bool no_loops, uint32_t *pu, uint32_t *pv) {
-	uint32_t u = 0, v = 0;
-	uint64_t h = 0;
-	for (uint32_t l = 0; l < scale; ++l) {
-		if ((l & 1) == 0) h = splitmix64(seed ^ splitmix64(i * 64 + l));
-		uint32_t r = (l & 1) ? (uint32_t) (h >> 32) : (uint32_t) h;
-		uint32_t bu, bv;
-		if (r < t.ta) { bu = 0; bv = 0; }
-		else if (r < t.tab) { bu = 0; bv = 1; }
-		else if (r < t.tabc) { bu = 1; bv = 0; }
-		else { bu = 1; bv = 1; }
-		u = (u << 1) | bu;
-		v = (v << 1) | bv;
-	}
-	if (u >= n || v >= n) return false;
-	if (no_loops && u == v) return false;
-	*pu = u;
-	*pv = v;
-	return true;
-}
+using bfsg::rmat::splitmix64;
+using bfsg::rmat::Thresholds;
+using bfsg::rmat::candidate;
 
 // Drops repeated keys, keeping the first occurrence, order otherwise kept.
 // Keys are hashed into buckets (each bucket keeps candidate order), buckets
@@ -97,12 +65,6 @@ void dedup_stable(std::vector<uint64_t> &keys) {
 	keys.resize(w);
 }
 
-inline uint32_t to_threshold(double p) {
-	if (p <= 0) return 0;
-	if (p >= 1) return 0xFFFFFFFFu;
-	return (uint32_t) (p * 4294967296.0);
-}
-
 } // namespace
 
 using namespace bfsg;
@@ -120,8 +82,9 @@ extern "C" int bfs_gen_rmat(const bfs_rmat_params *p, uint32_t *src, uint32_t *d
 		if (m > max_m) return BFS_EARG;
 	}
 	const uint32_t scale = ceil_log2(n);
-	Thresholds t{to_threshold(p->a), to_threshold(p->a + p->b), to_threshold(p->a + p->b + p->c)};
-	const uint64_t seed = splitmix64(p->seed ^ 0x5851F42D4C957F2Dull);
+	Thresholds t{bfsg::rmat::to_threshold(p->a), bfsg::rmat::to_threshold(p->a + p->b),
+			bfsg::rmat::to_threshold(p->a + p->b + p->c)};
+	const uint64_t seed = bfsg::rmat::mixed_seed(p->seed);
 	const unsigned nt = host_threads();
 
 	// Accepted edges as 64-bit keys (u << 32 | v) in candidate order.
@@ -150,16 +113,7 @@ extern "C" int bfs_gen_rmat(const bfs_rmat_params *p, uint32_t *src, uint32_t *d
 	keys.resize(m);
 
 	std::vector<uint32_t> perm;
-	if (p->flags & BFS_RMAT_PERMUTE) {
-		perm.resize(n);
-		for (uint32_t v = 0; v < n; ++v) perm[v] = v;
-		uint64_t st = splitmix64(seed ^ 0xD1B54A32D192ED03ull);
-		for (uint32_t v = n - 1; v > 0; --v) {
-			st = splitmix64(st);
-			uint32_t j = (uint32_t) (((unsigned __int128) st * (uint64_t) (v + 1)) >> 64);
-			std::swap(perm[v], perm[j]);
-		}
-	}
+	if (p->flags & BFS_RMAT_PERMUTE) bfsg::rmat::permutation(seed, n, perm);
 	parallel_for(m, [&](uint64_t lo, uint64_t hi, unsigned) {
 		for (uint64_t i = lo; i < hi; ++i) {
 			uint32_t u = (uint32_t) (keys[i] >> 32), v = (uint32_t) keys[i];

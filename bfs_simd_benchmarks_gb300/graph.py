@@ -58,6 +58,17 @@ class Graph:
         return cls(h)
 
     @classmethod
+    def from_device_edges(cls, num_vertices: int, src_ptr: int, dst_ptr: int, num_edges: int, tile_width: int,
+                          stripe_length: int) -> "Graph":
+        """A graph built on the GPU from an edge list already in device memory
+        (uint32 src/dst device pointers; bfs_graph_from_edges with BFS_LOAD_DEVICE_BUILD)."""
+        h = C.c_void_p()
+        N.check(N.load().bfs_graph_from_edges(num_vertices, num_edges, C.cast(C.c_void_p(src_ptr), _u32p_type()),
+                                              C.cast(C.c_void_p(dst_ptr), _u32p_type()), tile_width, stripe_length,
+                                              N.BFS_LOAD_DEVICE_BUILD, C.byref(h)), "bfs_graph_from_edges")
+        return cls(h)
+
+    @classmethod
     def from_arrays(cls, num_vertices: int, degrees, csr_dst, heads, tails, tile_offsets,
                     tile_width: int, stripe_length: int, host_only: bool = False) -> "Graph":
         lib = N.load()
@@ -433,6 +444,29 @@ def gen_rmat(num_vertices: int, num_edges: int, a: float = 0.57, b: float = 0.19
     N.check(N.load().bfs_gen_rmat(C.byref(p), _ptr(src, C.c_uint32), _ptr(dst, C.c_uint32), num_edges),
             "bfs_gen_rmat")
     return src, dst
+
+
+def gen_rmat_device(num_vertices: int, num_edges: int, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+                    seed: int = 1, dedup: bool = True, no_self_loops: bool = True, permute: bool = False):
+    """gen_rmat's edge list drawn on the current CUDA device: two torch uint32-
+    valued int32 CUDA tensors (src, dst) holding exactly gen_rmat's arrays."""
+    import torch
+    p = N.RmatParams()
+    p.num_vertices = num_vertices
+    p.num_edges = num_edges
+    p.a, p.b, p.c = a, b, c
+    p.seed = seed
+    p.flags = ((N.BFS_RMAT_DEDUP if dedup else 0) | (N.BFS_RMAT_NO_SELF_LOOPS if no_self_loops else 0)
+               | (N.BFS_RMAT_PERMUTE if permute else 0))
+    src = torch.empty(num_edges, dtype=torch.int32, device="cuda")
+    dst = torch.empty(num_edges, dtype=torch.int32, device="cuda")
+    N.check(N.load().bfs_gen_rmat_device(C.byref(p), C.c_void_p(src.data_ptr()), C.c_void_p(dst.data_ptr()),
+                                         num_edges), "bfs_gen_rmat_device")
+    return src, dst
+
+
+def _u32p_type():
+    return C.POINTER(C.c_uint32)
 
 
 def pick_sources(degrees, count: int, seed: int) -> np.ndarray:

@@ -52,7 +52,8 @@ typedef struct bfs_graph bfs_graph;
 #define BFS_LOAD_PREFER_REORDER 0x2u /* try <data>_reorder_* before <data>_* */
 #define BFS_LOAD_HOST_ONLY 0x4u    /* parse and validate only; allocate nothing on the GPU */
 #define BFS_LOAD_DEVICE_BUILD 0x8u /* bfs_graph_from_edges: build CSR, in-edge lists and packed tiles on the
-                                      GPU (edge order inside rows and tiles unspecified; results unchanged) */
+                                      GPU (edge order inside rows and tiles unspecified; results unchanged);
+                                      src and dst may then be host or device memory */
 
 /*
  * Loads a graph from the reference's tiled text files and uploads it to HBM.
@@ -536,6 +537,13 @@ typedef struct bfs_rmat_params {
 
 /* Seeded, platform-independent R-MAT edge list into src/dst (capacity >= num_edges). */
 int bfs_gen_rmat(const bfs_rmat_params *p, uint32_t *src, uint32_t *dst, uint64_t capacity);
+/* The same edge list, element for element, drawn on the current CUDA device
+ * into DEVICE memory src/dst (capacity >= num_edges; num_edges < 2^32).  It
+ * allocates its own temporaries (with deduplication a hash table of about
+ * 2 x 12 bytes per edge, rounded up to a power of two) and returns when the
+ * list is written.  The bench's large synthetic graphs come from here (the
+ * host generator takes over a minute for 1.47 G edges). */
+int bfs_gen_rmat_device(const bfs_rmat_params *p, uint32_t *src, uint32_t *dst, uint64_t capacity);
 
 /* Library version string. */
 const char *bfs_version(void);
