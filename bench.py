@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--serve", default="c4", help="serving measurement: 'c4' (8 graphs, Poisson load) or 'none'")
     ap.add_argument("--serve-rates", default="2000,10000,50000", help="query arrival rates (queries/s)")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="arrival window per rate")
+    ap.add_argument("--large", default="twitter", help="large single-GPU graph measured last ('none' skips it)")
+    ap.add_argument("--large-sources", type=int, default=16, help="large graph: single-source traversals")
+    ap.add_argument("--large-batch", type=int, default=1024, help="large graph: sources of the batched traversal")
+    ap.add_argument("--large-budget-mb", type=int, default=65536, help="large graph: HBM budget of the level planes")
     return ap.parse_args()
 
 
@@ -572,6 +576,107 @@ def bench_serving(args, torch, dev):
     return res
 
 
+def bench_large(args, torch, dev):
+    """The large single-GPU configuration (Twitter shape: 41,652,230 vertices,
+    1,468,365,182 edges, permuted ids, W=1024, S=16): the edge list drawn on
+    the GPU (the host generator's list, element for element), the layout built
+    on the GPU from the device arrays, then `large_sources` single-source
+    traversals and one `large_batch`-source batched traversal, timed with CUDA
+    events, L2 flushed before each.  Parity at full size: the BFS-level
+    certificate of the oracle (oracle/bfs_oracle.c orc_check_levels: every
+    edge and vertex checked against the levels) for 2 single-source results
+    and 2 batched rows."""
+    import bfs_simd_benchmarks_gb300 as B
+    from oracle import oracle as O
+    wl = workloads.get(args.large)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ds, dd = B.gen_rmat_device(wl.n, wl.m, wl.a, wl.b, wl.c, seed=wl.seed, permute=wl.permute)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g = B.Graph.from_device_edges(wl.n, ds.data_ptr(), dd.data_ptr(), wl.m, wl.w, wl.s)
+    build_s = time.perf_counter() - t0
+    hs = ds.cpu().numpy().view(np.uint32)
+    hd = dd.cpu().numpy().view(np.uint32)
+    del ds, dd
+    torch.cuda.empty_cache()
+    deg = g.degrees()
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    lev = torch.empty(wl.n, dtype=torch.int32, device=dev)
+    par = torch.empty(wl.n, dtype=torch.int32, device=dev)
+    sources = wl.sources(deg, args.large_sources)
+
+    def single(s):
+        with torch.cuda.stream(stream):
+            flush.fill_(int(s) & 0xFF)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.run_device(int(s), lev.data_ptr(), par.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+        st = g.last_stats()
+        if st["status"] != 0:
+            raise RuntimeError(f"large graph: traversal status {st['status']}")
+        return e0.elapsed_time(e1), st
+
+    for s in sources[:2]:
+        single(s)
+    runs = [single(s) for s in sources]
+    s_ms = sum(r[0] for r in runs)
+    s_edges = sum(r[1]["edges_traversed"] for r in runs)
+    checks, ok = 0, 0
+    for s in sources[:2]:
+        single(s)
+        checks += 1
+        ok += int(O.check_levels(wl.n, hs, hd, int(s), lev.cpu().numpy()) == 0)
+    # the batched traversal
+    g.set_options(batch_budget_mb=args.large_budget_mb)
+    bsrc = wl.sources(deg, args.large_batch)
+    out = torch.empty((len(bsrc), wl.n), dtype=torch.uint8, device=dev)
+    bruns = []
+    for i in range(3):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.run_batch_device(bsrc, out.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+        st = g.last_batch_stats()
+        if st["status"] != 0:
+            raise RuntimeError(f"large graph: batched status {st['status']}")
+        if i >= 1:
+            bruns.append((e0.elapsed_time(e1), st))
+    b_ms = statistics.mean(r[0] for r in bruns)
+    b_edges = bruns[0][1]["edges_traversed"]
+    for i in (0, len(bsrc) - 1):
+        row = out[i].cpu().numpy()
+        checks += 1
+        ok += int(O.check_levels(wl.n, hs, hd, int(bsrc[i]), np.where(row == 255, -1, row.astype(np.int32))) == 0)
+    single_gteps = s_edges / (s_ms / 1e3) / 1e9
+    batch_gteps = b_edges / (b_ms / 1e3) / 1e9
+    st = bruns[-1][1]
+    res = {"workload": wl.describe() | {"sources": len(sources), "batch_sources": len(bsrc)},
+           "generate_s": round(gen_s, 2), "generator": "bfs_gen_rmat_device (the host generator's edge list)",
+           "graph_build_s": round(build_s, 2),
+           "single_source": {"gteps": single_gteps, "ms_per_traversal_mean": s_ms / len(runs),
+                             "edges_per_traversal_mean": s_edges / len(runs), "sources": len(runs)},
+           "batched": {"gteps": batch_gteps, "ms_per_batch_mean": b_ms, "levels_ms": st["levels_ms"],
+                       "output_ms": st["output_ms"], "depth": st["depth"], "planes": st["planes"],
+                       "spills": st["spills"], "words_per_vertex": st["words_per_vertex"],
+                       "output_bytes": len(bsrc) * wl.n, "steps": len(bruns)},
+           "speedup_batched_vs_single_source": batch_gteps / single_gteps,
+           "parity": f"{ok}/{checks} level vectors (2 single-source, 2 batched rows) pass the oracle's BFS-level "
+                     "certificate over all edges and vertices (oracle/bfs_oracle.c orc_check_levels)",
+           "l2": "flushed (256 MiB write) before every traversal and batch"}
+    del out
+    g.close()
+    torch.cuda.empty_cache()
+    return res
+
+
 def serve_host_check(srv, graphs, edges, pools, count: int = 256, per_graph: int = 2):
     """A burst of `count` queries over all graphs with levels delivered to
     host memory; `per_graph` results of every graph compared with the oracle."""
@@ -726,6 +831,7 @@ def main():
             got, _, _ = g.run(s, parents=False)
             ok += int(np.array_equal(got, ref))
         parity = f"levels bit-exact on {ok}/{len(cpu_levels)} sources checked against the oracle"
+    large = None
     bc = None
     if args.bc_sources > 0 and world == 1:
         bc_arr = None
@@ -733,6 +839,8 @@ def main():
             from oracle import oracle as O
             bc_arr = O.csr_arrays(wl.n, src, dst)
         bc = bench_bc(args, torch, dev, g, sources, flush, bc_arr)
+    if args.large != "none" and world == 1:
+        large = bench_large(args, torch, dev)
     if rank == 0:
         clocks = clk.summary()
         line = {
@@ -775,6 +883,7 @@ def main():
             "batched": batched,
             "serving": serving,
             "betweenness": bc,
+            "large": large,
         }
         print(json.dumps(line))
     if world > 1:

@@ -1147,3 +1147,46 @@ int orc_gen_rmat(unsigned n, unsigned long long m, double a, double b, double c,
 	free(out);
 	return ORC_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* BFS level certificate over an edge list                                  */
+/* ------------------------------------------------------------------------ */
+
+/* Checks that cost[] are the BFS distances from `source` in the directed
+ * edge list (src[i] -> dst[i]) without running a BFS, so that graphs of
+ * billions of edges can be checked in seconds: cost is the distance function
+ * exactly when
+ *   (1) cost[source] == 0 and no other vertex has cost 0 or below -1;
+ *   (2) every edge u -> v with cost[u] >= 0 has 0 <= cost[v] <= cost[u] + 1;
+ *   (3) every v != source with cost[v] >= 0 has an edge u -> v with
+ *       cost[u] == cost[v] - 1.
+ * ((2) bounds every reached cost by the distance along any path from the
+ * source; (3) gives every reached vertex a path of exactly cost[v] edges.)
+ * Returns the number of violated conditions (0 = the levels are the BFS
+ * levels).  OpenMP over the edges and the vertices. */
+unsigned long long orc_check_levels(unsigned n, unsigned long long m, const unsigned *src, const unsigned *dst,
+		unsigned source, const int *cost)
+{
+	if (source >= n) return 1;
+	unsigned long long bad = 0;
+	unsigned char *has_parent = (unsigned char *) calloc(n ? n : 1, 1);
+	if (!has_parent) return 1;
+	if (cost[source] != 0) bad++;
+	#pragma omp parallel for schedule(static) reduction(+:bad)
+	for (int64_t v = 0; v < (int64_t) n; ++v)
+		if ((unsigned) v != source && (cost[v] == 0 || cost[v] < -1)) bad++;
+	#pragma omp parallel for schedule(static) reduction(+:bad)
+	for (int64_t i = 0; i < (int64_t) m; ++i) {
+		const unsigned u = src[i], v = dst[i];
+		if (u >= n || v >= n) { bad++; continue; }
+		const int cu = cost[u], cv = cost[v];
+		if (cu < 0) continue;
+		if (cv < 0 || cv > cu + 1) bad++;
+		else if (cv == cu + 1) has_parent[v] = 1;  /* a benign race: every writer stores 1 */
+	}
+	#pragma omp parallel for schedule(static) reduction(+:bad)
+	for (int64_t v = 0; v < (int64_t) n; ++v)
+		if ((unsigned) v != source && cost[v] > 0 && !has_parent[v]) bad++;
+	free(has_parent);
+	return bad;
+}

@@ -69,11 +69,12 @@ def lib() -> C.CDLL:
             "orc_max_threads": [],
             "orc_gen_rmat": [C.c_uint, C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.c_ulonglong, C.c_uint,
                              _u32p, _u32p],
+            "orc_check_levels": [C.c_uint, C.c_ulonglong, _u32p, _u32p, C.c_uint, _i32p],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
             fn.argtypes = args
-            fn.restype = C.c_ulonglong if name == "orc_check_parents" else C.c_int
+            fn.restype = C.c_ulonglong if name in ("orc_check_parents", "orc_check_levels") else C.c_int
         _lib = L
     return _lib
 
@@ -184,6 +185,14 @@ def bc_single(arr: dict, source: int):
                             _p(sigma), dep.ctypes.data_as(C.POINTER(C.c_float)), _p(cost),
                             scale.ctypes.data_as(C.POINTER(C.c_double))), "bc_single")
     return sigma, dep, cost, scale
+
+
+def check_levels(n: int, src, dst, source: int, cost) -> int:
+    """Violations of the BFS-level certificate (orc_check_levels): 0 when cost
+    are exactly the BFS levels from source in the edge list src -> dst."""
+    s, d = _u(src), _u(dst)
+    c = np.ascontiguousarray(cost, dtype=np.int32)
+    return int(lib().orc_check_levels(n, s.size, _p(s), _p(d), int(source), _p(c)))
 
 
 def max_threads() -> int:

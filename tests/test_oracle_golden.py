@@ -112,3 +112,29 @@ def test_oracle_generator_equals_product_generator(native, oracle, n, m, permute
     b = B.gen_rmat(n, m, seed=77, permute=permute, dedup=dedup, no_self_loops=not loops)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_level_certificate_accepts_bfs_levels_and_rejects_others(oracle):
+    """orc_check_levels (the full-size check of the bench's large graph)
+    against the oracle's BFS on R-MAT graphs, and on planted mistakes."""
+    import bfs_simd_benchmarks_gb300 as B
+    rng = np.random.default_rng(3)
+    for n, m, perm in ((1 << 12, 1 << 16, False), (3000, 30000, True)):
+        src, dst = oracle.gen_rmat(n, m, seed=31, permute=perm)
+        arr = oracle.csr_arrays(n, src, dst)
+        for s in B.pick_sources(arr["degrees"], 3, seed=8):
+            lev = oracle.bfs_levels(arr, int(s))
+            assert oracle.check_levels(n, src, dst, int(s), lev) == 0
+            reached = np.flatnonzero(lev > 0)
+            for mutate in range(4):
+                bad = lev.copy()
+                v = int(rng.choice(reached))
+                if mutate == 0:
+                    bad[v] += 1            # too deep
+                elif mutate == 1:
+                    bad[v] = max(1, bad[v] - 1) if bad[v] > 1 else 2
+                elif mutate == 2:
+                    bad[v] = -1            # dropped a reached vertex
+                else:
+                    bad[int(s)] = 1        # wrong source
+                assert oracle.check_levels(n, src, dst, int(s), bad) > 0
