@@ -26,6 +26,7 @@ BFS_LOAD_WEIGHTED = 0x1
 BFS_LOAD_PREFER_REORDER = 0x2
 BFS_LOAD_HOST_ONLY = 0x4
 BFS_LOAD_DEVICE_BUILD = 0x8
+BFS_LOAD_DEGREE_ORDER = 0x20
 BFS_TOOL_DEVICE = 0x10
 
 BFS_MODE_PERSISTENT = 0
@@ -196,6 +197,7 @@ class Stats(C.Structure):
 
 
 BFS_TUNE_SINGLE, BFS_TUNE_BATCH, BFS_TUNE_MAX_TRIALS = 1, 2, 256
+BFS_TUNE_DEVICE_BUILD, BFS_TUNE_LAYOUTS = 4, 8
 
 
 class TuneTrial(C.Structure):
@@ -205,7 +207,7 @@ class TuneTrial(C.Structure):
         ("options", Options),
         ("gteps", C.c_double),
         ("kind", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("load_flags", C.c_uint32),
     ]
 
 
@@ -220,6 +222,8 @@ class TuneResult(C.Structure):
         ("default_batch_gteps", C.c_double),
         ("num_trials", C.c_uint32),
         ("from_cache", C.c_uint32),
+        ("load_flags", C.c_uint32),
+        ("reserved", C.c_uint32),
         ("trials", TuneTrial * BFS_TUNE_MAX_TRIALS),
     ]
 
@@ -228,7 +232,8 @@ class TuneResult(C.Structure):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("options", "trials")}
         d["options"] = opt(self.options)
         d["trials"] = [{"tile_width": t.tile_width, "stripe_length": t.stripe_length, "gteps": t.gteps,
-                        "kind": t.kind, "options": opt(t.options)} for t in self.trials[:self.num_trials]]
+                        "kind": t.kind, "load_flags": t.load_flags, "options": opt(t.options)}
+                       for t in self.trials[:self.num_trials]]
         return d
 
 

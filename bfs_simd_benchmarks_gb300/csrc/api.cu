@@ -52,6 +52,13 @@ struct bfs_graph {
 	size_t device_bytes = 0;
 	int32_t *level_buf = nullptr;    // internal outputs for bfs_run
 	uint32_t *parent_buf = nullptr;
+	// BFS_LOAD_DEGREE_ORDER: the device layout uses ids ranked by out-degree;
+	// callers' ids are mapped in (sources) and out (levels, parents)
+	bool relabeled = false;
+	std::vector<uint32_t> new_of_old;
+	uint32_t *d_new_of_old = nullptr, *d_old_of_new = nullptr;
+	int32_t *rl_level = nullptr;     // a run's outputs in the layout's ids
+	uint32_t *rl_parent = nullptr;
 	DevStats *h_stats = nullptr;     // pinned
 	unsigned long long *h_part = nullptr;  // pinned (stepwise mode): one slot's per-CTA partials
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
@@ -108,6 +115,42 @@ int cuda_ok(cudaError_t e) { return e == cudaSuccess ? BFS_OK : BFS_ECUDA; }
 // Bound of the device-side waits of a run, from the options (0 = default).
 uint64_t wait_limit_ns(const bfs_options &o) {
 	return o.wait_limit_us ? (uint64_t) o.wait_limit_us * 1000ull : 2000000000ull;  // default 2 s
+}
+
+// The degree order of tools/vertex_id_reorder_to_degrees (bfs.cpp:50-80)
+// with a deterministic tie-break: new ids by out-degree descending, equal
+// degrees by ascending old id (a stable counting sort by degree).  The tool
+// breaks ties with rand(); this order is the project's own.
+std::vector<uint32_t> degree_order(const std::vector<uint32_t> &deg) {
+	const uint32_t n = (uint32_t) deg.size();
+	uint32_t maxd = 0;
+	for (uint32_t d : deg) maxd = std::max(maxd, d);
+	std::vector<uint64_t> start((size_t) maxd + 2, 0);
+	for (uint32_t d : deg) start[maxd - d + 1]++;  // bucket maxd - d: highest degree first
+	for (size_t b = 1; b < start.size(); ++b) start[b] += start[b - 1];
+	std::vector<uint32_t> new_of_old(n);
+	for (uint32_t v = 0; v < n; ++v) new_of_old[v] = (uint32_t) start[maxd - deg[v]]++;
+	return new_of_old;
+}
+
+__global__ void k_relabel_edges(uint64_t m, const uint32_t *new_of_old, uint32_t *src, uint32_t *dst) {
+	for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t) gridDim.x * blockDim.x) {
+		src[i] = __ldg(new_of_old + src[i]);
+		dst[i] = __ldg(new_of_old + dst[i]);
+	}
+}
+
+// levels[v] / parents[v] in the caller's ids from a run in the layout's ids
+__global__ void k_unrelabel(uint32_t n, const uint32_t *new_of_old, const uint32_t *old_of_new, const int32_t *lv_new,
+		const uint32_t *pa_new, int32_t *levels, uint32_t *parents) {
+	for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+		const uint32_t x = __ldg(new_of_old + v);
+		levels[v] = lv_new[x];
+		if (parents) {
+			const uint32_t p = pa_new[x];
+			parents[v] = p == 0xFFFFFFFFu ? p : __ldg(old_of_new + p);
+		}
+	}
 }
 
 template <class T> int dev_alloc(bfs_graph *g, T **out, size_t count) {
@@ -352,7 +395,7 @@ struct TmpDev {
 // segment offsets, and a scatter; the out-degrees and in-edge offsets come
 // back for the host-side fields.
 int upload_device_build(bfs_graph *g, uint32_t n, uint64_t m, const uint32_t *src, const uint32_t *dst, uint32_t w,
-		uint32_t s) {
+		uint32_t s, std::vector<uint32_t> *degree_order_out) {
 	g->n = n;
 	g->m = m;
 	g->w = w;
@@ -382,6 +425,20 @@ int upload_device_build(bfs_graph *g, uint32_t n, uint64_t m, const uint32_t *sr
 	int herr = 0;
 	if (cudaMemcpy(&herr, d_err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BFS_ECUDA;
 	if (herr) return herr;
+	if (degree_order_out) {
+		// relabel the edges by the degree order, then count again
+		std::vector<uint32_t> deg(n);
+		if (cudaMemcpy(deg.data(), out_deg, (size_t) n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BFS_ECUDA;
+		*degree_order_out = degree_order(deg);
+		uint32_t *d_map = nullptr;
+		if ((st = tmp.alloc(&d_map, n))) return st;
+		if (cudaMemcpy(d_map, degree_order_out->data(), (size_t) n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+			return BFS_ECUDA;
+		k_relabel_edges<<<g->num_sms * 8, 512, 0, cs>>>(m, d_map, d_src, d_dst);
+		if (cudaMemset(out_deg, 0, (size_t) n * 4) != cudaSuccess || cudaMemset(in_deg, 0, (size_t) n * 4) != cudaSuccess)
+			return BFS_ECUDA;
+		if ((st = dbuild_degrees(d_src, d_dst, m, n, out_deg, in_deg, d_err, g->num_sms, cs))) return st;
+	}
 	// CSR and in-edge lists
 	uint32_t *row_off = nullptr, *col = nullptr, *in_off = nullptr, *in_src = nullptr;
 	if ((st = dev_alloc(g, &row_off, (size_t) n + 1)) || (st = dev_alloc(g, &col, m)) ||
@@ -457,6 +514,33 @@ int upload_device_build(bfs_graph *g, uint32_t n, uint64_t m, const uint32_t *sr
 	d.hasin = hasin;
 	set_shape(g, pk, words);
 	return alloc_run(g);
+}
+
+// Makes a graph built on relabelled edges answer in the caller's ids: the
+// maps on the device, run buffers in the layout's ids, out-degrees in the
+// caller's order.
+int attach_relabel(bfs_graph *g, std::vector<uint32_t> &&new_of_old) {
+	const uint32_t n = g->n;
+	std::vector<uint32_t> old_of_new(n);
+	for (uint32_t v = 0; v < n; ++v) old_of_new[new_of_old[v]] = v;
+	std::vector<uint32_t> deg(n);
+	for (uint32_t v = 0; v < n; ++v) deg[v] = g->degrees[new_of_old[v]];
+	g->degrees.swap(deg);
+	int st;
+	if (g->host_only) {
+		g->new_of_old = std::move(new_of_old);
+		g->relabeled = true;
+		return BFS_OK;
+	}
+	if ((st = dev_alloc(g, &g->d_new_of_old, n)) || (st = dev_alloc(g, &g->d_old_of_new, n)) ||
+			(st = dev_alloc(g, &g->rl_level, n)) || (st = dev_alloc(g, &g->rl_parent, n)))
+		return st;
+	if (cudaMemcpy(g->d_new_of_old, new_of_old.data(), (size_t) n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+			cudaMemcpy(g->d_old_of_new, old_of_new.data(), (size_t) n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+		return BFS_ECUDA;
+	g->new_of_old = std::move(new_of_old);
+	g->relabeled = true;
+	return BFS_OK;
 }
 
 int finish_graph(HostGraph &h, uint32_t flags, bfs_graph **out) {
@@ -557,10 +641,10 @@ int run_impl(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, 
 	if (source >= g->n || !levels) return BFS_EARG;
 	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
 	RunCtx r = g->rc;
-	r.level = levels;
-	r.parent = parents;
+	r.level = g->relabeled ? g->rl_level : levels;
+	r.parent = g->relabeled ? (parents ? g->rl_parent : nullptr) : parents;
 	StepParams p{};
-	p.source = source;
+	p.source = g->relabeled ? g->new_of_old[source] : source;
 	p.warp_max_degree = g->opt.warp_max_degree;
 	p.cta_max_degree = g->opt.cta_max_degree;
 	p.bottom_up = g->opt.bottom_up;
@@ -582,6 +666,11 @@ int run_impl(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, 
 		if ((rc = run_stepwise(g, r, p, st))) return rc;
 	} else {
 		if ((rc = launch_persistent(g->dg, r, p, g->batch, g->grid, g->smem, st))) return rc;
+	}
+	if (g->relabeled) {
+		k_unrelabel<<<g->num_sms * 4, 512, 0, st>>>(g->n, g->d_new_of_old, g->d_old_of_new, r.level, r.parent, levels,
+				parents);
+		if (cudaGetLastError() != cudaSuccess) return BFS_ECUDA;
 	}
 	if (cudaEventRecord(g->ev1, st) != cudaSuccess) return BFS_ECUDA;
 	g->last_stream = st;
@@ -755,7 +844,7 @@ bool stream_capturing(cudaStream_t st) {
 // `dev_sources`: `sources` is device memory (validated by the kernel).
 int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *levels, cudaStream_t st,
 		cudaEvent_t wait_before = nullptr, cudaEvent_t between = nullptr, bool dev_sources = false) {
-	if (g->host_only) return BFS_EUNSUPPORTED;
+	if (g->host_only || g->relabeled) return BFS_EUNSUPPORTED;
 	if (!sources || !levels || ns == 0 || ns > BFS_BATCH_MAX_SOURCES) return BFS_EARG;
 	if (!dev_sources)
 		for (uint32_t i = 0; i < ns; ++i)
@@ -934,6 +1023,7 @@ int bc_prepare(bfs_graph *g) {
 // dependency launch.  sigma / delta: where the path counts and dependencies go
 // (the graph's own buffers when null); acc: accumulated into when non-null.
 int bc_enqueue(bfs_graph *g, uint32_t source, uint32_t *sigma, float *delta, float *acc, cudaStream_t st) {
+	if (g->relabeled) return BFS_EUNSUPPORTED;
 	auto &b = g->bc;
 	RunCtx r = g->rc;
 	r.level = g->level_buf;
@@ -1191,7 +1281,8 @@ int run_batch_ex(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *le
 size_t graph_device_bytes(const bfs_graph *g) { return g ? g->device_bytes : 0; }
 uint32_t graph_num_vertices(const bfs_graph *g) { return g ? g->n : 0; }
 int graph_device(const bfs_graph *g) { return g ? g->device : -1; }
-bool graph_on_device(const bfs_graph *g) { return g && !g->host_only; }
+// a graph the batched kernels can serve (on the device, caller's own ids)
+bool graph_on_device(const bfs_graph *g) { return g && !g->host_only && !g->relabeled; }
 
 } // namespace bfsg
 
@@ -1257,9 +1348,13 @@ int bfs_graph_from_edges(uint32_t num_vertices, uint64_t num_edges, const uint32
 	*out = nullptr;
 	int st = check_shape(num_vertices, num_edges, tile_width, stripe_length);
 	if (st) return st;
+	const bool degree_order_layout = flags & BFS_LOAD_DEGREE_ORDER;
 	if ((flags & BFS_LOAD_DEVICE_BUILD) && !(flags & BFS_LOAD_HOST_ONLY)) {
 		bfs_graph *g = new bfs_graph();
-		st = upload_device_build(g, num_vertices, num_edges, src, dst, tile_width, stripe_length);
+		std::vector<uint32_t> new_of_old;
+		st = upload_device_build(g, num_vertices, num_edges, src, dst, tile_width, stripe_length,
+				degree_order_layout ? &new_of_old : nullptr);
+		if (!st && degree_order_layout) st = attach_relabel(g, std::move(new_of_old));
 		if (st) {
 			release(g);
 			delete g;
@@ -1267,6 +1362,26 @@ int bfs_graph_from_edges(uint32_t num_vertices, uint64_t num_edges, const uint32
 		}
 		*out = g;
 		return BFS_OK;
+	}
+	// the degree-ordered layout on the host: relabelled copies of the edges
+	std::vector<uint32_t> rs, rd, new_of_old;
+	if (degree_order_layout) {
+		std::vector<uint32_t> deg(num_vertices, 0);
+		for (uint64_t i = 0; i < num_edges; ++i) {
+			if (src[i] >= num_vertices || dst[i] >= num_vertices) return BFS_EFORMAT;
+			deg[src[i]]++;
+		}
+		new_of_old = degree_order(deg);
+		rs.resize(num_edges);
+		rd.resize(num_edges);
+		parallel_for(num_edges, [&](uint64_t lo, uint64_t hi, unsigned) {
+			for (uint64_t i = lo; i < hi; ++i) {
+				rs[i] = new_of_old[src[i]];
+				rd[i] = new_of_old[dst[i]];
+			}
+		});
+		src = rs.data();
+		dst = rd.data();
 	}
 	HostGraph h;
 	init_shape(h, num_vertices, num_edges, tile_width, stripe_length);
@@ -1276,7 +1391,13 @@ int bfs_graph_from_edges(uint32_t num_vertices, uint64_t num_edges, const uint32
 	if ((st = colmajor_from_csr(num_vertices, num_edges, tile_width, stripe_length, cs.data(), h.csr_dst.data(),
 				 h.heads, h.tails, nullptr)))
 		return st;
-	return finish_graph(h, flags, out);
+	if ((st = finish_graph(h, flags, out))) return st;
+	if (degree_order_layout && (st = attach_relabel(*out, std::move(new_of_old)))) {
+		bfs_graph_free(*out);
+		*out = nullptr;
+		return st;
+	}
+	return BFS_OK;
 }
 
 int bfs_graph_from_arrays(uint32_t num_vertices, uint64_t num_edges, const uint32_t *degrees, const uint32_t *csr_dst,
@@ -1321,7 +1442,7 @@ int bfs_graph_bfs_order(bfs_graph *g, uint32_t source, uint32_t *vertex_map) {
 
 int bfs_graph_save(const bfs_graph *g, const char *path) {
 	if (!g || !path) return BFS_EARG;
-	if (g->host_only) return BFS_EUNSUPPORTED;
+	if (g->host_only || g->relabeled) return BFS_EUNSUPPORTED;
 	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
 	FILE *f = std::fopen(path, "wb");
 	if (!f) return BFS_EIO;
@@ -1453,7 +1574,7 @@ int bfs_batch_graph_create(bfs_graph *g, const uint32_t *sources, uint32_t num_s
 	if (!g || !out) return BFS_EARG;
 	*out = nullptr;
 	std::lock_guard<std::mutex> lk(g->mu);
-	if (g->host_only) return BFS_EUNSUPPORTED;
+	if (g->host_only || g->relabeled) return BFS_EUNSUPPORTED;
 	if (!sources || !levels || num_sources == 0 || num_sources > BFS_BATCH_MAX_SOURCES) return BFS_EARG;
 	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
 	// allocate the batch state before capturing (no allocation inside a capture)

@@ -16,6 +16,7 @@
 // only time does.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -33,6 +34,7 @@ struct Tuner {
 	uint32_t tile_width, stripe_length;
 	uint8_t *d_levels = nullptr;  // batch output
 	bfs_tune_result *res;
+	uint32_t load_flags = 0;      // the layout of the graph being tuned
 };
 
 void add_trial(Tuner &t, const bfs_options &o, double gteps, uint32_t kind) {
@@ -44,6 +46,7 @@ void add_trial(Tuner &t, const bfs_options &o, double gteps, uint32_t kind) {
 	tr.options = o;
 	tr.gteps = gteps;
 	tr.kind = kind;
+	tr.load_flags = t.load_flags;
 }
 
 // Single-source GTEPS of the sources with options o (0 on any error).
@@ -149,6 +152,8 @@ bool cache_lookup(const char *path, const std::string &key, bfs_tune_result *r) 
 		r->single_gteps = sg;
 		r->batch_gteps = bg;
 		r->from_cache = 1;
+		const char *lf = std::strstr(line, " layout=");
+		r->load_flags = lf ? (uint32_t) std::strtoul(lf + 8, nullptr, 10) : 0u;
 		found = true;  // the last matching line wins
 	}
 	std::fclose(f);
@@ -162,7 +167,7 @@ void cache_append(const char *path, const std::string &key, const bfs_tune_resul
 			r->batch_gteps);
 	bfs_options o = r->options;
 	for (int i = 0; i < kNumFields; ++i) std::fprintf(f, " %s=%u", kFields[i], *field_ptr(o, i));
-	std::fprintf(f, "\n");
+	std::fprintf(f, " layout=%u\n", r->load_flags);
 	std::fclose(f);
 }
 
@@ -291,18 +296,24 @@ int bfs_autotune(uint32_t num_vertices, uint64_t num_edges, const uint32_t *src,
 	if (cache_path && cache_lookup(cache_path, key, result)) return BFS_OK;
 
 	const bool by_single = flags & BFS_TUNE_SINGLE;
+	// layouts: the caller's ids, and (single-source tuning only) the degree order
+	std::vector<uint32_t> layouts = {0u};
+	if ((flags & BFS_TUNE_LAYOUTS) && !(flags & BFS_TUNE_BATCH)) layouts.push_back(BFS_LOAD_DEGREE_ORDER);
+	const uint32_t build_flags = (flags & BFS_TUNE_DEVICE_BUILD) ? BFS_LOAD_DEVICE_BUILD : 0u;
 	double best = -1;
 	bool first = true;
 	int last_err = BFS_EUNSUPPORTED;
+	for (uint32_t layout : layouts)
 	for (uint32_t wi = 0; wi < num_widths; ++wi) {
 		for (uint32_t si = 0; si < num_stripes; ++si) {
 			bfs_graph *g = nullptr;
-			int st = bfs_graph_from_edges(num_vertices, num_edges, src, dst, tile_widths[wi], stripe_lengths[si], 0, &g);
+			int st = bfs_graph_from_edges(num_vertices, num_edges, src, dst, tile_widths[wi], stripe_lengths[si],
+					build_flags | layout, &g);
 			if (st) {
 				last_err = st;
 				continue;  // a shape the packing cannot hold
 			}
-			Tuner t{g, sources, num_sources, tile_widths[wi], stripe_lengths[si], nullptr, result};
+			Tuner t{g, sources, num_sources, tile_widths[wi], stripe_lengths[si], nullptr, result, layout};
 			bfs_options o;
 			double sg = 0, bg = 0, dsg = 0, dbg = 0;
 			st = tune(t, flags, &o, &sg, &bg, &dsg, &dbg);
@@ -324,6 +335,7 @@ int bfs_autotune(uint32_t num_vertices, uint64_t num_edges, const uint32_t *src,
 				result->options = o;
 				result->single_gteps = sg;
 				result->batch_gteps = bg;
+				result->load_flags = layout;
 			}
 		}
 	}

@@ -45,14 +45,17 @@ class Graph:
 
     @classmethod
     def from_edges(cls, num_vertices: int, src, dst, tile_width: int, stripe_length: int,
-                   host_only: bool = False, device_build: bool = False) -> "Graph":
-        """device_build: build the layout on the GPU (BFS_LOAD_DEVICE_BUILD)."""
+                   host_only: bool = False, device_build: bool = False, degree_order: bool = False) -> "Graph":
+        """device_build: build the layout on the GPU (BFS_LOAD_DEVICE_BUILD);
+        degree_order: lay it out on degree-ranked ids (BFS_LOAD_DEGREE_ORDER;
+        every call still takes and returns the caller's ids)."""
         lib = N.load()
         s, d = _u32(src), _u32(dst)
         if s.shape != d.shape:
             raise ValueError("src and dst differ in length")
         h = C.c_void_p()
-        flags = (N.BFS_LOAD_HOST_ONLY if host_only else 0) | (N.BFS_LOAD_DEVICE_BUILD if device_build else 0)
+        flags = ((N.BFS_LOAD_HOST_ONLY if host_only else 0) | (N.BFS_LOAD_DEVICE_BUILD if device_build else 0)
+                 | (N.BFS_LOAD_DEGREE_ORDER if degree_order else 0))
         N.check(lib.bfs_graph_from_edges(num_vertices, s.size, _ptr(s, C.c_uint32), _ptr(d, C.c_uint32),
                                          tile_width, stripe_length, flags, C.byref(h)), "bfs_graph_from_edges")
         return cls(h)
@@ -380,13 +383,16 @@ def tile_size_range(num_vertices: int, num_edges: int) -> tuple[int, int]:
 
 
 def autotune(num_vertices: int, src, dst, sources, tile_widths=(512, 1024, 2048, 4096), stripe_lengths=(8, 16, 32),
-             single: bool = True, batch: bool = False, cache_path: str | None = None) -> dict:
-    """bfs_autotune: the best tile shape and options of an edge list, by measurement.
-    tile_widths=None: the powers of two in tile_size_range(N, E)."""
+             single: bool = True, batch: bool = False, cache_path: str | None = None, device_build: bool = False,
+             layouts: bool = False) -> dict:
+    """bfs_autotune: the best tile shape, layout and options of an edge list, by
+    measurement.  tile_widths=None: the powers of two in tile_size_range(N, E);
+    layouts: also try the degree-ordered layout (single-source tuning)."""
     s, d, so = _u32(src), _u32(dst), _u32(sources)
     w, sl = _u32(tile_widths if tile_widths is not None else []), _u32(stripe_lengths)
     r = N.TuneResult()
-    flags = (N.BFS_TUNE_SINGLE if single else 0) | (N.BFS_TUNE_BATCH if batch else 0)
+    flags = ((N.BFS_TUNE_SINGLE if single else 0) | (N.BFS_TUNE_BATCH if batch else 0)
+             | (N.BFS_TUNE_DEVICE_BUILD if device_build else 0) | (N.BFS_TUNE_LAYOUTS if layouts else 0))
     N.check(N.load().bfs_autotune(num_vertices, s.size, _ptr(s, C.c_uint32), _ptr(d, C.c_uint32),
                                   _ptr(so, C.c_uint32), so.size, _ptr(w, C.c_uint32), w.size, _ptr(sl, C.c_uint32),
                                   sl.size, flags, cache_path.encode() if cache_path else None, C.byref(r)),

@@ -51,6 +51,13 @@ typedef struct bfs_graph bfs_graph;
 #define BFS_LOAD_WEIGHTED 0x1u     /* files carry "u v w" lines (-w); weights are dropped */
 #define BFS_LOAD_PREFER_REORDER 0x2u /* try <data>_reorder_* before <data>_* */
 #define BFS_LOAD_HOST_ONLY 0x4u    /* parse and validate only; allocate nothing on the GPU */
+#define BFS_LOAD_DEGREE_ORDER 0x20u /* bfs_graph_from_edges: lay the graph out on vertex ids ranked by
+                                       out-degree (descending, ties by ascending id) -- the layout of
+                                       tools/vertex_id_reorder_to_degrees, with this library's tie-break;
+                                       every call still takes and returns the caller's ids (sources are
+                                       mapped in, levels and parents gathered back on the device);
+                                       single-source runs only (batches, betweenness, serving and
+                                       bfs_graph_save answer BFS_EUNSUPPORTED) */
 #define BFS_LOAD_DEVICE_BUILD 0x8u /* bfs_graph_from_edges: build CSR, in-edge lists and packed tiles on the
                                       GPU (edge order inside rows and tiles unspecified; results unchanged);
                                       src and dst may then be host or device memory */
@@ -296,6 +303,8 @@ int bfs_batch_graph_destroy(bfs_batch_graph *bg);
  * by hand with tools/tile-size-computer and the T_RATIO constant) -------- */
 #define BFS_TUNE_SINGLE 1u  /* tune the single-source options (variant, switch ratios, bucket bounds) */
 #define BFS_TUNE_BATCH 2u   /* tune batch_push_div on one batch of all the sources */
+#define BFS_TUNE_DEVICE_BUILD 4u  /* bfs_autotune: build each candidate layout on the GPU */
+#define BFS_TUNE_LAYOUTS 8u  /* bfs_autotune (single-source): also try BFS_LOAD_DEGREE_ORDER per shape */
 #define BFS_TUNE_MAX_TRIALS 256
 
 typedef struct bfs_tune_trial {
@@ -303,7 +312,7 @@ typedef struct bfs_tune_trial {
 	bfs_options options;
 	double gteps;              /* single-source trials: sum m(s) / sum kernel time; batch trials: the batch's */
 	uint32_t kind;             /* BFS_TUNE_SINGLE or BFS_TUNE_BATCH */
-	uint32_t reserved;
+	uint32_t load_flags;       /* layout of the trial's graph (0 or BFS_LOAD_DEGREE_ORDER) */
 } bfs_tune_trial;
 
 typedef struct bfs_tune_result {
@@ -315,6 +324,8 @@ typedef struct bfs_tune_result {
 	double default_batch_gteps;
 	uint32_t num_trials;
 	uint32_t from_cache;                  /* 1: read from the cache file, nothing measured */
+	uint32_t load_flags;                  /* the best layout (0 or BFS_LOAD_DEGREE_ORDER; bfs_autotune) */
+	uint32_t reserved;
 	bfs_tune_trial trials[BFS_TUNE_MAX_TRIALS];
 } bfs_tune_result;
 

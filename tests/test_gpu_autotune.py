@@ -73,3 +73,37 @@ def test_autotune_default_widths_from_tile_size_range(native, oracle):
         expect.add(w)
         w *= 2
     assert widths == expect and r["tile_width"] in expect
+
+
+@pytest.mark.parametrize("device_build", [False, True])
+def test_degree_ordered_layout_keeps_callers_ids(native, oracle, device_build):
+    """BFS_LOAD_DEGREE_ORDER (tools/vertex_id_reorder_to_degrees' layout with
+    this library's tie-break): sources, levels, parents and out-degrees stay in
+    the caller's ids, bit-exact against the oracle on the original graph, in
+    both execution modes; the batched, betweenness and save paths refuse it."""
+    import bfs_simd_benchmarks_gb300 as B
+    n = 20000
+    src, dst = B.gen_rmat(n, 12 * n, seed=515, permute=True)
+    arr = oracle.arrays_from_edges(n, src, dst, 256, 8)
+    with B.Graph.from_edges(n, src, dst, 256, 8, device_build=device_build, degree_order=True) as g:
+        np.testing.assert_array_equal(g.degrees(), arr["degrees"])
+        for mode in ("persistent", "stepwise"):
+            g.set_options(mode=mode)
+            for s in B.pick_sources(arr["degrees"], 4, seed=3):
+                lev, par, st = g.run(int(s))
+                np.testing.assert_array_equal(lev, oracle.bfs_levels(arr, int(s)))
+                assert oracle.check_parents(arr, int(s), lev, par) == 0
+        for call in (lambda: g.run_batch([0, 1, 2, 3, 4, 5]), lambda: g.bc(0)):
+            with pytest.raises(B.BfsError) as e:
+                call()
+            assert e.value.status == 8
+
+
+def test_autotune_searches_layouts(native, oracle):
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 14
+    src, dst = B.gen_rmat(n, 16 * n, seed=516, permute=True)
+    srcs = B.pick_sources(np.bincount(src, minlength=n), 4, seed=1)
+    r = B.autotune(n, src, dst, srcs, tile_widths=(512,), stripe_lengths=(8,), device_build=True, layouts=True)
+    assert {t["load_flags"] for t in r["trials"]} == {0, B._native.BFS_LOAD_DEGREE_ORDER}
+    assert r["load_flags"] in (0, B._native.BFS_LOAD_DEGREE_ORDER)
