@@ -51,7 +51,10 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", default="pokec")
     ap.add_argument("--mode", choices=["persistent", "stepwise"], default="persistent")
-    ap.add_argument("--bottom-up", choices=["pull", "stream"], default="pull")
+    ap.add_argument("--bottom-up", choices=["pull", "stream"], default=None,
+                    help="bottom-up variant (default: the autotuner's choice, pull without tuning)")
+    ap.add_argument("--no-shape-search", action="store_true",
+                    help="keep the workload's tile width / stripe length / layout (skip bfs_autotune)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sources", type=int, default=0, help="use only the first K sources (profiling runs)")
@@ -730,16 +733,43 @@ def main():
     B.load_library(build_if_missing=True)
     t_gen = time.perf_counter()
     src, dst = wl.edges()
-    g = B.Graph.from_edges(wl.n, src, dst, wl.w, wl.s, device_build=wl.m >= DEVICE_BUILD_EDGES)
-    g.set_options(mode=args.mode, bottom_up=args.bottom_up)
-    info = g.info()
     t_gen = time.perf_counter() - t_gen
-    degrees = g.degrees()
+    degrees = np.bincount(src, minlength=wl.n).astype(np.uint32)  # out-degrees, as Graph.degrees()
     sources = wl.sources(degrees)
     if args.sources:
         sources = sources[: args.sources]
     n = wl.n
-    sw = wl.s * wl.w
+    # layout search (bfs_autotune): tile width over the tile-size computer's
+    # range x stripe length {8, 16, 32} x {caller ids, degree order}, each
+    # layout built on the GPU and its options tuned on 16 of the sources
+    W, S, degree_order, shape_tune, shape_opts = wl.w, wl.s, False, None, None
+    if not args.no_tune and not args.no_shape_search and args.mode == "persistent":
+        t_t = time.perf_counter()
+        r = B.autotune(wl.n, src, dst, sources[:16], tile_widths=None, stripe_lengths=(8, 16, 32),
+                       device_build=True, layouts=True)
+        W, S = r["tile_width"], r["stripe_length"]
+        degree_order = r["load_flags"] == N.BFS_LOAD_DEGREE_ORDER
+        shape_opts = {k: v for k, v in r["options"].items() if k not in ("wait_limit_us", "test_hold_barrier")}
+        best = {}
+        for t in r["trials"]:
+            key = (t["tile_width"], t["stripe_length"], "degree order" if t["load_flags"] else "caller ids")
+            best[key] = max(best.get(key, 0.0), t["gteps"])
+        shape_tune = {"tile_width": W, "stripe_length": S,
+                      "layout": "degree order" if degree_order else "caller ids",
+                      "threads_per_cta": 512,  # the kernels' compile-time block size
+                      "ctas_per_sm": shape_opts["ctas_per_sm"] or "max (2)",
+                      "gteps_kernel_16_sources": r["single_gteps"],
+                      "layouts_tried": [{"tile_width": k[0], "stripe_length": k[1], "layout": k[2], "best_gteps": v}
+                                        for k, v in sorted(best.items())],
+                      "seconds": round(time.perf_counter() - t_t, 2)}
+    t_b = time.perf_counter()
+    g = B.Graph.from_edges(wl.n, src, dst, W, S, device_build=True, degree_order=degree_order)
+    if shape_opts:
+        g.set_options(**shape_opts)
+    g.set_options(mode=args.mode, **({"bottom_up": args.bottom_up} if args.bottom_up else {}))
+    info = g.info()
+    t_gen += time.perf_counter() - t_b
+    sw = S * W
     tuned = None
     if not args.no_tune and args.mode == "persistent":
         t_t = time.perf_counter()
@@ -794,7 +824,8 @@ def main():
     value = edges_all / (total_ms_max / 1e3) / 1e9
 
     # roofline of the traversal kernel (k_bfs_persistent), per launch
-    alg = [algorithmic_bytes(st, n, sw, args.bottom_up == "pull") for _, _, st in timed]
+    pull = g.get_options()["bottom_up"] == N.BFS_BU_PULL
+    alg = [algorithmic_bytes(st, n, sw, pull) for _, _, st in timed]
     achieved = statistics.mean(alg) / (statistics.mean(kern_ms) / 1e3) / 1e9
     peak, peak_kind = peaks()
     traffic = ncu_traffic(args.workload)
@@ -838,7 +869,11 @@ def main():
         if not args.no_cpu_baseline:
             from oracle import oracle as O
             bc_arr = O.csr_arrays(wl.n, src, dst)
-        bc = bench_bc(args, torch, dev, g, sources, flush, bc_arr)
+        # betweenness runs on the caller's ids (a degree-ordered layout refuses it)
+        bc_g = B.Graph.from_edges(wl.n, src, dst, W, S, device_build=True) if degree_order else g
+        bc = bench_bc(args, torch, dev, bc_g, sources, flush, bc_arr)
+        if bc_g is not g:
+            bc_g.close()
     if args.large != "none" and world == 1:
         large = bench_large(args, torch, dev)
     if rank == 0:
@@ -850,7 +885,9 @@ def main():
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded R-MAT stand-in, see config)",
             "config": bench_config(wl, len(sources)),
             "parallelism": "replicas" if world > 1 else "single GPU",
-            "gpu_config": {"mode": args.mode, "bottom_up": args.bottom_up,
+            "gpu_config": {"mode": args.mode, "bottom_up": "pull" if pull else "stream",
+                           "tile_width": W, "stripe_length": S, "layout": "degree order" if degree_order else "caller ids",
+                           "layout_search": shape_tune,
                            "graph_device_bytes": info["device_bytes"], "grid_ctas": timed[0][2]["grid_ctas"],
                            "column_groups": info["num_groups"], "autotune": tuned,
                            "graph_build_s": round(t_gen, 2)},

@@ -141,6 +141,11 @@ class Graph:
         N.check(N.load().bfs_get_options(self._h, C.byref(o)), "bfs_get_options")
         return {k: getattr(o, k) for k, _ in N.Options._fields_}
 
+    def get_options(self) -> dict:
+        o = N.Options()
+        N.check(N.load().bfs_get_options(self._h, C.byref(o)), "bfs_get_options")
+        return {k: getattr(o, k) for k, _ in N.Options._fields_}
+
     def set_options(self, **kw) -> None:
         o = N.Options()
         lib = N.load()
