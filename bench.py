@@ -55,6 +55,10 @@ def parse():
                     help="bottom-up variant (default: the autotuner's choice, pull without tuning)")
     ap.add_argument("--no-shape-search", action="store_true",
                     help="keep the workload's tile width / stripe length / layout (skip bfs_autotune)")
+    ap.add_argument("--tile-width", type=int, default=0, help="with --no-tune: this tile width (profiling runs)")
+    ap.add_argument("--stripe-length", type=int, default=0, help="with --no-tune: this stripe length")
+    ap.add_argument("--degree-order", action="store_true", help="with --no-tune: the degree-ordered layout")
+    ap.add_argument("--options", default="", help="with --no-tune: traversal options as JSON (profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sources", type=int, default=0, help="use only the first K sources (profiling runs)")
@@ -90,15 +94,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(workload: str):
-    """Per-launch DRAM bytes of the traversal kernel from the committed ncu summary, if any."""
+def ncu_traffic(workload: str, key: str = "dram_bytes_per_launch"):
+    """DRAM bytes per launch (or per batch) from the committed ncu summaries, if any."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
     ent = d.get(workload)
-    return None if ent is None else ent.get("dram_bytes_per_launch")
+    return None if ent is None else ent.get(key)
 
 
 class ClockSampler:
@@ -418,7 +422,10 @@ def bench_batched(args, torch, dev, graph=None, build_s=0.0, edges=None):
         "cuda_graph": cuda_graph,
         "autotune": tuned,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "kernels": "k_ms_bfs + k_ms_emit", "peak_kind": peak_kind, "algorithmic_bytes_per_batch": alg},
+                     "kernels": "k_ms_bfs + k_ms_emit", "peak_kind": peak_kind, "algorithmic_bytes_per_batch": alg,
+                     "traffic": ncu_traffic(args.batch_workload, "dram_bytes_per_batch"),
+                     "traffic_note": "per batch; from the R-MAT scale 18 capture scaled x16 "
+                                     "(profiles/k_ms_bfs_emit_rmat18_4096src.md)"},
         "parity": f"batched rows bit-exact to the oracle's levels (oracle/bfs_oracle.c orc_bfs_levels) on "
                   f"{rows_ok}/{len(check)} sampled sources",
         "steps": len(ms), "l2": "flushed (256 MiB write) before every batch; batch state far above L2",
@@ -742,7 +749,8 @@ def main():
     # layout search (bfs_autotune): tile width over the tile-size computer's
     # range x stripe length {8, 16, 32} x {caller ids, degree order}, each
     # layout built on the GPU and its options tuned on 16 of the sources
-    W, S, degree_order, shape_tune, shape_opts = wl.w, wl.s, False, None, None
+    W, S, degree_order, shape_tune = args.tile_width or wl.w, args.stripe_length or wl.s, args.degree_order, None
+    shape_opts = json.loads(args.options) if args.options else None
     if not args.no_tune and not args.no_shape_search and args.mode == "persistent":
         t_t = time.perf_counter()
         r = B.autotune(wl.n, src, dst, sources[:16], tile_widths=None, stripe_lengths=(8, 16, 32),
