@@ -173,13 +173,15 @@ __device__ __forceinline__ uint64_t row_mask(uint64_t n0, uint64_t n1) {
 // After a push level: the OR'ed words lose the bits already visited, the rest
 // are new, go into vis and put v into the next frontier.  A warp takes 32
 // vertices, then works through the touched ones together (K words each).
-__device__ void ms_push_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, uint64_t *actn, unsigned long long &actdeg) {
+__device__ void ms_push_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, uint64_t *actn, unsigned long long &actdeg,
+		unsigned long long *s_act) {
 	const uint32_t K = a.K;
 	const unsigned lane = lane_id();
 	uint32_t *qn = a.queue[(lvl + 1) & 1];
 	MsCounters *cn = &a.ctl->ctr[(lvl + 1) % 3];
 	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
 	const uint32_t nwarps = gridDim.x * kMsWarps;
+	uint64_t newacc[2] = {0ull, 0ull};
 	for (uint32_t vb = gwarp * 32; vb < a.n; vb += nwarps * 32) {
 		const uint32_t v = vb + lane;
 		const bool t = v < a.n && ld_cg_u8(a.touched + v);
@@ -198,6 +200,7 @@ __device__ void ms_push_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, uin
 				nw[h] = w & ~vv;
 				if (nw[h] != w) nxt[row + k] = nw[h];
 				if (nw[h]) a.vis[row + k] = vv | nw[h];
+				newacc[h] |= nw[h];
 			}
 			const uint64_t mask = row_mask(nw[0], nw[1]);
 			if (lane == 0) actn[vb + j] = mask;
@@ -210,6 +213,8 @@ __device__ void ms_push_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, uin
 		ms_append(a, cn, qn, v, any && d <= kMsBig, any && d > kMsBig);
 		actdeg += d;
 	}
+	if (lane < a.K && newacc[0]) atomicOr(s_act + lane, (unsigned long long) newacc[0]);
+	if (lane + 32 < a.K && newacc[1]) atomicOr(s_act + lane + 32, (unsigned long long) newacc[1]);
 }
 
 // Pull appends: small vertices go through a per-warp shared buffer (one
@@ -229,10 +234,15 @@ __device__ __forceinline__ void ms_wq_flush(MsCounters *cn, uint32_t *qn, uint32
 // The bits a complete word of lane's word (lane + 32 * h) holds.
 struct FullMask {
 	uint64_t f0, f1;
-	__device__ __forceinline__ FullMask(const MsArgs &a, unsigned lane) {
+	// `act` (may be null: every source): the level's active words
+	__device__ __forceinline__ FullMask(const MsArgs &a, unsigned lane, const unsigned long long *act = nullptr) {
 		const uint64_t last = a.last_bits == 64 ? ~0ull : ((1ull << a.last_bits) - 1);
 		f0 = lane < a.K ? (lane == a.K - 1 ? last : ~0ull) : 0ull;
 		f1 = lane + 32 < a.K ? (lane + 32 == a.K - 1 ? last : ~0ull) : 0ull;
+		if (act) {
+			if (lane < a.K) f0 &= ld_cg64((const uint64_t *) act + lane);
+			if (lane + 32 < a.K) f1 &= ld_cg64((const uint64_t *) act + lane + 32);
+		}
 	}
 	__device__ __forceinline__ bool complete(uint64_t x0, uint64_t x1) const {
 		return __all_sync(kFull, (x0 & f0) == f0 && (x1 & f1) == f1);
@@ -375,10 +385,11 @@ __device__ __forceinline__ void ms_gather_edges(const MsArgs &a, const uint64_t 
 // `mine` false only take part in the warp-wide appends.
 __device__ __forceinline__ void ms_pull_lane(const MsArgs &a, const uint64_t *cur, const uint64_t *actc,
 		uint64_t *nxt, uint64_t *actn, uint32_t v, uint32_t beg, uint32_t end, bool mine, unsigned long long &actdeg,
-		unsigned long long &gathered, MsCounters *cn, uint32_t *qn) {
+		unsigned long long &gathered, MsCounters *cn, uint32_t *qn, uint64_t act0, uint64_t act1, uint64_t &new0,
+		uint64_t &new1) {
 	const uint32_t K = a.K;
 	const uint64_t last = a.last_bits == 64 ? ~0ull : ((1ull << a.last_bits) - 1);
-	const uint64_t f0 = K == 1 ? last : ~0ull, f1 = K == 2 ? last : 0ull;
+	const uint64_t f0 = (K == 1 ? last : ~0ull) & act0, f1 = (K == 2 ? last : 0ull) & act1;
 	uint64_t vis0 = 0, vis1 = 0, acc0 = 0, acc1 = 0;
 	bool any = false;
 	uint32_t d = 0;
@@ -407,6 +418,8 @@ __device__ __forceinline__ void ms_pull_lane(const MsArgs &a, const uint64_t *cu
 			for (int t = 0; t < 4; ++t) { acc0 |= g0[t]; acc1 |= g1[t]; }
 		}
 		const uint64_t w0 = acc0 & ~vis0 & f0, w1 = acc1 & ~vis1 & f1;
+		new0 |= w0;
+		new1 |= w1;
 		nxt[row] = w0;
 		if (w0) a.vis[row] = vis0 | w0;
 		if (K == 2) {
@@ -431,7 +444,8 @@ __device__ __forceinline__ void ms_pull_lane(const MsArgs &a, const uint64_t *cu
 // time: lane l owns words l and l + 32.  The rows of many-in-edge
 // destinations are cleared here and filled by ms_pull_chunks.
 __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, const uint64_t *actc, uint64_t *nxt,
-		uint64_t *actn, unsigned long long &actdeg, unsigned long long &gathered, uint32_t *wq_base) {
+		uint64_t *actn, unsigned long long &actdeg, unsigned long long &gathered, uint32_t *wq_base,
+		const unsigned long long *act, unsigned long long *s_act) {
 	const uint32_t K = a.K;
 	uint32_t *qn = a.queue[(lvl + 1) & 1];
 	MsCounters *cn = &a.ctl->ctr[(lvl + 1) % 3];
@@ -439,7 +453,11 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, cons
 	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
 	const uint32_t nwarps = gridDim.x * kMsWarps;
 	const bool w0 = lane < K, w1 = lane + 32 < K;
-	const FullMask fm(a, lane);
+	const FullMask fm(a, lane, act);
+	const uint64_t lact0 = act ? ld_cg64((const uint64_t *) act) : ~0ull;
+	const uint64_t lact1 = act && K > 1 ? ld_cg64((const uint64_t *) act + 1) : ~0ull;
+	uint64_t new_lane0 = 0, new_lane1 = 0;  // new words lane / lane + 32 (warp-per-destination paths)
+	uint64_t new_w0 = 0, new_w1 = 0;        // new words 0 / 1 (lane-per-destination path)
 	uint32_t *wbuf = wq_base + warp_id() * kMsWq;
 	uint32_t wn = 0;
 	// blocks of 32 destinations in a hashed order: in-degree follows the id
@@ -468,7 +486,8 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, cons
 		if (K <= kLaneMaxWords) {
 			const bool mine = needy && lend - lbeg <= kLaneMaxDeg;
 			warpm &= ~__ballot_sync(kFull, mine);
-			ms_pull_lane(a, cur, actc, nxt, actn, vl, lbeg, lend, mine, actdeg, gathered, cn, qn);
+			ms_pull_lane(a, cur, actc, nxt, actn, vl, lbeg, lend, mine, actdeg, gathered, cn, qn, lact0, lact1, new_w0,
+					new_w1);
 		}
 		for (uint32_t m = warpm; m; m &= m - 1) {
 			const int jj = __ffs(m) - 1;
@@ -494,6 +513,8 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, cons
 				ms_gather(a, cur, actc, beg, end, fm, vis0, vis1, acc0, acc1, gathered);
 			}
 			const uint64_t n0 = acc0 & ~vis0 & fm.f0, n1 = acc1 & ~vis1 & fm.f1;
+			new_lane0 |= n0;
+			new_lane1 |= n1;
 			if (w0) { nxt[row + lane] = n0; if (n0) a.vis[row + lane] = vis0 | n0; }
 			if (w1) { nxt[row + lane + 32] = n1; if (n1) a.vis[row + lane + 32] = vis1 | n1; }
 			const uint64_t mask = row_mask(n0, n1);
@@ -515,18 +536,22 @@ __device__ void ms_pull(const MsArgs &a, uint32_t lvl, const uint64_t *cur, cons
 		}
 	}
 	ms_wq_flush(cn, qn, wbuf, wn);
+	if (w0 && new_lane0) atomicOr(s_act + lane, (unsigned long long) new_lane0);
+	if (w1 && new_lane1) atomicOr(s_act + lane + 32, (unsigned long long) new_lane1);
+	if (new_w0) atomicOr(s_act, (unsigned long long) new_w0);
+	if (new_w1) atomicOr(s_act + 1, (unsigned long long) new_w1);
 }
 
 // Pull, destinations with many in-edges: warps take chunks of kMsChunk
 // in-edges over the whole grid and OR what they gather into the row.
 __device__ void ms_pull_chunks(const MsArgs &a, const uint64_t *cur, const uint64_t *actc, uint64_t *nxt,
-		unsigned long long &gathered) {
+		unsigned long long &gathered, const unsigned long long *act) {
 	const uint32_t K = a.K;
 	const unsigned lane = lane_id();
 	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
 	const uint32_t nwarps = gridDim.x * kMsWarps;
 	const bool w0 = lane < K, w1 = lane + 32 < K;
-	const FullMask fm(a, lane);
+	const FullMask fm(a, lane, act);
 	for (uint32_t c = gwarp; c < a.nchunks; c += nwarps) {
 		const uint32_t v = __ldg(a.chunk_v + c), beg = __ldg(a.chunk_beg + c);
 		const uint32_t end = min(beg + kMsChunk, __ldg(a.in_off + v + 1));
@@ -558,7 +583,7 @@ __device__ void ms_pull_chunks(const MsArgs &a, const uint64_t *cur, const uint6
 // After ms_pull_chunks: the many-in-edge destinations' rows hold their new
 // bits; update vis, the frontier mask and the queue.
 __device__ void ms_pull_chunks_finish(const MsArgs &a, uint32_t lvl, uint64_t *nxt, uint64_t *actn,
-		unsigned long long &actdeg) {
+		unsigned long long &actdeg, unsigned long long *s_act) {
 	const uint32_t K = a.K;
 	uint32_t *qn = a.queue[(lvl + 1) & 1];
 	MsCounters *cn = &a.ctl->ctr[(lvl + 1) % 3];
@@ -566,6 +591,7 @@ __device__ void ms_pull_chunks_finish(const MsArgs &a, uint32_t lvl, uint64_t *n
 	const uint32_t gwarp = blockIdx.x * kMsWarps + warp_id();
 	const uint32_t nwarps = gridDim.x * kMsWarps;
 	const bool w0 = lane < K, w1 = lane + 32 < K;
+	uint64_t new0 = 0, new1 = 0;
 	for (uint32_t j = gwarp; j < a.nbig_in; j += nwarps) {
 		const uint32_t v = __ldg(a.in_big + j);
 		const size_t row = (size_t) v * K;
@@ -578,6 +604,8 @@ __device__ void ms_pull_chunks_finish(const MsArgs &a, uint32_t lvl, uint64_t *n
 			n1 = ld_cg64(nxt + row + lane + 32);
 			if (n1) a.vis[row + lane + 32] = ld_cg64(a.vis + row + lane + 32) | n1;
 		}
+		new0 |= n0;
+		new1 |= n1;
 		const uint64_t mask = row_mask(n0, n1);
 		if (lane == 0) {
 			actn[v] = mask;
@@ -589,6 +617,8 @@ __device__ void ms_pull_chunks_finish(const MsArgs &a, uint32_t lvl, uint64_t *n
 			}
 		}
 	}
+	if (w0 && new0) atomicOr(s_act + lane, (unsigned long long) new0);
+	if (w1 && new1) atomicOr(s_act + lane + 32, (unsigned long long) new1);
 }
 
 // Planes [first, last] (levels base + p) -> uint8 levels [source][vertex].
@@ -751,6 +781,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 	unsigned long long gathered = 0;
 	uint32_t base = 0, lvl = 0;
 	bool complete = false;
+	__shared__ unsigned long long s_act[64];  // this CTA's OR of the next frontier's words
 	for (; ok; ++lvl) {
 		MsCounters *cc = &ctl->ctr[lvl % 3];
 		const uint32_t nq = ld_volatile(&cc->nact), nb = ld_volatile(&cc->nbig);
@@ -783,7 +814,12 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 			c2->nact = 0;
 			c2->nbig = 0;
 			c2->act_deg = 0;
+			for (uint32_t k = 0; k < a.K; ++k) ctl->active[(lvl + 2) % 3][k] = 0;
 		}
+		if (threadIdx.x < 64) s_act[threadIdx.x] = 0;
+		__syncthreads();
+		// the sources with a frontier at this level (level 0: every source)
+		const unsigned long long *act = lvl == 0 ? nullptr : ctl->active[lvl % 3];
 		const uint64_t *cur = a.hist + (size_t) (lvl - base) * nK;
 		uint64_t *nxt = a.hist + (size_t) (lvl + 1 - base) * nK;
 		const uint64_t *actc = a.pmask + (size_t) (lvl - base) * a.n;
@@ -799,16 +835,16 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 			ms_push(a, lvl, cur, actc, nxt, nq, nb);
 			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 			if (leader && tph) tph[1] = global_timer_ns();
-			ms_push_finish(a, lvl, nxt, actn, actdeg);
+			ms_push_finish(a, lvl, nxt, actn, actdeg, s_act);
 		} else {
-			ms_pull(a, lvl, cur, actc, nxt, actn, actdeg, gathered, wq);
+			ms_pull(a, lvl, cur, actc, nxt, actn, actdeg, gathered, wq, act, s_act);
 			if (a.nbig_in) {
 				if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 				if (leader && tph) tph[0] = global_timer_ns();
-				ms_pull_chunks(a, cur, actc, nxt, gathered);
+				ms_pull_chunks(a, cur, actc, nxt, gathered, act);
 				if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 				if (leader && tph) tph[1] = global_timer_ns();
-				ms_pull_chunks_finish(a, lvl, nxt, actn, actdeg);
+				ms_pull_chunks_finish(a, lvl, nxt, actn, actdeg, s_act);
 			}
 		}
 		// the next frontier's out-degree: per-CTA sum, one atomic per CTA
@@ -824,6 +860,9 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 				if (push) ctl->stats.push_levels++;
 			}
 		}
+		// the next level's active sources: this CTA's share
+		if (threadIdx.x < a.K && s_act[threadIdx.x])
+			atomicOr(&ctl->active[(lvl + 1) % 3][threadIdx.x], s_act[threadIdx.x]);
 		__syncthreads();
 		ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
 	}

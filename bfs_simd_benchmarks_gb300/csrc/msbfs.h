@@ -44,6 +44,10 @@ struct MsControl {
 	unsigned push_chunks;  // push level: 1024-edge chunks of its high-degree frontier vertices
 	MsCounters ctr[3];
 	MsStats stats;
+	// active[l % 3][k]: OR of word k over level l's frontier rows -- the
+	// sources that still have a frontier; only they can reach a vertex at
+	// level l, so the pulls' completion tests ignore the others
+	unsigned long long active[3][64];
 };
 
 struct MsArgs {
