@@ -83,10 +83,12 @@ class Options(C.Structure):
         ("bu_alpha", C.c_uint32),
         ("td_beta", C.c_uint32),
         ("ctas_per_sm", C.c_uint32),
+        ("bc_batch", C.c_uint32),
     ]
 
 
 BFS_BC_TRACE_LEVELS = 64
+BFS_BC_BATCH_MAX_SOURCES = 64
 
 
 class BcStats(C.Structure):
@@ -109,10 +111,17 @@ class BcStats(C.Structure):
         ("level_vertices", C.c_uint32 * BFS_BC_TRACE_LEVELS),
         ("level_big", C.c_uint32 * BFS_BC_TRACE_LEVELS),
         ("level_medium", C.c_uint32 * BFS_BC_TRACE_LEVELS),
+        ("batched_sources", C.c_uint32),
+        ("fallback_sources", C.c_uint32),
+        ("edges_matched_forward", C.c_uint64),
+        ("edges_matched_reverse", C.c_uint64),
+        ("source_reached", C.c_uint32 * BFS_BC_BATCH_MAX_SOURCES),
     ]
 
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("level_")}
+        d = {k: getattr(self, k) for k, _ in self._fields_
+             if not k.startswith("level_") and k != "source_reached"}
+        d["source_reached"] = list(self.source_reached[:min(self.num_sources, BFS_BC_BATCH_MAX_SOURCES)])
         k = min(self.depth + 1, BFS_BC_TRACE_LEVELS)
         for name in ("level_paths_ms", "level_dependencies_ms"):
             d[name] = [round(x, 4) for x in getattr(self, name)[:k]]
@@ -325,6 +334,8 @@ _SIGNATURES = [
     ("bfs_bc_run", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(BcStats)]),
     ("bfs_bc_run_device", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("bfs_bc_last_stats", C.c_int, [C.c_void_p, C.POINTER(BcStats)]),
+    ("bfs_bc_run_batch", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(BcStats)]),
+    ("bfs_bc_run_batch_device", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("bfs_bc_accumulate", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_void_p, C.POINTER(BcStats)]),
     ("bfs_bc_accumulate_device", C.c_int, [C.c_void_p, _u32p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("bfs_run_batch_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),

@@ -18,7 +18,7 @@ LIB_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIB_DIR, "libbfs_gb300.so")
 CLI = os.path.join(LIB_DIR, "bfs")
 
-SOURCES = ["api.cu", "bfs_kernels.cu", "bfs_noalloc.cu", "msbfs.cu", "bc.cu", "build_device.cu", "rmat_device.cu", "server.cpp", "autotune.cpp", "host_io.cpp", "layout.cpp", "rmat.cpp"]
+SOURCES = ["api.cu", "bfs_kernels.cu", "bfs_noalloc.cu", "msbfs.cu", "bc.cu", "bc_batch.cu", "build_device.cu", "rmat_device.cu", "server.cpp", "autotune.cpp", "host_io.cpp", "layout.cpp", "rmat.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

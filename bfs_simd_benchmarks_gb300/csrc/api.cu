@@ -12,6 +12,7 @@
 #include "internal.h"
 #include "kernels_api.h"
 #include "bc.h"
+#include "bc_batch.h"
 #include "msbfs.h"
 
 using namespace bfsg;
@@ -105,6 +106,27 @@ struct bfs_graph {
 		size_t bytes = 0;
 		std::vector<DevBuf> bufs;
 	} bc;
+	// batched betweenness state, allocated by the first batched bfs_bc_* call
+	struct BcBatch {
+		uint32_t *sigma = nullptr, *partial = nullptr, *d_sources = nullptr;
+		float *dsum = nullptr;
+		float *delta = nullptr;      // [64][n] staging of host outputs (allocated when first asked for)
+		uint32_t *paths = nullptr;
+		BbControl *ctl = nullptr;
+		BbControl *h_ctl = nullptr;  // pinned
+		MsControl *h_ms = nullptr;   // pinned: the traversal's control block
+		cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
+		cudaStream_t stream = nullptr;
+		uint32_t ns = 0;
+		int grid = 0;
+		size_t bytes = 0;
+		std::vector<DevBuf> bufs;
+	} bb;
+	// out-edge chunks of vertices with many out-edges (batched betweenness)
+	const uint32_t *bb_ochunk_v = nullptr, *bb_ochunk_beg = nullptr;
+	uint32_t bb_noch = 0;
+	bool bb_chunks_ready = false;
+	bool bc_last_batched = false;    // bfs_bc_last_stats describes a batched run
 	std::mutex mu;
 };
 
@@ -195,9 +217,21 @@ void release_bc(bfs_graph *g) {
 	b = bfs_graph::Bc{};
 }
 
+void release_bb(bfs_graph *g) {
+	auto &b = g->bb;
+	for (auto &x : b.bufs) cudaFree(x.p);
+	b.bufs.clear();
+	if (b.h_ctl) cudaFreeHost(b.h_ctl);
+	if (b.h_ms) cudaFreeHost(b.h_ms);
+	for (cudaEvent_t e : {b.e0, b.e1, b.e2, b.e3})
+		if (e) cudaEventDestroy(e);
+	b = bfs_graph::BcBatch{};
+}
+
 void release(bfs_graph *g) {
 	release_batch(g);
 	release_bc(g);
+	release_bb(g);
 	if (g->mb.h_ctl) cudaFreeHost(g->mb.h_ctl);
 	if (g->mb.e0) cudaEventDestroy(g->mb.e0);
 	if (g->mb.e1) cudaEventDestroy(g->mb.e1);
@@ -232,6 +266,7 @@ void default_options(bfs_options *o) {
 	o->bu_alpha = 14;
 	o->td_beta = 24;
 	o->ctas_per_sm = 0;
+	o->bc_batch = 1;
 }
 
 int device_setup(bfs_graph *g) {
@@ -836,6 +871,31 @@ __global__ void __launch_bounds__(512) k_levels_u8(const int32_t *lev, uint8_t *
 	}
 }
 
+// The batched traversal's arguments: K words per vertex, ns sources, `planes`
+// level planes (the buffers batch_prepare made).
+MsArgs batch_args(const bfs_graph *g, uint32_t K, uint32_t ns, uint32_t planes) {
+	MsArgs a = g->mb.args;
+	a.n = g->n;
+	a.m = (uint32_t) g->m;
+	a.K = K;
+	a.last_bits = ns - 64 * (K - 1);
+	a.planes = planes;
+	a.push_div = std::max<uint32_t>(1, g->opt.batch_push_div);
+	a.wait_limit_ns = wait_limit_ns(g->opt);
+	a.hold_barrier = g->opt.test_hold_barrier;
+	a.ctas_per_sm = g->opt.ctas_per_sm;
+	a.row_off = g->dg.row_off;
+	a.col = g->dg.col;
+	a.in_off = g->dg.in_off;
+	a.in_src = g->dg.in_src;
+	a.in_big = g->ms_in_big;
+	a.chunk_v = g->ms_chunk_v;
+	a.chunk_beg = g->ms_chunk_beg;
+	a.nbig_in = g->ms_nbig_in;
+	a.nchunks = g->ms_nchunks;
+	return a;
+}
+
 bool stream_capturing(cudaStream_t st) {
 	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
 	return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
@@ -855,25 +915,7 @@ int run_batch_impl(bfs_graph *g, const uint32_t *sources, uint32_t ns, uint8_t *
 	int rc = batch_prepare(g, K, &planes);
 	if (rc) return rc;
 	auto &b = g->mb;
-	MsArgs a = b.args;
-	a.n = g->n;
-	a.m = (uint32_t) g->m;
-	a.K = K;
-	a.last_bits = ns - 64 * (K - 1);
-	a.planes = planes;
-	a.push_div = std::max<uint32_t>(1, g->opt.batch_push_div);
-	a.wait_limit_ns = wait_limit_ns(g->opt);
-	a.hold_barrier = g->opt.test_hold_barrier;
-	a.ctas_per_sm = g->opt.ctas_per_sm;
-	a.row_off = g->dg.row_off;
-	a.col = g->dg.col;
-	a.in_off = g->dg.in_off;
-	a.in_src = g->dg.in_src;
-	a.in_big = g->ms_in_big;
-	a.chunk_v = g->ms_chunk_v;
-	a.chunk_beg = g->ms_chunk_beg;
-	a.nbig_in = g->ms_nbig_in;
-	a.nchunks = g->ms_nchunks;
+	MsArgs a = batch_args(g, K, ns, planes);
 	const bool capturing = dev_sources && stream_capturing(st);
 	if (!capturing && cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
 	const bool singles = !dev_sources && ns <= g->opt.batch_single_max && g->opt.mode == BFS_MODE_PERSISTENT;
@@ -1069,6 +1111,7 @@ int bc_enqueue(bfs_graph *g, uint32_t source, uint32_t *sigma, float *delta, flo
 	if ((rc = bc_launch(a, g->num_sms, st, &b.grid))) return rc;
 	if (cudaEventRecord(b.e2, st) != cudaSuccess) return BFS_ECUDA;
 	b.stream = st;
+	g->bc_last_batched = false;
 	// the traversal's own statistics and events were not recorded
 	g->have_run = false;
 	return BFS_OK;
@@ -1115,6 +1158,200 @@ int bc_collect(bfs_graph *g, bfs_bc_stats *out) {
 		*out = s;
 	}
 	return c.err;
+}
+
+// ---- batched betweenness ----------------------------------------------------
+template <class T> int bb_alloc(bfs_graph *g, T **out, size_t count) {
+	size_t bytes = std::max<size_t>(sizeof(T) * count, 16);
+	void *p = nullptr;
+	if (cudaMalloc(&p, bytes) != cudaSuccess) {
+		cudaGetLastError();
+		return BFS_ENOMEM;
+	}
+	g->bb.bufs.push_back({p, bytes});
+	g->bb.bytes += bytes;
+	*out = (T *) p;
+	return BFS_OK;
+}
+
+// Out-edge chunks (once per graph), the per-(vertex, source) state, and
+// (host_out) the [64][n] staging of host outputs.
+int bb_prepare(bfs_graph *g, bool host_deps, bool host_paths) {
+	int rc;
+	if (!g->bb_chunks_ready) {
+		std::vector<uint32_t> off((size_t) g->n + 1);
+		if (cudaMemcpy(off.data(), g->dg.row_off, sizeof(uint32_t) * off.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+			return BFS_ECUDA;
+		std::vector<uint32_t> cv, cb;
+		for (uint32_t v = 0; v < g->n; ++v) {
+			if (off[v + 1] - off[v] <= kBbBig) continue;
+			for (uint32_t e = off[v]; e < off[v + 1]; e += kBbChunk) {
+				cv.push_back(v);
+				cb.push_back(e);
+			}
+		}
+		g->bb_noch = (uint32_t) cv.size();
+		if ((rc = dev_upload(g, &g->bb_ochunk_v, cv)) || (rc = dev_upload(g, &g->bb_ochunk_beg, cb))) return rc;
+		g->bb_chunks_ready = true;
+	}
+	auto &b = g->bb;
+	if (!b.ctl) {
+		const size_t rows = (size_t) g->n * kBbMaxSources;
+		const size_t part = (size_t) std::max(g->ms_nchunks, g->bb_noch) * kBbMaxSources;
+		if ((rc = bb_alloc(g, &b.sigma, rows)) || (rc = bb_alloc(g, &b.dsum, rows)) ||
+				(rc = bb_alloc(g, &b.partial, part)) || (rc = bb_alloc(g, &b.ctl, 1)) ||
+				(rc = bb_alloc(g, &b.d_sources, kBbMaxSources))) {
+			release_bb(g);
+			return rc;
+		}
+		if (cudaMallocHost(&b.h_ctl, sizeof(BbControl)) != cudaSuccess ||
+				cudaMallocHost(&b.h_ms, sizeof(MsControl)) != cudaSuccess || cudaEventCreate(&b.e0) != cudaSuccess ||
+				cudaEventCreate(&b.e1) != cudaSuccess || cudaEventCreate(&b.e2) != cudaSuccess ||
+				cudaEventCreate(&b.e3) != cudaSuccess) {
+			cudaGetLastError();
+			release_bb(g);
+			return BFS_ENOMEM;
+		}
+	}
+	const size_t stage = (size_t) g->n * kBbMaxSources;
+	if (host_deps && !b.delta && (rc = bb_alloc(g, &b.delta, stage))) return rc;
+	if (host_paths && !b.paths && (rc = bb_alloc(g, &b.paths, stage))) return rc;
+	return BFS_OK;
+}
+
+// Enqueues the batched traversal from `sources` (host, ns <= 64) with its
+// planes kept, then the path-count / dependency launch and the output pass
+// into delta / paths ([ns][n], device, either may be null) and acc.
+int bb_enqueue(bfs_graph *g, const uint32_t *sources, uint32_t ns, float *delta, uint32_t *paths, float *acc,
+		cudaStream_t st) {
+	if (g->relabeled) return BFS_EUNSUPPORTED;
+	uint32_t planes = 0;
+	int rc = batch_prepare(g, 1, &planes);
+	if (rc) return rc;
+	auto &b = g->bb;
+	const MsArgs a = batch_args(g, 1, ns, planes);
+	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
+	if (cudaMemcpyAsync(b.d_sources, sources, sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, st) != cudaSuccess)
+		return BFS_ECUDA;
+	int ms_grid = 0;
+	if ((rc = ms_launch(a, b.d_sources, ns, nullptr, g->num_sms, st, &ms_grid, nullptr, nullptr))) return rc;
+	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
+	BbArgs x{};
+	x.n = g->n;
+	x.ns = ns;
+	x.row_off = g->dg.row_off;
+	x.col = g->dg.col;
+	x.in_off = g->dg.in_off;
+	x.in_src = g->dg.in_src;
+	x.hist = a.hist;
+	x.vis = a.vis;
+	x.ms = a.ctl;
+	x.ichunk_v = g->ms_chunk_v;
+	x.ichunk_beg = g->ms_chunk_beg;
+	x.nich = g->ms_nchunks;
+	x.ochunk_v = g->bb_ochunk_v;
+	x.ochunk_beg = g->bb_ochunk_beg;
+	x.noch = g->bb_noch;
+	x.sigma = b.sigma;
+	x.dsum = b.dsum;
+	x.partial = b.partial;
+	x.ctl = b.ctl;
+	x.wait_limit_ns = wait_limit_ns(g->opt);
+	x.hold_barrier = g->opt.test_hold_barrier;
+	x.ctas_per_sm = g->opt.ctas_per_sm;
+	BbOut o{b.d_sources, delta, paths, acc};
+	if ((rc = bb_launch(x, o, g->num_sms, st, &b.grid, b.e2))) return rc;
+	if (cudaEventRecord(b.e3, st) != cudaSuccess) return BFS_ECUDA;
+	b.stream = st;
+	b.ns = ns;
+	g->bc_last_batched = true;
+	// the batch buffers now hold this traversal, not a bfs_run_batch result
+	g->mb.have_run = false;
+	return BFS_OK;
+}
+
+// Waits for the last batched betweenness run; its statistics into *out.
+int bb_collect(bfs_graph *g, bfs_bc_stats *out) {
+	auto &b = g->bb;
+	cudaStream_t st = b.stream;
+	if (cudaMemcpyAsync(b.h_ctl, b.ctl, sizeof(BbControl), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+			cudaMemcpyAsync(b.h_ms, g->mb.args.ctl, sizeof(MsControl), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+			cudaStreamSynchronize(st) != cudaSuccess)
+		return BFS_ECUDA;
+	const BbControl &c = *b.h_ctl;
+	const MsStats &ms = b.h_ms->stats;
+	if (out) {
+		bfs_bc_stats s{};
+		s.num_sources = b.ns;
+		s.batched_sources = b.ns;
+		s.depth = ms.depth ? ms.depth - 1 : 0;
+		s.reached = c.reached[b.ns - 1];
+		s.status = (uint32_t) c.err;
+		s.edges_reached = ms.traversed;
+		s.edges_forward = c.edges_fwd;
+		s.edges_reverse = c.edges_rev;
+		s.edges_matched_forward = c.matched_fwd;
+		s.edges_matched_reverse = c.matched_rev;
+		float ms_all = 0, tms = 0;
+		cudaEventElapsedTime(&ms_all, b.e0, b.e3);
+		cudaEventElapsedTime(&tms, b.e0, b.e1);
+		s.device_ms = ms_all;
+		s.traversal_ms = tms;
+		if (c.t[0] && c.t[1] >= c.t[0]) s.paths_ms = (float) ((c.t[1] - c.t[0]) * 1e-6);
+		if (c.t[1] && c.t[2] >= c.t[1]) s.dependencies_ms = (float) ((c.t[2] - c.t[1]) * 1e-6);
+		s.grid_ctas = (uint32_t) b.grid;
+		for (uint32_t d = 0; d < ms.depth && d < BFS_BC_TRACE_LEVELS && d < kMsTraceLevels; ++d)
+			s.level_vertices[d] = ms.frontier[d];
+		for (uint32_t i = 0; i < b.ns; ++i) s.source_reached[i] = c.reached[i];
+		*out = s;
+	}
+	return c.err;
+}
+
+// Adds one run's statistics into a total over runs.
+void bc_stats_add(bfs_bc_stats &total, const bfs_bc_stats &one) {
+	total.depth = std::max(total.depth, one.depth);
+	total.reached = one.reached;
+	total.edges_reached += one.edges_reached;
+	total.edges_forward += one.edges_forward;
+	total.edges_reverse += one.edges_reverse;
+	total.edges_matched_forward += one.edges_matched_forward;
+	total.edges_matched_reverse += one.edges_matched_reverse;
+	total.traversal_ms += one.traversal_ms;
+	total.sort_ms += one.sort_ms;
+	total.paths_ms += one.paths_ms;
+	total.dependencies_ms += one.dependencies_ms;
+	total.num_sources += one.num_sources;
+	total.batched_sources += one.batched_sources;
+	total.fallback_sources += one.fallback_sources;
+	total.grid_ctas = one.grid_ctas;
+	std::memcpy(total.level_paths_ms, one.level_paths_ms, sizeof(one.level_paths_ms));
+	std::memcpy(total.level_dependencies_ms, one.level_dependencies_ms, sizeof(one.level_dependencies_ms));
+	std::memcpy(total.level_vertices, one.level_vertices, sizeof(one.level_vertices));
+	std::memcpy(total.level_big, one.level_big, sizeof(one.level_big));
+	std::memcpy(total.level_medium, one.level_medium, sizeof(one.level_medium));
+	std::memcpy(total.source_reached, one.source_reached, sizeof(one.source_reached));
+}
+
+// One source at a time through bfs_bc_run's kernel (the batch fallback):
+// dependencies / path counts to host rows (either may be null), acc added to.
+int bc_sources_one_by_one(bfs_graph *g, const uint32_t *sources, uint32_t ns, float *deps, uint32_t *paths,
+		float *acc, bfs_bc_stats &total) {
+	int rc = bc_prepare(g);
+	if (rc) return rc;
+	for (uint32_t i = 0; i < ns; ++i) {
+		bfs_bc_stats one{};
+		if ((rc = bc_enqueue(g, sources[i], nullptr, nullptr, acc, 0))) return rc;
+		if ((rc = bc_collect(g, &one))) return rc;
+		if (deps && cudaMemcpy(deps + (size_t) i * g->n, g->bc.delta, sizeof(float) * g->n, cudaMemcpyDeviceToHost) !=
+				cudaSuccess)
+			return BFS_ECUDA;
+		if (paths && cudaMemcpy(paths + (size_t) i * g->n, g->bc.sigma, sizeof(uint32_t) * g->n,
+						cudaMemcpyDeviceToHost) != cudaSuccess)
+			return BFS_ECUDA;
+		bc_stats_add(total, one);
+	}
+	return BFS_OK;
 }
 
 } // namespace
@@ -1512,7 +1749,7 @@ int bfs_set_options(bfs_graph *g, const bfs_options *opt) {
 			opt->warp_max_degree == 0 || opt->cta_max_degree < opt->warp_max_degree || opt->batch_planes == 1 ||
 			opt->batch_planes > kMsMaxLevel + 1 || (opt->batch_planes == 0 && opt->batch_budget_mb == 0) ||
 			opt->batch_push_div == 0 || opt->bc_level_bytes > 2 || opt->switch_rule > BFS_SWITCH_UNVISITED ||
-			opt->bu_alpha == 0 || opt->td_beta == 0 || opt->ctas_per_sm > 2)
+			opt->bu_alpha == 0 || opt->td_beta == 0 || opt->ctas_per_sm > 2 || opt->bc_batch > 1)
 		return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);
 	g->opt = *opt;
@@ -1679,8 +1916,56 @@ int bfs_bc_run_device(bfs_graph *g, uint32_t source, float *dependencies, uint32
 int bfs_bc_last_stats(bfs_graph *g, bfs_bc_stats *stats) {
 	if (!g || !stats) return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);
+	if (g->bc_last_batched) return bb_collect(g, stats);
 	if (!g->bc.ctl) return BFS_EARG;
 	return bc_collect(g, stats);
+}
+
+int bfs_bc_run_batch(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *dependencies,
+		uint32_t *num_paths, bfs_bc_stats *stats) {
+	if (!g || !sources || num_sources == 0 || num_sources > BFS_BC_BATCH_MAX_SOURCES) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	if (g->host_only) return BFS_EUNSUPPORTED;
+	for (uint32_t i = 0; i < num_sources; ++i)
+		if (sources[i] >= g->n) return BFS_EARG;
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	int rc = bb_prepare(g, dependencies != nullptr, num_paths != nullptr);
+	if (rc) return rc;
+	auto &b = g->bb;
+	if ((rc = bb_enqueue(g, sources, num_sources, dependencies ? b.delta : nullptr, num_paths ? b.paths : nullptr,
+				 nullptr, 0)))
+		return rc;
+	bfs_bc_stats s{};
+	rc = bb_collect(g, &s);
+	if (rc == BFS_EUNSUPPORTED) {
+		// deeper than the planes: one source at a time
+		bfs_bc_stats total{};
+		if ((rc = bc_sources_one_by_one(g, sources, num_sources, dependencies, num_paths, nullptr, total))) return rc;
+		total.fallback_sources = num_sources;
+		if (stats) *stats = total;
+		return BFS_OK;
+	}
+	if (rc) return rc;
+	const size_t cells = (size_t) num_sources * g->n;
+	if (dependencies && cudaMemcpy(dependencies, b.delta, sizeof(float) * cells, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return BFS_ECUDA;
+	if (num_paths && cudaMemcpy(num_paths, b.paths, sizeof(uint32_t) * cells, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return BFS_ECUDA;
+	if (stats) *stats = s;
+	return BFS_OK;
+}
+
+int bfs_bc_run_batch_device(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *dependencies,
+		uint32_t *num_paths, void *stream) {
+	if (!g || !sources || num_sources == 0 || num_sources > BFS_BC_BATCH_MAX_SOURCES) return BFS_EARG;
+	std::lock_guard<std::mutex> lk(g->mu);
+	if (g->host_only) return BFS_EUNSUPPORTED;
+	for (uint32_t i = 0; i < num_sources; ++i)
+		if (sources[i] >= g->n) return BFS_EARG;
+	if (cudaSetDevice(g->device) != cudaSuccess) return BFS_ECUDA;
+	int rc = bb_prepare(g, false, false);
+	if (rc) return rc;
+	return bb_enqueue(g, sources, num_sources, dependencies, num_paths, nullptr, (cudaStream_t) stream);
 }
 
 int bfs_bc_accumulate(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *centrality,
@@ -1694,41 +1979,42 @@ int bfs_bc_accumulate(bfs_graph *g, const uint32_t *sources, uint32_t num_source
 	int rc = bc_prepare(g);
 	if (rc) return rc;
 	auto &b = g->bc;
+	if (g->opt.bc_batch && (rc = bb_prepare(g, false, false))) return rc;
 	if (cudaMemsetAsync(b.acc, 0, sizeof(float) * g->n, 0) != cudaSuccess) return BFS_ECUDA;
-	cudaEvent_t start = nullptr;
-	if (cudaEventCreate(&start) != cudaSuccess || cudaEventRecord(start, 0) != cudaSuccess) {
+	cudaEvent_t start = nullptr, end = nullptr;
+	if (cudaEventCreate(&start) != cudaSuccess || cudaEventCreate(&end) != cudaSuccess ||
+			cudaEventRecord(start, 0) != cudaSuccess) {
 		if (start) cudaEventDestroy(start);
+		if (end) cudaEventDestroy(end);
 		return BFS_ECUDA;
 	}
 	bfs_bc_stats total{};
-	bfs_bc_stats one{};
-	for (uint32_t i = 0; i < num_sources && rc == BFS_OK; ++i) {
-		rc = bc_enqueue(g, sources[i], nullptr, nullptr, b.acc, 0);
-		if (rc == BFS_OK) rc = bc_collect(g, &one);
-		if (rc == BFS_OK) {
-			total.depth = std::max(total.depth, one.depth);
-			total.reached = one.reached;
-			total.edges_reached += one.edges_reached;
-			total.edges_forward += one.edges_forward;
-			total.edges_reverse += one.edges_reverse;
-			total.traversal_ms += one.traversal_ms;
-			total.sort_ms += one.sort_ms;
-			total.paths_ms += one.paths_ms;
-			total.dependencies_ms += one.dependencies_ms;
-			total.num_sources++;
+	if (!g->opt.bc_batch) {
+		rc = bc_sources_one_by_one(g, sources, num_sources, nullptr, nullptr, b.acc, total);
+	} else {
+		// groups of up to 64 sources; a group deeper than the planes one source at a time
+		for (uint32_t i = 0; i < num_sources && rc == BFS_OK; i += kBbMaxSources) {
+			const uint32_t k = std::min<uint32_t>(kBbMaxSources, num_sources - i);
+			bfs_bc_stats one{};
+			rc = bb_enqueue(g, sources + i, k, nullptr, nullptr, b.acc, 0);
+			if (rc == BFS_OK) rc = bb_collect(g, &one);
+			if (rc == BFS_EUNSUPPORTED) {
+				bfs_bc_stats part{};
+				rc = bc_sources_one_by_one(g, sources + i, k, nullptr, nullptr, b.acc, part);
+				part.fallback_sources = k;
+				if (rc == BFS_OK) bc_stats_add(total, part);
+			} else if (rc == BFS_OK) {
+				bc_stats_add(total, one);
+			}
 		}
 	}
 	float ms = 0;
-	if (rc == BFS_OK) cudaEventElapsedTime(&ms, start, b.e2);
+	if (rc == BFS_OK && cudaEventRecord(end, 0) == cudaSuccess && cudaEventSynchronize(end) == cudaSuccess)
+		cudaEventElapsedTime(&ms, start, end);
 	cudaEventDestroy(start);
+	cudaEventDestroy(end);
 	if (rc) return rc;
 	total.device_ms = ms;
-	total.grid_ctas = (uint32_t) b.grid;
-	std::memcpy(total.level_paths_ms, one.level_paths_ms, sizeof(one.level_paths_ms));
-	std::memcpy(total.level_dependencies_ms, one.level_dependencies_ms, sizeof(one.level_dependencies_ms));
-	std::memcpy(total.level_vertices, one.level_vertices, sizeof(one.level_vertices));
-	std::memcpy(total.level_big, one.level_big, sizeof(one.level_big));
-	std::memcpy(total.level_medium, one.level_medium, sizeof(one.level_medium));
 	if (stats) *stats = total;
 	if (cudaMemcpy(centrality, b.acc, sizeof(float) * g->n, cudaMemcpyDeviceToHost) != cudaSuccess) return BFS_ECUDA;
 	return BFS_OK;

@@ -1,0 +1,481 @@
+// bc_batch.cu -- betweenness dependencies of up to 64 sources in one pass.
+//
+// No counterpart in the reference, whose BC() (apps/betweennessCentrality_simd/
+// bc.cpp:1717-2097) handles one source per call; for every source the results
+// are that function's: path counts summed over in-edges from the previous
+// level (unsigned, wrapping), dependency sums over out-edges to the next level
+// from the deepest level up, and its float formulas (inverse
+// 1.0f / (float)(int) count, result (D - inverse) / inverse, 0 where the
+// count is 0).
+//
+// The batched traversal (msbfs.cu) leaves, for every level L, the plane
+// hist[L][v]: the sources that reached v first at level L.  u -> v is a
+// shortest-path edge of source s exactly when bit s is set in both
+// hist[L-1][u] and hist[L][v], so one AND of two words gives all the sources
+// an edge serves.  The state is per (vertex, source): sigma[v][64] and
+// dsum[v][64], a 256-byte row each; lane l of a warp owns sources l and l+32.
+//
+// One cooperative launch, levels separated by grid barriers:
+//   forward, L = 1 .. depth-1, every v with hist[L][v] != 0:
+//     sigma[v][s] = sum of sigma[u][s] over in-edges u -> v, s in hist[L][v] & hist[L-1][u];
+//   reverse, L = depth-1 .. 0:
+//     dsum[v][s] = (sum of dsum[w][s] over out-edges v -> w, s in hist[L][v] & hist[L+1][w])
+//                  + 1 / sigma[v][s].
+// Per level a warp screens 32 consecutive vertices and walks the concatenated
+// edge lists of those at that level, 32 edges per step (each edge's vertex
+// found by a binary search over the warp's degree prefix); an edge's source
+// mask is one AND.  The edges with a non-empty mask are then taken in edge
+// order, four at a time, each a coalesced read of the neighbour's row by the
+// lanes whose bit is set.  Vertices with more than kBbBig edges in the
+// sweep's direction are cut into kBbChunk-edge chunks that warps all over the
+// grid sum; the partial rows are added in chunk order after a grid barrier.
+// Every sum has a fixed order, so repeated runs give identical bits.
+// The output pass (its own launch) turns the [v][64] rows into [source][v]
+// rows through a shared-memory transpose, 0 for unreached pairs, and/or adds
+// each vertex's dependencies into an accumulator in source order.
+#include "bc_batch.h"
+
+#include <algorithm>
+
+#include "../../include/bfs_gb300.h"
+#include "device_common.cuh"
+
+namespace bfsg {
+namespace {
+
+constexpr int kBbThreads = 512;
+constexpr int kBbWarps = kBbThreads / 32;
+constexpr int kBbUnroll = 4;
+constexpr uint32_t kBbOutV = 64;   // output pass: vertices per tile
+constexpr int kBbOutThreads = 256;
+
+__device__ __forceinline__ uint64_t bb_shfl64(uint64_t x, int src) {
+	return (uint64_t) __shfl_sync(kFull, (unsigned long long) x, src);
+}
+__device__ __forceinline__ uint64_t bb_ldg64(const uint64_t *p) { return __ldg((const unsigned long long *) p); }
+
+// The two sweeps: forward reads in-edges and path counts, reverse reads
+// out-edges and dependency sums.
+template <bool kFwd> struct BbDir;
+template <> struct BbDir<true> {
+	using T = uint32_t;
+	static __device__ __forceinline__ const uint32_t *off(const BbArgs &a) { return a.in_off; }
+	static __device__ __forceinline__ const uint32_t *adj(const BbArgs &a) { return a.in_src; }
+	static __device__ __forceinline__ const uint32_t *chunk_v(const BbArgs &a) { return a.ichunk_v; }
+	static __device__ __forceinline__ const uint32_t *chunk_beg(const BbArgs &a) { return a.ichunk_beg; }
+	static __device__ __forceinline__ uint32_t nchunks(const BbArgs &a) { return a.nich; }
+	static __device__ __forceinline__ T load(const BbArgs &a, size_t i) { return __ldcg(a.sigma + i); }
+	static __device__ __forceinline__ T from_bits(uint32_t b) { return b; }
+	static __device__ __forceinline__ uint32_t to_bits(T x) { return x; }
+	static __device__ __forceinline__ uint32_t pre(const BbArgs &, size_t, bool) { return 0u; }
+	static __device__ __forceinline__ void store(const BbArgs &a, size_t i, T sum, uint32_t) { a.sigma[i] = sum; }
+};
+template <> struct BbDir<false> {
+	using T = float;
+	static __device__ __forceinline__ const uint32_t *off(const BbArgs &a) { return a.row_off; }
+	static __device__ __forceinline__ const uint32_t *adj(const BbArgs &a) { return a.col; }
+	static __device__ __forceinline__ const uint32_t *chunk_v(const BbArgs &a) { return a.ochunk_v; }
+	static __device__ __forceinline__ const uint32_t *chunk_beg(const BbArgs &a) { return a.ochunk_beg; }
+	static __device__ __forceinline__ uint32_t nchunks(const BbArgs &a) { return a.noch; }
+	static __device__ __forceinline__ T load(const BbArgs &a, size_t i) { return __ldcg(a.dsum + i); }
+	static __device__ __forceinline__ T from_bits(uint32_t b) { return __uint_as_float(b); }
+	static __device__ __forceinline__ uint32_t to_bits(T x) { return __float_as_uint(x); }
+	// the vertex's path count, loaded when the vertex's first edge is taken so
+	// that the load is done by the time its sum is
+	static __device__ __forceinline__ uint32_t pre(const BbArgs &a, size_t i, bool mine) {
+		return mine ? __ldcg(a.sigma + i) : 0u;
+	}
+	// the reference's inverse: signed conversion of the unsigned count
+	static __device__ __forceinline__ void store(const BbArgs &a, size_t i, T sum, uint32_t sg) {
+		const float inv = sg ? 1.0f / (float) (int) sg : 0.0f;
+		a.dsum[i] = sum + inv;
+	}
+};
+
+// What a vertex's finished sums need besides the sums (the reverse sweep: its
+// path counts for this lane's two sources), loaded ahead.
+struct BbPre {
+	uint32_t p0, p1;
+};
+template <bool kFwd> __device__ __forceinline__ BbPre bb_pre(const BbArgs &a, uint32_t v, uint64_t hv) {
+	const unsigned lane = lane_id();
+	const size_t row = (size_t) v * 64;
+	return {BbDir<kFwd>::pre(a, row + lane, (hv >> lane) & 1ull),
+			BbDir<kFwd>::pre(a, row + lane + 32, (hv >> (lane + 32)) & 1ull)};
+}
+
+// Writes vertex v's finished sums for the sources in hv (lane: sources lane
+// and lane + 32).
+template <bool kFwd>
+__device__ __forceinline__ void bb_flush(const BbArgs &a, uint32_t v, uint64_t hv, typename BbDir<kFwd>::T acc0,
+		typename BbDir<kFwd>::T acc1, BbPre pre) {
+	const unsigned lane = lane_id();
+	const size_t row = (size_t) v * 64;
+	if ((hv >> lane) & 1ull) BbDir<kFwd>::store(a, row + lane, acc0, pre.p0);
+	if ((hv >> (lane + 32)) & 1ull) BbDir<kFwd>::store(a, row + lane + 32, acc1, pre.p1);
+}
+
+// The next (up to) kBbUnroll edges of `bal` (lanes holding edges with a
+// non-empty source mask), lowest lane first: their neighbours' row entries for
+// this lane's two sources (0 where the edge does not serve the source) and
+// their vertex slots.  `bal` is warp-uniform; *cnt gets the edges taken.
+template <bool kFwd>
+__device__ __forceinline__ void bb_take(const BbArgs &a, uint32_t &bal, uint32_t u, uint64_t m, uint32_t slot,
+		typename BbDir<kFwd>::T (&x0)[kBbUnroll], typename BbDir<kFwd>::T (&x1)[kBbUnroll],
+		uint32_t (&oo)[kBbUnroll], int *cnt) {
+	using T = typename BbDir<kFwd>::T;
+	const unsigned lane = lane_id();
+	int c = 0;
+#pragma unroll
+	for (int k = 0; k < kBbUnroll; ++k) {
+		const bool ok = bal != 0u;
+		const int j = ok ? __ffs(bal) - 1 : 0;
+		bal &= bal - 1u;
+		const uint32_t uj = __shfl_sync(kFull, u, j);
+		const uint64_t mj = ok ? bb_shfl64(m, j) : 0ull;
+		oo[k] = __shfl_sync(kFull, slot, j);
+		c += ok ? 1 : 0;
+		const size_t row = (size_t) uj * 64;
+		x0[k] = ((mj >> lane) & 1ull) ? BbDir<kFwd>::load(a, row + lane) : T(0);
+		x1[k] = ((mj >> (lane + 32)) & 1ull) ? BbDir<kFwd>::load(a, row + lane + 32) : T(0);
+	}
+	*cnt = c;
+}
+
+// Block b of 32 consecutive vertices in one level of a sweep: those with at
+// most kBbBig edges in the sweep's direction.  `has_nb`: the neighbour level
+// exists (the reverse sweep's deepest level has none; its vertices get
+// 1/sigma alone).
+template <bool kFwd>
+__device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, unsigned long long &edges,
+		unsigned long long &matched) {
+	using D = BbDir<kFwd>;
+	using T = typename D::T;
+	const unsigned lane = lane_id();
+	const uint64_t *own = a.hist + (size_t) L * a.n;
+	const uint64_t *nb = a.hist + (size_t) (kFwd ? L - 1 : L + 1) * a.n;
+	const uint32_t *off = D::off(a), *adj = D::adj(a);
+	{
+		const uint32_t vb = b * 32, v = vb + lane;
+		const uint64_t hv = v < a.n ? bb_ldg64(own + v) : 0ull;
+		uint32_t beg = 0, end = 0;
+		if (hv) {
+			beg = __ldg(off + v);
+			end = __ldg(off + v + 1);
+		}
+		const bool part = hv != 0ull && end - beg <= kBbBig;
+		const uint32_t pm = __ballot_sync(kFull, part);
+		if (!pm) return;
+		const uint32_t d = part && has_nb ? end - beg : 0u;
+		const uint32_t incl = warp_incl_scan(d);
+		const uint32_t excl = incl - d;
+		const uint32_t total = __shfl_sync(kFull, incl, 31);
+		int cur = -1;
+		T acc0 = T(0), acc1 = T(0);
+		uint64_t hcur = 0;
+		BbPre pcur{0u, 0u};
+		uint32_t flushed = 0;
+		for (uint32_t e0 = 0; e0 < total; e0 += 32) {
+			const uint32_t e = e0 + lane;
+			// the edge's vertex slot: the first lane whose inclusive prefix exceeds e
+			uint32_t o = 0;
+#pragma unroll
+			for (uint32_t s = 16; s; s >>= 1) {
+				const uint32_t x = __shfl_sync(kFull, incl, o + s - 1);
+				if (x <= e) o += s;
+			}
+			const uint32_t obeg = __shfl_sync(kFull, beg, o), oex = __shfl_sync(kFull, excl, o);
+			const uint64_t ohv = bb_shfl64(hv, o);
+			uint32_t u = 0;
+			uint64_t m = 0;
+			if (e < total) {
+				u = __ldg(adj + obeg + (e - oex));
+				m = ohv & bb_ldg64(nb + u);
+			}
+			uint32_t bal = __ballot_sync(kFull, m != 0ull);
+			if (lane == 0) {
+				edges += min(32u, total - e0);
+				matched += __popc(bal);
+			}
+			while (bal) {
+				T x0[kBbUnroll], x1[kBbUnroll];
+				uint32_t oo[kBbUnroll];
+				int cnt;
+				bb_take<kFwd>(a, bal, u, m, o, x0, x1, oo, &cnt);
+#pragma unroll
+				for (int k = 0; k < kBbUnroll; ++k) {
+					if (k >= cnt) break;
+					if ((int) oo[k] != cur) {
+						if (cur >= 0) {
+							bb_flush<kFwd>(a, vb + cur, hcur, acc0, acc1, pcur);
+							flushed |= 1u << cur;
+						}
+						cur = (int) oo[k];
+						hcur = bb_shfl64(hv, cur);
+						pcur = bb_pre<kFwd>(a, vb + cur, hcur);
+						acc0 = T(0);
+						acc1 = T(0);
+					}
+					acc0 += x0[k];
+					acc1 += x1[k];
+				}
+			}
+		}
+		if (cur >= 0) {
+			bb_flush<kFwd>(a, vb + cur, hcur, acc0, acc1, pcur);
+			flushed |= 1u << cur;
+		}
+		// vertices none of whose edges serve their sources (the deepest level,
+		// sinks of the reverse sweep): nothing to add; two at a time, loads first
+		for (uint32_t r = pm & ~flushed; r;) {
+			const int j0 = __ffs(r) - 1;
+			r &= r - 1u;
+			const int j1 = r ? __ffs(r) - 1 : -1;
+			if (r) r &= r - 1u;
+			const uint64_t h0 = bb_shfl64(hv, j0), h1 = bb_shfl64(hv, j1 < 0 ? 0 : j1);
+			const BbPre p0 = bb_pre<kFwd>(a, vb + j0, h0);
+			const BbPre p1 = j1 >= 0 ? bb_pre<kFwd>(a, vb + j1, h1) : BbPre{0u, 0u};
+			bb_flush<kFwd>(a, vb + j0, h0, T(0), T(0), p0);
+			if (j1 >= 0) bb_flush<kFwd>(a, vb + j1, h1, T(0), T(0), p1);
+		}
+	}
+}
+
+// Chunk c (kBbChunk edges of a vertex with more than kBbBig edges) in one
+// level of a sweep: the sums of its edges into partial[c].
+template <bool kFwd>
+__device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, unsigned long long &edges,
+		unsigned long long &matched) {
+	using D = BbDir<kFwd>;
+	using T = typename D::T;
+	const unsigned lane = lane_id();
+	const uint64_t *own = a.hist + (size_t) L * a.n;
+	const uint64_t *nb = a.hist + (size_t) (kFwd ? L - 1 : L + 1) * a.n;
+	const uint32_t *off = D::off(a), *adj = D::adj(a), *cv = D::chunk_v(a), *cb = D::chunk_beg(a);
+	{
+		const uint32_t v = __ldg(cv + c);
+		const uint64_t hv = bb_ldg64(own + v);
+		if (!hv) return;
+		const uint32_t beg = __ldg(cb + c), end = min(beg + kBbChunk, __ldg(off + v + 1));
+		T acc0 = T(0), acc1 = T(0);
+		for (uint32_t e0 = beg; has_nb && e0 < end; e0 += 32) {
+			const uint32_t e = e0 + lane;
+			uint32_t u = 0;
+			uint64_t m = 0;
+			if (e < end) {
+				u = __ldg(adj + e);
+				m = hv & bb_ldg64(nb + u);
+			}
+			uint32_t bal = __ballot_sync(kFull, m != 0ull);
+			if (lane == 0) {
+				edges += min(32u, end - e0);
+				matched += __popc(bal);
+			}
+			while (bal) {
+				T x0[kBbUnroll], x1[kBbUnroll];
+				uint32_t oo[kBbUnroll];
+				int cnt;
+				bb_take<kFwd>(a, bal, u, m, 0u, x0, x1, oo, &cnt);
+#pragma unroll
+				for (int k = 0; k < kBbUnroll; ++k) {
+					if (k >= cnt) break;
+					acc0 += x0[k];
+					acc1 += x1[k];
+				}
+			}
+		}
+		const size_t row = (size_t) c * 64;
+		if ((hv >> lane) & 1ull) a.partial[row + lane] = D::to_bits(acc0);
+		if ((hv >> (lane + 32)) & 1ull) a.partial[row + lane + 32] = D::to_bits(acc1);
+	}
+}
+
+// After the chunk sums of a level: each chunked vertex of that level adds its
+// chunks' partial rows in chunk order (by the warp that holds its first chunk).
+template <bool kFwd>
+__device__ void bb_finish(const BbArgs &a, uint32_t L) {
+	using D = BbDir<kFwd>;
+	using T = typename D::T;
+	const uint32_t nch = D::nchunks(a);
+	const unsigned lane = lane_id();
+	const uint64_t *own = a.hist + (size_t) L * a.n;
+	const uint32_t *off = D::off(a), *cv = D::chunk_v(a), *cb = D::chunk_beg(a);
+	const uint32_t gwarp = blockIdx.x * kBbWarps + warp_id(), nwarps = gridDim.x * kBbWarps;
+	for (uint32_t c = gwarp; c < nch; c += nwarps) {
+		const uint32_t v = __ldg(cv + c);
+		const uint32_t b0 = __ldg(off + v);
+		if (__ldg(cb + c) != b0) continue;
+		const uint64_t hv = bb_ldg64(own + v);
+		if (!hv) continue;
+		const uint32_t k = (__ldg(off + v + 1) - b0 + kBbChunk - 1) / kBbChunk;
+		const bool w0 = (hv >> lane) & 1ull, w1 = (hv >> (lane + 32)) & 1ull;
+		T acc0 = T(0), acc1 = T(0);
+		for (uint32_t i = 0; i < k; i += kBbUnroll) {
+			T x0[kBbUnroll], x1[kBbUnroll];
+#pragma unroll
+			for (int j = 0; j < kBbUnroll; ++j) {
+				const bool in = i + j < k;
+				const size_t row = (size_t) (c + i + j) * 64;
+				x0[j] = in && w0 ? D::from_bits(ld_cg(a.partial + row + lane)) : T(0);
+				x1[j] = in && w1 ? D::from_bits(ld_cg(a.partial + row + lane + 32)) : T(0);
+			}
+#pragma unroll
+			for (int j = 0; j < kBbUnroll; ++j) {
+				acc0 += x0[j];
+				acc1 += x1[j];
+			}
+		}
+		bb_flush<kFwd>(a, v, hv, acc0, acc1, bb_pre<kFwd>(a, v, hv));
+	}
+}
+
+// One level of a sweep: the level's chunks, then its blocks of 32 vertices,
+// handed out one at a time through a counter (the cost of a block varies
+// with the edges of its vertices that serve a source; a fixed deal left warps
+// waiting at the level's barrier).  The next item is claimed while the
+// current one runs.
+template <bool kFwd>
+__device__ void bb_level(const BbArgs &a, uint32_t L, bool has_nb, unsigned *counter, unsigned long long &edges,
+		unsigned long long &matched) {
+	const uint32_t nch = BbDir<kFwd>::nchunks(a);
+	const uint32_t items = nch + (a.n + 31) / 32;
+	const unsigned lane = lane_id();
+	uint32_t item = lane == 0 ? atomicAdd(counter, 1u) : 0u;
+	item = __shfl_sync(kFull, item, 0);
+	while (item < items) {
+		const uint32_t next = lane == 0 ? atomicAdd(counter, 1u) : 0u;
+		if (item < nch) bb_chunk<kFwd>(a, L, has_nb, item, edges, matched);
+		else bb_block<kFwd>(a, L, has_nb, item - nch, edges, matched);
+		item = __shfl_sync(kFull, next, 0);
+	}
+}
+
+__device__ __forceinline__ void bb_add_counter(unsigned long long *dst, unsigned long long x) {
+	if (lane_id() == 0 && x) atomicAdd(dst, x);
+}
+
+__global__ void __launch_bounds__(kBbThreads, 2) k_bc_batch(BbArgs a) {
+	BbControl *ctl = a.ctl;
+	const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+	if (leader) ctl->t[0] = global_timer_ns();
+	// the traversal's outcome decides for every CTA alike: its planes must hold
+	// every level from 0 (no early output pass)
+	const MsControl *ms = a.ms;
+	const int ms_err = *(const volatile int *) &ms->err;
+	const uint32_t complete = *(const volatile unsigned *) &ms->stats.complete;
+	const uint32_t base = *(const volatile unsigned *) &ms->stats.base;
+	const uint32_t spills = *(const volatile unsigned *) &ms->stats.spills;
+	const uint32_t depth = *(const volatile unsigned *) &ms->stats.depth;
+	if (ms_err || !complete || base || spills || depth == 0) {
+		if (leader) ctl->err = ms_err ? ms_err : BFS_EUNSUPPORTED;
+		return;
+	}
+	if (leader) ctl->depth = depth;
+	unsigned epoch = 0;
+	const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+	for (uint32_t v = t0; v < a.n; v += stride) {
+		uint64_t h = bb_ldg64(a.hist + v);
+		while (h) {
+			a.sigma[(size_t) v * 64 + (__ffsll((long long) h) - 1)] = 1u;
+			h &= h - 1ull;
+		}
+	}
+	bool ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
+	unsigned long long ef = 0, mf = 0, er = 0, mr = 0;
+	for (uint32_t L = 1; ok && L < depth; ++L) {
+		bb_level<true>(a, L, true, &ctl->work[0][L], ef, mf);
+		if (a.nich) {
+			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
+			bb_finish<true>(a, L);
+		}
+		ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
+	}
+	if (leader) ctl->t[1] = global_timer_ns();
+	for (int L = (int) depth - 1; ok && L >= 0; --L) {
+		const bool has_nb = (uint32_t) L + 1 < depth;
+		bb_level<false>(a, (uint32_t) L, has_nb, &ctl->work[1][L], er, mr);
+		if (a.noch) {
+			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
+			bb_finish<false>(a, (uint32_t) L);
+		}
+		if (L > 0) ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
+	}
+	if (leader) ctl->t[2] = global_timer_ns();
+	bb_add_counter(&ctl->edges_fwd, ef);
+	bb_add_counter(&ctl->matched_fwd, mf);
+	bb_add_counter(&ctl->edges_rev, er);
+	bb_add_counter(&ctl->matched_rev, mr);
+}
+
+// Output pass: [v][64] rows -> dependencies and path counts [source][v]
+// (0 for unreached pairs) and/or acc[v] += dependencies of the sources != v,
+// in source order; counts the vertices each source reached.
+__global__ void __launch_bounds__(kBbOutThreads) k_bc_batch_out(BbArgs a, BbOut o) {
+	if (*(const volatile int *) &a.ctl->err) return;
+	__shared__ float sd[kBbOutV][kBbMaxSources + 1];
+	__shared__ uint32_t sp[kBbOutV][kBbMaxSources + 1];
+	__shared__ uint64_t svis[kBbOutV];
+	__shared__ uint32_t ssrc[kBbMaxSources];
+	const uint32_t t = threadIdx.x, ns = a.ns;
+	if (t < kBbMaxSources) ssrc[t] = t < ns ? o.sources[t] : 0xFFFFFFFFu;
+	const uint64_t smask = ns >= 64 ? ~0ull : (1ull << ns) - 1ull;
+	uint32_t reached = 0;  // threads 64..127: vertices reached from source t - 64
+	for (uint32_t v0 = blockIdx.x * kBbOutV; v0 < a.n; v0 += gridDim.x * kBbOutV) {
+		const uint32_t nv = min(kBbOutV, a.n - v0);
+		__syncthreads();
+		if (t < nv) svis[t] = bb_ldg64(a.vis + v0 + t) & smask;
+		__syncthreads();
+		for (uint32_t i = t; i < nv * 64; i += blockDim.x) {
+			const uint32_t j = i / 64, s = i % 64;
+			const bool r = (svis[j] >> s) & 1ull;
+			const size_t x = (size_t) v0 * 64 + i;
+			const uint32_t sg = r ? a.sigma[x] : 0u;
+			const float dv = r ? a.dsum[x] : 0.0f;
+			const float inv = sg ? 1.0f / (float) (int) sg : 0.0f;
+			sd[j][s] = inv != 0.0f ? (dv - inv) / inv : 0.0f;
+			sp[j][s] = sg;
+		}
+		__syncthreads();
+		if (o.delta || o.paths)
+			for (uint32_t i = t; i < ns * kBbOutV; i += blockDim.x) {
+				const uint32_t s = i / kBbOutV, j = i % kBbOutV;
+				if (j >= nv) continue;
+				const size_t x = (size_t) s * a.n + v0 + j;
+				if (o.delta) o.delta[x] = sd[j][s];
+				if (o.paths) o.paths[x] = sp[j][s];
+			}
+		if (o.acc && t < nv) {
+			const uint32_t v = v0 + t;
+			float x = o.acc[v];
+			for (uint32_t s = 0; s < ns; ++s)
+				if (ssrc[s] != v) x += sd[t][s];
+			o.acc[v] = x;
+		}
+		if (t >= 64 && t < 64 + ns)
+			for (uint32_t j = 0; j < nv; ++j) reached += (uint32_t) ((svis[j] >> (t - 64)) & 1ull);
+	}
+	if (t >= 64 && t < 64 + ns && reached) atomicAdd(&a.ctl->reached[t - 64], reached);
+}
+
+} // namespace
+
+int bb_launch(const BbArgs &a, const BbOut &o, int num_sms, cudaStream_t st, int *grid, cudaEvent_t between) {
+	if (a.ns == 0 || a.ns > kBbMaxSources) return BFS_EARG;
+	int per_sm = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bc_batch, kBbThreads, 0) != cudaSuccess || per_sm < 1)
+		return BFS_ECUDA;
+	per_sm = std::min(per_sm, 2);
+	if (a.ctas_per_sm) per_sm = std::min(per_sm, (int) a.ctas_per_sm);
+	const int g = num_sms * per_sm;
+	if (grid) *grid = g;
+	if (cudaMemsetAsync(a.ctl, 0, sizeof(BbControl), st) != cudaSuccess) return BFS_ECUDA;
+	BbArgs aa = a;
+	void *args[] = {&aa};
+	if (cudaLaunchCooperativeKernel((const void *) k_bc_batch, dim3(g), dim3(kBbThreads), args, 0, st) != cudaSuccess)
+		return BFS_ECUDA;
+	if (between && cudaEventRecord(between, st) != cudaSuccess) return BFS_ECUDA;
+	k_bc_batch_out<<<num_sms * 4, kBbOutThreads, 0, st>>>(a, o);
+	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
+}
+
+} // namespace bfsg

@@ -1,0 +1,62 @@
+// bc_batch.h -- betweenness dependencies of up to 64 sources at once, on the
+// bit-sliced batched traversal (internal).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "msbfs.h"
+
+namespace bfsg {
+
+constexpr uint32_t kBbMaxSources = 64;       // one 64-bit word of sources per vertex
+constexpr uint32_t kBbBig = kMsPullBig;      // degree above which a vertex's edges are summed in chunks ...
+constexpr uint32_t kBbChunk = kMsChunk;      // ... of this many edges (the batched pull's in-edge chunks)
+
+struct BbControl {
+	unsigned bar[2];                 // grid barrier
+	int err;                         // BFS_* status (0 ok)
+	uint32_t depth;                  // levels of the traversal (deepest level + 1)
+	unsigned long long edges_fwd;    // in-edges read by the path-count sweeps
+	unsigned long long edges_rev;    // out-edges read by the dependency sweeps
+	unsigned long long matched_fwd;  // of which into the previous level for at least one source
+	unsigned long long matched_rev;  // ... into the next level
+	unsigned long long t[3];         // global timer: start, path counts done, dependencies done
+	unsigned int reached[kBbMaxSources];  // vertices reached from each source (output pass)
+	unsigned int work[2][kMsMaxLevel + 1];  // per sweep and level: next work item (chunks, then vertex blocks)
+};
+
+struct BbArgs {
+	uint32_t n, ns;
+	const uint32_t *row_off, *col;     // CSR
+	const uint32_t *in_off, *in_src;   // in-edge lists
+	const uint64_t *hist;              // plane L at hist + L * n: sources that reached v first at level L
+	const uint64_t *vis;               // [n] sources that reached v
+	const MsControl *ms;               // the traversal's control block (depth, completion, status)
+	const uint32_t *ichunk_v, *ichunk_beg;  // in-edge chunks of vertices with in-degree > kBbBig
+	uint32_t nich;
+	const uint32_t *ochunk_v, *ochunk_beg;  // out-edge chunks of vertices with out-degree > kBbBig
+	uint32_t noch;
+	uint32_t *sigma;                   // [n][64] path counts (mod 2^32)
+	float *dsum;                       // [n][64] 1/sigma + the dependency sums of the next level
+	uint32_t *partial;                 // [max(nich, noch)][64] chunk sums (value bits)
+	BbControl *ctl;
+	unsigned long long wait_limit_ns;  // bound of every grid-barrier wait
+	uint32_t hold_barrier;             // tests: CTA 0 skips its arrival at this barrier (0 = off)
+	uint32_t ctas_per_sm;              // 0 = as many as fit (at most 2)
+};
+
+struct BbOut {
+	const uint32_t *sources;  // [ns] device
+	float *delta;             // [ns][n] dependencies, or null
+	uint32_t *paths;          // [ns][n] path counts, or null
+	float *acc;               // [n] or null: += the dependency of each source s on v (v != s), sources in order
+};
+
+// Enqueues, after the batched traversal that filled a.hist / a.vis / a.ms,
+// the cooperative path-count and dependency launch and the output pass; the
+// control block is cleared first.  `between` (may be null) is recorded
+// between the two launches; *grid gets the CTA count.
+int bb_launch(const BbArgs &a, const BbOut &o, int num_sms, cudaStream_t st, int *grid, cudaEvent_t between);
+
+} // namespace bfsg

@@ -792,6 +792,10 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 			break;
 		}
 		if (lvl + 1 - base >= a.planes) {
+			if (!levels) {  // planes kept for a later pass (betweenness): they must hold every level
+				if (leader) atomicExch(&ctl->err, BFS_EUNSUPPORTED);
+				break;
+			}
 			// planes full: write them out, keep the frontier's plane as plane 0
 			ms_emit(a, levels, ns, base, base == 0 ? 0 : 1, lvl - base, base != 0, lev);
 			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
@@ -927,7 +931,7 @@ int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *
 		return BFS_ECUDA;
 	if (between && cudaEventRecord(between, st) != cudaSuccess) return BFS_ECUDA;
 	if (between2 && cudaEventRecord(between2, st) != cudaSuccess) return BFS_ECUDA;
-	k_ms_emit<<<num_sms * 2, kMsThreads, 0, st>>>(a, ns, levels);
+	if (levels) k_ms_emit<<<num_sms * 2, kMsThreads, 0, st>>>(a, ns, levels);
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }
 

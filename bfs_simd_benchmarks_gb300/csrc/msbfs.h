@@ -79,7 +79,9 @@ struct MsArgs {
 // Enqueues the whole batched traversal (one cooperative launch and the
 // output pass) on `st`; `between` and `between2` (either may be null) are
 // recorded between the two;
-// *grid receives the launch's CTA count.
+// *grid receives the launch's CTA count.  levels == null: no output pass, the
+// planes stay for a later pass, and a traversal deeper than the planes stops
+// with BFS_EUNSUPPORTED.
 int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *levels, int num_sms, cudaStream_t st,
 		int *grid, cudaEvent_t between, cudaEvent_t between2);
 

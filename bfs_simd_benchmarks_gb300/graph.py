@@ -246,6 +246,28 @@ class Graph:
                                            C.c_void_p(paths_ptr) if paths_ptr else None,
                                            C.c_void_p(stream) if stream else None), "bfs_bc_run_device")
 
+    def bc_batch(self, sources, paths: bool = True):
+        """Betweenness of up to 64 sources at once (bfs_bc_run_batch): float32
+        [k, N] dependencies, uint32 [k, N] shortest-path counts (or None) and
+        the stats."""
+        src = _u32(sources)
+        n = self.num_vertices
+        dep = np.empty((src.size, n), dtype=np.float32)
+        sig = np.empty((src.size, n), dtype=np.uint32) if paths else None
+        st = N.BcStats()
+        N.check(N.load().bfs_bc_run_batch(self._h, _ptr(src, C.c_uint32), src.size, dep.ctypes.data_as(C.c_void_p),
+                                          sig.ctypes.data_as(C.c_void_p) if paths else None, C.byref(st)),
+                "bfs_bc_run_batch")
+        return dep, sig, st.as_dict()
+
+    def bc_batch_device(self, sources, dependencies_ptr: int = 0, paths_ptr: int = 0, stream: int = 0) -> None:
+        """bfs_bc_run_batch_device: enqueued on `stream`, [k, N] results into device buffers."""
+        src = _u32(sources)
+        N.check(N.load().bfs_bc_run_batch_device(self._h, _ptr(src, C.c_uint32), src.size,
+                                                 C.c_void_p(dependencies_ptr) if dependencies_ptr else None,
+                                                 C.c_void_p(paths_ptr) if paths_ptr else None,
+                                                 C.c_void_p(stream) if stream else None), "bfs_bc_run_batch_device")
+
     def bc_stats(self) -> dict:
         st = N.BcStats()
         N.check(N.load().bfs_bc_last_stats(self._h, C.byref(st)), "bfs_bc_last_stats")

@@ -166,6 +166,8 @@ typedef struct bfs_options {
 	uint32_t td_beta;          /* BFS_SWITCH_UNVISITED: beta (default 24) */
 	uint32_t ctas_per_sm;      /* CTAs per SM of the cooperative traversal grids: 0 = as many as fit (at most
 	                              2), or 1 or 2 */
+	uint32_t bc_batch;         /* bfs_bc_accumulate: 1 (default) = sources in groups of up to 64 through the
+	                              batched betweenness kernel (bfs_bc_run_batch); 0 = one source at a time */
 } bfs_options;
 
 #define BFS_SWITCH_REFERENCE 0u
@@ -514,6 +516,13 @@ typedef struct bfs_bc_stats {
 	uint32_t level_vertices[BFS_BC_TRACE_LEVELS];
 	uint32_t level_big[BFS_BC_TRACE_LEVELS];
 	uint32_t level_medium[BFS_BC_TRACE_LEVELS];
+	/* batched runs (bfs_bc_run_batch, bfs_bc_accumulate with bc_batch = 1) */
+	uint32_t batched_sources;   /* sources run through the batched kernel */
+	uint32_t fallback_sources;  /* sources run one at a time because their batch's traversal was deeper than
+	                               the batch's level planes */
+	uint64_t edges_matched_forward;  /* edges read by the path-count sweeps that serve at least one source */
+	uint64_t edges_matched_reverse;  /* ... by the dependency sweeps */
+	uint32_t source_reached[64];     /* the last batch: vertices reached from each of its sources */
 } bfs_bc_stats;
 
 /* dependencies[N] and num_paths[N] are HOST buffers (either may be NULL). */
@@ -523,13 +532,36 @@ int bfs_bc_run(bfs_graph *g, uint32_t source, float *dependencies, uint32_t *num
 int bfs_bc_run_device(bfs_graph *g, uint32_t source, float *dependencies, uint32_t *num_paths, void *stream);
 /* Statistics of the last bfs_bc_* run (synchronises with it). */
 int bfs_bc_last_stats(bfs_graph *g, bfs_bc_stats *stats);
+/* Batched betweenness (no counterpart in the reference, whose BC() takes one
+ * source per call): the dependencies and path counts of up to 64 sources from
+ * one bit-sliced traversal (the bfs_run_batch kernel) and one pass over the
+ * graph per level and direction, every (vertex, source) pair in 8 bytes of
+ * state.  Per source the values are bfs_bc_run's (path counts bit-exact;
+ * dependencies the same formulas, float sums in another fixed order: repeated
+ * calls give identical bits).  dependencies [num_sources][N] and num_paths
+ * [num_sources][N] are HOST buffers (either may be NULL).  A batch whose
+ * traversal is deeper than its level planes (bfs_options.batch_planes /
+ * batch_budget_mb; or more than 254 levels) runs one source at a time
+ * through bfs_bc_run's kernel instead (stats->fallback_sources). */
+#define BFS_BC_BATCH_MAX_SOURCES 64
+int bfs_bc_run_batch(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *dependencies,
+		uint32_t *num_paths, bfs_bc_stats *stats);
+/* The same enqueued on `stream` into DEVICE buffers [num_sources][N] (either
+ * may be NULL); sources is a host array.  No fallback: a batch deeper than its
+ * planes ends with status BFS_EUNSUPPORTED (bfs_bc_last_stats) and leaves the
+ * buffers unwritten. */
+int bfs_bc_run_batch_device(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *dependencies,
+		uint32_t *num_paths, void *stream);
 /* Betweenness centrality over a set of sources: centrality[v] (HOST, N floats,
- * overwritten) = sum over the sources s != v of the dependencies of s on v;
- * over all N sources it is the unnormalised directed betweenness. */
+ * overwritten) = sum over the sources s != v of the dependencies of s on v,
+ * added in source order; over all N sources it is the unnormalised directed
+ * betweenness.  With bfs_options.bc_batch = 1 (default) the sources go through
+ * the batched kernel 64 at a time. */
 int bfs_bc_accumulate(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *centrality,
 		bfs_bc_stats *stats);
 /* The same into a DEVICE buffer that is added to (not cleared), enqueued on
- * `stream`; sources is a host array. */
+ * `stream`; sources is a host array.  One source at a time (bfs_bc_run's
+ * kernel), whatever bc_batch says: an enqueued call cannot fall back. */
 int bfs_bc_accumulate_device(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *centrality,
 		void *stream);
 

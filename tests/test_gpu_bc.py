@@ -193,6 +193,7 @@ def test_bc_device_entry_points_match_host(native):
         assert d_dep.cpu().numpy().tobytes() == dep.tobytes()
         assert d_sig.cpu().numpy().view(np.uint32).tobytes() == sig.tobytes()
         srcs = c["sources"]
+        g.set_options(bc_batch=0)   # the device accumulation runs one source at a time
         host_bc, _ = g.betweenness(srcs)
         acc = torch.zeros(n, dtype=torch.float32, device="cuda")
         g.betweenness_device(srcs, acc.data_ptr(), stream)
