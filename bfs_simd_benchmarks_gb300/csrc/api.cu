@@ -112,6 +112,9 @@ struct bfs_graph {
 		float *dsum = nullptr;
 		float *delta = nullptr;      // [64][n] staging of host outputs (allocated when first asked for)
 		uint32_t *paths = nullptr;
+		uint32_t *blist = nullptr, *ilist = nullptr, *olist = nullptr;  // per-level work lists
+		uint32_t list_planes = 0;    // levels they have room for
+		std::vector<DevBuf> lbufs;
 		BbControl *ctl = nullptr;
 		BbControl *h_ctl = nullptr;  // pinned
 		MsControl *h_ms = nullptr;   // pinned: the traversal's control block
@@ -221,6 +224,8 @@ void release_bb(bfs_graph *g) {
 	auto &b = g->bb;
 	for (auto &x : b.bufs) cudaFree(x.p);
 	b.bufs.clear();
+	for (auto &x : b.lbufs) cudaFree(x.p);
+	b.lbufs.clear();
 	if (b.h_ctl) cudaFreeHost(b.h_ctl);
 	if (b.h_ms) cudaFreeHost(b.h_ms);
 	for (cudaEvent_t e : {b.e0, b.e1, b.e2, b.e3})
@@ -1229,6 +1234,27 @@ int bb_enqueue(bfs_graph *g, const uint32_t *sources, uint32_t ns, float *delta,
 	int rc = batch_prepare(g, 1, &planes);
 	if (rc) return rc;
 	auto &b = g->bb;
+	if (b.list_planes < planes) {
+		// per-level work lists for this many levels (the old ones may still be in use)
+		if (cudaStreamSynchronize(st) != cudaSuccess) return BFS_ECUDA;
+		for (auto &x : b.lbufs) cudaFree(x.p);
+		b.lbufs.clear();
+		b.list_planes = 0;
+		const size_t nblk = (g->n + 31) / 32;
+		const size_t sizes[3] = {planes * nblk, (size_t) planes * g->ms_nchunks, (size_t) planes * g->bb_noch};
+		uint32_t **dst[3] = {&b.blist, &b.ilist, &b.olist};
+		for (int i = 0; i < 3; ++i) {
+			void *p = nullptr;
+			const size_t bytes = std::max<size_t>(sizeof(uint32_t) * sizes[i], 16);
+			if (cudaMalloc(&p, bytes) != cudaSuccess) {
+				cudaGetLastError();
+				return BFS_ENOMEM;
+			}
+			b.lbufs.push_back({p, bytes});
+			*dst[i] = (uint32_t *) p;
+		}
+		b.list_planes = planes;
+	}
 	const MsArgs a = batch_args(g, 1, ns, planes);
 	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
 	if (cudaMemcpyAsync(b.d_sources, sources, sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, st) != cudaSuccess)
@@ -1255,6 +1281,10 @@ int bb_enqueue(bfs_graph *g, const uint32_t *sources, uint32_t ns, float *delta,
 	x.sigma = b.sigma;
 	x.dsum = b.dsum;
 	x.partial = b.partial;
+	x.blist = b.blist;
+	x.ilist = b.ilist;
+	x.olist = b.olist;
+	x.planes = b.list_planes;
 	x.ctl = b.ctl;
 	x.wait_limit_ns = wait_limit_ns(g->opt);
 	x.hold_barrier = g->opt.test_hold_barrier;
@@ -1300,8 +1330,18 @@ int bb_collect(bfs_graph *g, bfs_bc_stats *out) {
 		if (c.t[0] && c.t[1] >= c.t[0]) s.paths_ms = (float) ((c.t[1] - c.t[0]) * 1e-6);
 		if (c.t[1] && c.t[2] >= c.t[1]) s.dependencies_ms = (float) ((c.t[2] - c.t[1]) * 1e-6);
 		s.grid_ctas = (uint32_t) b.grid;
-		for (uint32_t d = 0; d < ms.depth && d < BFS_BC_TRACE_LEVELS && d < kMsTraceLevels; ++d)
+		for (uint32_t d = 0; d < ms.depth && d < BFS_BC_TRACE_LEVELS && d < kMsTraceLevels; ++d) {
 			s.level_vertices[d] = ms.frontier[d];
+			if (d >= kBbTraceLevels) continue;
+			if (d > 0 && c.t_fwd[d - 1] && c.t_fwd[d] >= c.t_fwd[d - 1])
+				s.level_paths_ms[d] = (float) ((c.t_fwd[d] - c.t_fwd[d - 1]) * 1e-6);
+			// the dependency sums of level d start where level d + 1 ended (the
+			// deepest level: where the path counts ended)
+			const bool deepest = d + 1 == ms.depth;
+			if (!deepest && d + 1 >= kBbTraceLevels) continue;
+			const unsigned long long r0 = deepest ? c.t[1] : c.t_rev[d + 1], r1 = c.t_rev[d];
+			if (r0 && r1 >= r0) s.level_dependencies_ms[d] = (float) ((r1 - r0) * 1e-6);
+		}
 		for (uint32_t i = 0; i < b.ns; ++i) s.source_reached[i] = c.reached[i];
 		*out = s;
 	}

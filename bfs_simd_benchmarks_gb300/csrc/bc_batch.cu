@@ -244,18 +244,14 @@ __device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, u
 // Chunk c (kBbChunk edges of a vertex with more than kBbBig edges) in one
 // level of a sweep: the sums of its edges into partial[c].
 template <bool kFwd>
-__device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, unsigned long long &edges,
-		unsigned long long &matched) {
+__device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, uint32_t v, uint64_t hv,
+		unsigned long long &edges, unsigned long long &matched) {
 	using D = BbDir<kFwd>;
 	using T = typename D::T;
 	const unsigned lane = lane_id();
-	const uint64_t *own = a.hist + (size_t) L * a.n;
 	const uint64_t *nb = a.hist + (size_t) (kFwd ? L - 1 : L + 1) * a.n;
-	const uint32_t *off = D::off(a), *adj = D::adj(a), *cv = D::chunk_v(a), *cb = D::chunk_beg(a);
+	const uint32_t *off = D::off(a), *adj = D::adj(a), *cb = D::chunk_beg(a);
 	{
-		const uint32_t v = __ldg(cv + c);
-		const uint64_t hv = bb_ldg64(own + v);
-		if (!hv) return;
 		const uint32_t beg = __ldg(cb + c), end = min(beg + kBbChunk, __ldg(off + v + 1));
 		T acc0 = T(0), acc1 = T(0);
 		for (uint32_t e0 = beg; has_nb && e0 < end; e0 += 32) {
@@ -291,31 +287,33 @@ __device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, u
 }
 
 // After the chunk sums of a level: each chunked vertex of that level adds its
-// chunks' partial rows in chunk order (by the warp that holds its first chunk).
+// chunks' partial rows in chunk order (by the warp that meets its first chunk
+// in the level's list).
 template <bool kFwd>
 __device__ void bb_finish(const BbArgs &a, uint32_t L) {
 	using D = BbDir<kFwd>;
 	using T = typename D::T;
-	const uint32_t nch = D::nchunks(a);
+	const uint32_t ncl = ld_volatile(kFwd ? &a.ctl->ni_at[L] : &a.ctl->no_at[L]);
+	const uint32_t *clist = (kFwd ? a.ilist : a.olist) + (size_t) L * D::nchunks(a);
 	const unsigned lane = lane_id();
 	const uint64_t *own = a.hist + (size_t) L * a.n;
 	const uint32_t *off = D::off(a), *cv = D::chunk_v(a), *cb = D::chunk_beg(a);
 	const uint32_t gwarp = blockIdx.x * kBbWarps + warp_id(), nwarps = gridDim.x * kBbWarps;
-	for (uint32_t c = gwarp; c < nch; c += nwarps) {
+	for (uint32_t i = gwarp; i < ncl; i += nwarps) {
+		const uint32_t c = __ldcg(clist + i);
 		const uint32_t v = __ldg(cv + c);
 		const uint32_t b0 = __ldg(off + v);
 		if (__ldg(cb + c) != b0) continue;
 		const uint64_t hv = bb_ldg64(own + v);
-		if (!hv) continue;
 		const uint32_t k = (__ldg(off + v + 1) - b0 + kBbChunk - 1) / kBbChunk;
 		const bool w0 = (hv >> lane) & 1ull, w1 = (hv >> (lane + 32)) & 1ull;
 		T acc0 = T(0), acc1 = T(0);
-		for (uint32_t i = 0; i < k; i += kBbUnroll) {
+		for (uint32_t i2 = 0; i2 < k; i2 += kBbUnroll) {
 			T x0[kBbUnroll], x1[kBbUnroll];
 #pragma unroll
 			for (int j = 0; j < kBbUnroll; ++j) {
-				const bool in = i + j < k;
-				const size_t row = (size_t) (c + i + j) * 64;
+				const bool in = i2 + j < k;
+				const size_t row = (size_t) (c + i2 + j) * 64;
 				x0[j] = in && w0 ? D::from_bits(ld_cg(a.partial + row + lane)) : T(0);
 				x1[j] = in && w1 ? D::from_bits(ld_cg(a.partial + row + lane + 32)) : T(0);
 			}
@@ -329,23 +327,81 @@ __device__ void bb_finish(const BbArgs &a, uint32_t L) {
 	}
 }
 
+// Lists, per level, of the blocks of 32 vertices and of the edge chunks
+// that have a vertex at that level, so that a level's work is only its own
+// (the planes are final once the traversal has ended).  A warp takes 32
+// consecutive blocks (lane j: block j) or 32 chunks; one atomic per warp and
+// level places them.
+__device__ void bb_lists(const BbArgs &a, uint32_t depth) {
+	BbControl *ctl = a.ctl;
+	const unsigned lane = lane_id();
+	const uint32_t gwarp = blockIdx.x * kBbWarps + warp_id(), nwarps = gridDim.x * kBbWarps;
+	const uint32_t nblk = (a.n + 31) / 32;
+	for (uint32_t wb = gwarp; wb * 32 < nblk; wb += nwarps) {
+		for (uint32_t L = 0; L < depth; ++L) {
+			const uint64_t *pl = a.hist + (size_t) L * a.n;
+			uint32_t act = 0;
+#pragma unroll 8
+			for (uint32_t j = 0; j < 32; ++j) {
+				const uint32_t v = (wb * 32 + j) * 32 + lane;
+				const uint64_t h = v < a.n ? bb_ldg64(pl + v) : 0ull;
+				if (__any_sync(kFull, h != 0ull)) act |= 1u << j;
+			}
+			if (!act) continue;
+			uint32_t base = 0;
+			if (lane == 0) base = atomicAdd(&ctl->nb_at[L], (unsigned) __popc(act));
+			base = __shfl_sync(kFull, base, 0);
+			if ((act >> lane) & 1u) a.blist[(size_t) L * nblk + base + __popc(act & lanemask_lt())] = wb * 32 + lane;
+		}
+	}
+	for (int dir = 0; dir < 2; ++dir) {
+		const uint32_t nch = dir ? a.noch : a.nich;
+		const uint32_t *cv = dir ? a.ochunk_v : a.ichunk_v;
+		uint32_t *list = dir ? a.olist : a.ilist;
+		unsigned *cnt = dir ? ctl->no_at : ctl->ni_at;
+		for (uint32_t c0 = gwarp * 32; c0 < nch; c0 += nwarps * 32) {
+			const uint32_t c = c0 + lane;
+			const uint32_t v = c < nch ? __ldg(cv + c) : 0u;
+			for (uint32_t L = 0; L < depth; ++L) {
+				const bool at = c < nch && bb_ldg64(a.hist + (size_t) L * a.n + v) != 0ull;
+				const uint32_t m = __ballot_sync(kFull, at);
+				if (!m) continue;
+				uint32_t base = 0;
+				if (lane == 0) base = atomicAdd(cnt + L, (unsigned) __popc(m));
+				base = __shfl_sync(kFull, base, 0);
+				if (at) list[(size_t) L * nch + base + __popc(m & lanemask_lt())] = c;
+			}
+		}
+	}
+}
+
 // One level of a sweep: the level's chunks, then its blocks of 32 vertices,
-// handed out one at a time through a counter (the cost of a block varies
-// with the edges of its vertices that serve a source; a fixed deal left warps
-// waiting at the level's barrier).  The next item is claimed while the
-// current one runs.
+// from the level's lists, handed out one at a time through a counter (the
+// cost of a block varies with the edges of its vertices that serve a source;
+// a fixed deal left warps waiting at the level's barrier).  The next item is
+// claimed while the current one runs.
 template <bool kFwd>
 __device__ void bb_level(const BbArgs &a, uint32_t L, bool has_nb, unsigned *counter, unsigned long long &edges,
 		unsigned long long &matched) {
-	const uint32_t nch = BbDir<kFwd>::nchunks(a);
-	const uint32_t items = nch + (a.n + 31) / 32;
+	using D = BbDir<kFwd>;
+	const uint32_t nblk = (a.n + 31) / 32;
+	const uint32_t ncl = ld_volatile(kFwd ? &a.ctl->ni_at[L] : &a.ctl->no_at[L]);
+	const uint32_t nbl = ld_volatile(&a.ctl->nb_at[L]);
+	const uint32_t *clist = (kFwd ? a.ilist : a.olist) + (size_t) L * D::nchunks(a);
+	const uint32_t *blist = a.blist + (size_t) L * nblk;
+	const uint32_t items = ncl + nbl;
 	const unsigned lane = lane_id();
 	uint32_t item = lane == 0 ? atomicAdd(counter, 1u) : 0u;
 	item = __shfl_sync(kFull, item, 0);
 	while (item < items) {
 		const uint32_t next = lane == 0 ? atomicAdd(counter, 1u) : 0u;
-		if (item < nch) bb_chunk<kFwd>(a, L, has_nb, item, edges, matched);
-		else bb_block<kFwd>(a, L, has_nb, item - nch, edges, matched);
+		if (item < ncl) {
+			const uint32_t c = __ldcg(clist + item);
+			const uint32_t v = __ldg(D::chunk_v(a) + c);
+			bb_chunk<kFwd>(a, L, has_nb, c, v, bb_ldg64(a.hist + (size_t) L * a.n + v), edges, matched);
+		} else {
+			bb_block<kFwd>(a, L, has_nb, __ldcg(blist + (item - ncl)), edges, matched);
+		}
 		item = __shfl_sync(kFull, next, 0);
 	}
 }
@@ -366,7 +422,7 @@ __global__ void __launch_bounds__(kBbThreads, 2) k_bc_batch(BbArgs a) {
 	const uint32_t base = *(const volatile unsigned *) &ms->stats.base;
 	const uint32_t spills = *(const volatile unsigned *) &ms->stats.spills;
 	const uint32_t depth = *(const volatile unsigned *) &ms->stats.depth;
-	if (ms_err || !complete || base || spills || depth == 0) {
+	if (ms_err || !complete || base || spills || depth == 0 || depth > a.planes) {
 		if (leader) ctl->err = ms_err ? ms_err : BFS_EUNSUPPORTED;
 		return;
 	}
@@ -380,25 +436,29 @@ __global__ void __launch_bounds__(kBbThreads, 2) k_bc_batch(BbArgs a) {
 			h &= h - 1ull;
 		}
 	}
+	bb_lists(a, depth);
 	bool ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
+	if (leader) ctl->t_fwd[0] = global_timer_ns();
 	unsigned long long ef = 0, mf = 0, er = 0, mr = 0;
 	for (uint32_t L = 1; ok && L < depth; ++L) {
 		bb_level<true>(a, L, true, &ctl->work[0][L], ef, mf);
-		if (a.nich) {
+		if (ld_volatile(&ctl->ni_at[L])) {
 			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 			bb_finish<true>(a, L);
 		}
 		ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
+		if (leader && L < kBbTraceLevels) ctl->t_fwd[L] = global_timer_ns();
 	}
 	if (leader) ctl->t[1] = global_timer_ns();
 	for (int L = (int) depth - 1; ok && L >= 0; --L) {
 		const bool has_nb = (uint32_t) L + 1 < depth;
 		bb_level<false>(a, (uint32_t) L, has_nb, &ctl->work[1][L], er, mr);
-		if (a.noch) {
+		if (ld_volatile(&ctl->no_at[L])) {
 			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 			bb_finish<false>(a, (uint32_t) L);
 		}
 		if (L > 0) ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
+		if (leader && (uint32_t) L < kBbTraceLevels) ctl->t_rev[L] = global_timer_ns();
 	}
 	if (leader) ctl->t[2] = global_timer_ns();
 	bb_add_counter(&ctl->edges_fwd, ef);

@@ -12,6 +12,7 @@ namespace bfsg {
 constexpr uint32_t kBbMaxSources = 64;       // one 64-bit word of sources per vertex
 constexpr uint32_t kBbBig = kMsPullBig;      // degree above which a vertex's edges are summed in chunks ...
 constexpr uint32_t kBbChunk = kMsChunk;      // ... of this many edges (the batched pull's in-edge chunks)
+constexpr uint32_t kBbTraceLevels = 64;      // per-level timers kept for the first levels
 
 struct BbControl {
 	unsigned bar[2];                 // grid barrier
@@ -22,8 +23,13 @@ struct BbControl {
 	unsigned long long matched_fwd;  // of which into the previous level for at least one source
 	unsigned long long matched_rev;  // ... into the next level
 	unsigned long long t[3];         // global timer: start, path counts done, dependencies done
+	unsigned long long t_fwd[kBbTraceLevels];  // end of the path counts of level d (d = 0: the seeds)
+	unsigned long long t_rev[kBbTraceLevels];  // end of the dependency sums of level d
 	unsigned int reached[kBbMaxSources];  // vertices reached from each source (output pass)
 	unsigned int work[2][kMsMaxLevel + 1];  // per sweep and level: next work item (chunks, then vertex blocks)
+	unsigned int nb_at[kMsMaxLevel + 1];    // per level: blocks of 32 vertices with a vertex at that level
+	unsigned int ni_at[kMsMaxLevel + 1];    // ... in-edge chunks whose vertex is at that level
+	unsigned int no_at[kMsMaxLevel + 1];    // ... out-edge chunks
 };
 
 struct BbArgs {
@@ -40,6 +46,11 @@ struct BbArgs {
 	uint32_t *sigma;                   // [n][64] path counts (mod 2^32)
 	float *dsum;                       // [n][64] 1/sigma + the dependency sums of the next level
 	uint32_t *partial;                 // [max(nich, noch)][64] chunk sums (value bits)
+	// per level L < planes, built at the start of the launch (any order):
+	uint32_t *blist;                   // [planes][ceil(n / 32)] blocks of 32 vertices with a vertex at level L
+	uint32_t *ilist;                   // [planes][nich] in-edge chunks of vertices at level L
+	uint32_t *olist;                   // [planes][noch] out-edge chunks of vertices at level L
+	uint32_t planes;                   // levels the lists have room for
 	BbControl *ctl;
 	unsigned long long wait_limit_ns;  // bound of every grid-barrier wait
 	uint32_t hold_barrier;             // tests: CTA 0 skips its arrival at this barrier (0 = off)
