@@ -526,6 +526,86 @@ def bench_bc(args, torch, dev, g, sources, flush, arr=None):
     return out
 
 
+def bench_bc_batch(args, torch, dev, g, sources, flush, arr=None):
+    """Batched betweenness (bfs_bc_run_batch_device): 64 sources from one
+    bit-sliced traversal and one path-count / dependency launch over all of
+    them.  GTEPS = sum of m(s) / device time, L2 flushed before each batch;
+    e2e through bfs_bc_accumulate over the same sources (centrality to host
+    memory), against the per-source loop of bench_bc."""
+    n = g.num_vertices
+    srcs = np.asarray(sources[:64], np.uint32)
+    k = int(srcs.size)
+    stream = torch.cuda.Stream(device=dev)
+    dep = torch.empty((k, n), dtype=torch.float32, device=dev)
+
+    def one(i):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
+        g.bc_batch_device(srcs, dep.data_ptr(), 0, stream.cuda_stream)
+        st = g.bc_stats()
+        if st["status"] != 0 or st["batched_sources"] != k:
+            raise RuntimeError(f"batched betweenness status {st['status']}, batched {st['batched_sources']}")
+        return st
+
+    for i in range(max(1, args.warmup)):
+        one(i)
+    torch.cuda.synchronize()
+    sts = [one(i) for i in range(args.steps)]
+    dev_ms = statistics.mean(st["device_ms"] for st in sts)
+    trav_ms = statistics.mean(st["traversal_ms"] for st in sts)
+    kern_ms = statistics.mean(st["paths_ms"] + st["dependencies_ms"] for st in sts)
+    st0 = sts[0]
+    edges = st0["edges_reached"]
+    reached_pairs = sum(st0["source_reached"])
+    depth = st0["depth"]
+    # algorithmic bytes of k_bc_batch: per edge read its neighbour id and the
+    # neighbour's level word (12 B); per (edge, source) pair summed the
+    # neighbour's value (4 B); per reached (vertex, source) pair the path count
+    # written, read back and the dependency sum written (12 B); every level's
+    # plane read twice (16 B per vertex and level)
+    alg = (12 * (st0["edges_forward"] + st0["edges_reverse"]) + 4 * (st0["pairs_forward"] + st0["pairs_reverse"]) +
+           12 * reached_pairs + 16 * n * (depth + 1))
+    peak, _ = peaks()
+    ach = alg / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
+    traffic = ncu_traffic("pokec_bc_batch", "dram_bytes_per_launch")
+    # e2e: centrality over the same sources to host memory
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cent, ast = g.betweenness(srcs)
+    e2e_s = time.perf_counter() - t0
+    out = {
+        "what": "betweenness of 64 sources at once on the bit-sliced traversal (path counts + dependency sums for "
+                "every (vertex, source) pair)",
+        "sources": k, "steps": args.steps,
+        "gteps": edges / (dev_ms / 1e3) / 1e9,
+        "ms_per_batch": dev_ms, "ms_per_source": dev_ms / k,
+        "traversal_ms": trav_ms, "kernel_ms": kern_ms, "output_ms": dev_ms - trav_ms - kern_ms,
+        "phase_ms_mean": {x: statistics.mean(st[x] for st in sts) for x in ("paths_ms", "dependencies_ms")},
+        "depth": depth,
+        "edges_read": {"forward": st0["edges_forward"], "reverse": st0["edges_reverse"]},
+        "edges_serving_a_source": st0["edges_matched_forward"],
+        "edge_source_pairs": st0["pairs_forward"],
+        "example_levels": {x: st0[x] for x in ("level_vertices", "level_paths_ms", "level_dependencies_ms")},
+        "roofline": {"kernel": "k_bc_batch", "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": ach / peak if peak else None, "algorithmic_bytes_per_launch": alg,
+                     "traffic": traffic},
+        "e2e": {"value": ast["edges_reached"] / e2e_s / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": 4 * k,
+                "d2h_bytes_per_step": 4 * n, "note": "bfs_bc_accumulate(): 64 sources, centrality to host memory"},
+        "gpu_launches": 3,
+    }
+    if arr is not None:
+        from oracle import oracle as O
+        d, p, _ = g.bc_batch(srcs[:8])
+        ok = 0
+        for i in (0, 7):
+            osig, odep, _, oscale = O.bc_single(arr, int(srcs[i]))
+            ok += int(np.array_equal(p[i], osig) and
+                      bool((np.abs(d[i].astype(np.float64) - odep) <= 1e-4 * (np.abs(oscale) + 1)).all()))
+        out["parity"] = (f"{ok}/2 sources of a batch: path counts bit-exact, dependencies within 1e-4 x (scale + 1) "
+                         "of the oracle")
+    return out
+
+
 def bench_serving(args, torch, dev):
     """The serving loop: 8 resident R-MAT graphs (scales 14, 16, 18-23, edge
     factor 16) under a 40 GB HBM admission budget; open-loop Poisson arrivals
@@ -880,6 +960,7 @@ def main():
         # betweenness runs on the caller's ids (a degree-ordered layout refuses it)
         bc_g = B.Graph.from_edges(wl.n, src, dst, W, S, device_build=True) if degree_order else g
         bc = bench_bc(args, torch, dev, bc_g, sources, flush, bc_arr)
+        bc["batched"] = bench_bc_batch(args, torch, dev, bc_g, sources, flush, bc_arr)
         if bc_g is not g:
             bc_g.close()
     if args.large != "none" and world == 1:

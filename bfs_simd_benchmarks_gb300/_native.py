@@ -115,6 +115,8 @@ class BcStats(C.Structure):
         ("fallback_sources", C.c_uint32),
         ("edges_matched_forward", C.c_uint64),
         ("edges_matched_reverse", C.c_uint64),
+        ("pairs_forward", C.c_uint64),
+        ("pairs_reverse", C.c_uint64),
         ("source_reached", C.c_uint32 * BFS_BC_BATCH_MAX_SOURCES),
     ]
 

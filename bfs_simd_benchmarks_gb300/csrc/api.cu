@@ -1318,10 +1318,12 @@ int bb_collect(bfs_graph *g, bfs_bc_stats *out) {
 		s.reached = c.reached[b.ns - 1];
 		s.status = (uint32_t) c.err;
 		s.edges_reached = ms.traversed;
-		s.edges_forward = c.edges_fwd;
-		s.edges_reverse = c.edges_rev;
-		s.edges_matched_forward = c.matched_fwd;
-		s.edges_matched_reverse = c.matched_rev;
+		s.edges_forward = c.fwd[0];
+		s.edges_reverse = c.rev[0];
+		s.edges_matched_forward = c.fwd[1];
+		s.edges_matched_reverse = c.rev[1];
+		s.pairs_forward = c.fwd[2];
+		s.pairs_reverse = c.rev[2];
 		float ms_all = 0, tms = 0;
 		cudaEventElapsedTime(&ms_all, b.e0, b.e3);
 		cudaEventElapsedTime(&tms, b.e0, b.e1);
@@ -1357,6 +1359,8 @@ void bc_stats_add(bfs_bc_stats &total, const bfs_bc_stats &one) {
 	total.edges_reverse += one.edges_reverse;
 	total.edges_matched_forward += one.edges_matched_forward;
 	total.edges_matched_reverse += one.edges_matched_reverse;
+	total.pairs_forward += one.pairs_forward;
+	total.pairs_reverse += one.pairs_reverse;
 	total.traversal_ms += one.traversal_ms;
 	total.sort_ms += one.sort_ms;
 	total.paths_ms += one.paths_ms;

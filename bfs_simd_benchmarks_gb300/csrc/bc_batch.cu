@@ -54,6 +54,12 @@ __device__ __forceinline__ uint64_t bb_shfl64(uint64_t x, int src) {
 }
 __device__ __forceinline__ uint64_t bb_ldg64(const uint64_t *p) { return __ldg((const unsigned long long *) p); }
 
+// A warp's counts over a sweep: edges read (lane 0), edges that serve a
+// source (lane 0), and (edge, source) pairs summed (every lane its own edges).
+struct BbCount {
+	unsigned long long edges, matched, served;
+};
+
 // The two sweeps: forward reads in-edges and path counts, reverse reads
 // out-edges and dependency sums.
 template <bool kFwd> struct BbDir;
@@ -147,8 +153,7 @@ __device__ __forceinline__ void bb_take(const BbArgs &a, uint32_t &bal, uint32_t
 // exists (the reverse sweep's deepest level has none; its vertices get
 // 1/sigma alone).
 template <bool kFwd>
-__device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, unsigned long long &edges,
-		unsigned long long &matched) {
+__device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, BbCount &cnt) {
 	using D = BbDir<kFwd>;
 	using T = typename D::T;
 	const unsigned lane = lane_id();
@@ -194,9 +199,10 @@ __device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, u
 			}
 			uint32_t bal = __ballot_sync(kFull, m != 0ull);
 			if (lane == 0) {
-				edges += min(32u, total - e0);
-				matched += __popc(bal);
+				cnt.edges += min(32u, total - e0);
+				cnt.matched += __popc(bal);
 			}
+			cnt.served += __popcll(m);
 			while (bal) {
 				T x0[kBbUnroll], x1[kBbUnroll];
 				uint32_t oo[kBbUnroll];
@@ -245,7 +251,7 @@ __device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, u
 // level of a sweep: the sums of its edges into partial[c].
 template <bool kFwd>
 __device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, uint32_t v, uint64_t hv,
-		unsigned long long &edges, unsigned long long &matched) {
+		BbCount &cnt) {
 	using D = BbDir<kFwd>;
 	using T = typename D::T;
 	const unsigned lane = lane_id();
@@ -264,9 +270,10 @@ __device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, u
 			}
 			uint32_t bal = __ballot_sync(kFull, m != 0ull);
 			if (lane == 0) {
-				edges += min(32u, end - e0);
-				matched += __popc(bal);
+				cnt.edges += min(32u, end - e0);
+				cnt.matched += __popc(bal);
 			}
+			cnt.served += __popcll(m);
 			while (bal) {
 				T x0[kBbUnroll], x1[kBbUnroll];
 				uint32_t oo[kBbUnroll];
@@ -381,8 +388,7 @@ __device__ void bb_lists(const BbArgs &a, uint32_t depth) {
 // a fixed deal left warps waiting at the level's barrier).  The next item is
 // claimed while the current one runs.
 template <bool kFwd>
-__device__ void bb_level(const BbArgs &a, uint32_t L, bool has_nb, unsigned *counter, unsigned long long &edges,
-		unsigned long long &matched) {
+__device__ void bb_level(const BbArgs &a, uint32_t L, bool has_nb, unsigned *counter, BbCount &cnt) {
 	using D = BbDir<kFwd>;
 	const uint32_t nblk = (a.n + 31) / 32;
 	const uint32_t ncl = ld_volatile(kFwd ? &a.ctl->ni_at[L] : &a.ctl->no_at[L]);
@@ -398,16 +404,21 @@ __device__ void bb_level(const BbArgs &a, uint32_t L, bool has_nb, unsigned *cou
 		if (item < ncl) {
 			const uint32_t c = __ldcg(clist + item);
 			const uint32_t v = __ldg(D::chunk_v(a) + c);
-			bb_chunk<kFwd>(a, L, has_nb, c, v, bb_ldg64(a.hist + (size_t) L * a.n + v), edges, matched);
+			bb_chunk<kFwd>(a, L, has_nb, c, v, bb_ldg64(a.hist + (size_t) L * a.n + v), cnt);
 		} else {
-			bb_block<kFwd>(a, L, has_nb, __ldcg(blist + (item - ncl)), edges, matched);
+			bb_block<kFwd>(a, L, has_nb, __ldcg(blist + (item - ncl)), cnt);
 		}
 		item = __shfl_sync(kFull, next, 0);
 	}
 }
 
-__device__ __forceinline__ void bb_add_counter(unsigned long long *dst, unsigned long long x) {
-	if (lane_id() == 0 && x) atomicAdd(dst, x);
+__device__ __forceinline__ void bb_add_counts(unsigned long long *dst, const BbCount &c) {
+	const unsigned long long served = warp_sum(c.served);
+	if (lane_id() == 0) {
+		if (c.edges) atomicAdd(dst, c.edges);
+		if (c.matched) atomicAdd(dst + 1, c.matched);
+		if (served) atomicAdd(dst + 2, served);
+	}
 }
 
 __global__ void __launch_bounds__(kBbThreads, 2) k_bc_batch(BbArgs a) {
@@ -439,9 +450,9 @@ __global__ void __launch_bounds__(kBbThreads, 2) k_bc_batch(BbArgs a) {
 	bb_lists(a, depth);
 	bool ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier);
 	if (leader) ctl->t_fwd[0] = global_timer_ns();
-	unsigned long long ef = 0, mf = 0, er = 0, mr = 0;
+	BbCount cf{0, 0, 0}, cr{0, 0, 0};
 	for (uint32_t L = 1; ok && L < depth; ++L) {
-		bb_level<true>(a, L, true, &ctl->work[0][L], ef, mf);
+		bb_level<true>(a, L, true, &ctl->work[0][L], cf);
 		if (ld_volatile(&ctl->ni_at[L])) {
 			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 			bb_finish<true>(a, L);
@@ -452,7 +463,7 @@ __global__ void __launch_bounds__(kBbThreads, 2) k_bc_batch(BbArgs a) {
 	if (leader) ctl->t[1] = global_timer_ns();
 	for (int L = (int) depth - 1; ok && L >= 0; --L) {
 		const bool has_nb = (uint32_t) L + 1 < depth;
-		bb_level<false>(a, (uint32_t) L, has_nb, &ctl->work[1][L], er, mr);
+		bb_level<false>(a, (uint32_t) L, has_nb, &ctl->work[1][L], cr);
 		if (ld_volatile(&ctl->no_at[L])) {
 			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 			bb_finish<false>(a, (uint32_t) L);
@@ -461,10 +472,8 @@ __global__ void __launch_bounds__(kBbThreads, 2) k_bc_batch(BbArgs a) {
 		if (leader && (uint32_t) L < kBbTraceLevels) ctl->t_rev[L] = global_timer_ns();
 	}
 	if (leader) ctl->t[2] = global_timer_ns();
-	bb_add_counter(&ctl->edges_fwd, ef);
-	bb_add_counter(&ctl->matched_fwd, mf);
-	bb_add_counter(&ctl->edges_rev, er);
-	bb_add_counter(&ctl->matched_rev, mr);
+	bb_add_counts(ctl->fwd, cf);
+	bb_add_counts(ctl->rev, cr);
 }
 
 // Output pass: [v][64] rows -> dependencies and path counts [source][v]

@@ -18,10 +18,10 @@ struct BbControl {
 	unsigned bar[2];                 // grid barrier
 	int err;                         // BFS_* status (0 ok)
 	uint32_t depth;                  // levels of the traversal (deepest level + 1)
-	unsigned long long edges_fwd;    // in-edges read by the path-count sweeps
-	unsigned long long edges_rev;    // out-edges read by the dependency sweeps
-	unsigned long long matched_fwd;  // of which into the previous level for at least one source
-	unsigned long long matched_rev;  // ... into the next level
+	// path-count sweeps (in-edges) / dependency sweeps (out-edges): edges read,
+	// of which serving at least one source, and (edge, source) pairs summed
+	unsigned long long fwd[3];
+	unsigned long long rev[3];
 	unsigned long long t[3];         // global timer: start, path counts done, dependencies done
 	unsigned long long t_fwd[kBbTraceLevels];  // end of the path counts of level d (d = 0: the seeds)
 	unsigned long long t_rev[kBbTraceLevels];  // end of the dependency sums of level d

@@ -522,6 +522,8 @@ typedef struct bfs_bc_stats {
 	                               the batch's level planes */
 	uint64_t edges_matched_forward;  /* edges read by the path-count sweeps that serve at least one source */
 	uint64_t edges_matched_reverse;  /* ... by the dependency sweeps */
+	uint64_t pairs_forward;          /* (edge, source) pairs summed by the path-count sweeps */
+	uint64_t pairs_reverse;          /* ... by the dependency sweeps */
 	uint32_t source_reached[64];     /* the last batch: vertices reached from each of its sources */
 } bfs_bc_stats;
 

@@ -83,6 +83,11 @@ def test_bc_batch_rmat_64_sources_with_hubs(native, oracle):
         dep, sig, st = g.bc_batch(sources)
         assert st["status"] == 0 and st["batched_sources"] == 64
         assert st["edges_matched_forward"] <= st["edges_forward"]
+        assert st["edges_matched_forward"] == st["edges_matched_reverse"]
+        # (edge, source) pairs summed = the shortest-path DAG edges of every source
+        lev = [oracle.bfs_levels(arr, int(x)) for x in sources]
+        dag = sum(int(((lv[src] >= 0) & (lv[dst] == lv[src] + 1)).sum()) for lv in lev)
+        assert st["pairs_forward"] == dag and st["pairs_reverse"] == dag
         _check_rows(oracle, arr, sources, dep, sig, st)
         # the duplicate's rows equal the original's
         assert dep[61].tobytes() == dep[3].tobytes() and sig[61].tobytes() == sig[3].tobytes()
