@@ -21,15 +21,18 @@
 //   reverse, L = depth-1 .. 0:
 //     dsum[v][s] = (sum of dsum[w][s] over out-edges v -> w, s in hist[L][v] & hist[L+1][w])
 //                  + 1 / sigma[v][s].
-// Per level a warp screens 32 consecutive vertices and walks the concatenated
-// edge lists of those at that level, 32 edges per step (each edge's vertex
-// found by a binary search over the warp's degree prefix); an edge's source
-// mask is one AND.  The edges with a non-empty mask are then taken in edge
-// order, four at a time, each a coalesced read of the neighbour's row by the
-// lanes whose bit is set.  Vertices with more than kBbBig edges in the
-// sweep's direction are cut into kBbChunk-edge chunks that warps all over the
-// grid sum; the partial rows are added in chunk order after a grid barrier.
-// Every sum has a fixed order, so repeated runs give identical bits.
+// The launch first lists, per level, the blocks of 32 consecutive vertices
+// and the edge chunks that have a vertex at that level; a level then hands
+// its list items to warps one at a time through a counter.  A warp takes a
+// block and walks the concatenated edge lists of its vertices at that level,
+// 32 edges per step (each edge's vertex found by a binary search over the
+// warp's degree prefix); an edge's source mask is one AND.  The edges with a
+// non-empty mask are then taken in edge order, four at a time, each a
+// coalesced read of the neighbour's row by the lanes whose bit is set.
+// Vertices with more than kBbBig edges in the sweep's direction are cut into
+// kBbChunk-edge chunks, one list item each; the partial rows are added in
+// chunk order after a grid barrier.  Every sum has a fixed order, so repeated
+// runs give identical bits.
 // The output pass (its own launch) turns the [v][64] rows into [source][v]
 // rows through a shared-memory transpose, 0 for unreached pairs, and/or adds
 // each vertex's dependencies into an accumulator in source order.
@@ -160,90 +163,88 @@ __device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, B
 	const uint64_t *own = a.hist + (size_t) L * a.n;
 	const uint64_t *nb = a.hist + (size_t) (kFwd ? L - 1 : L + 1) * a.n;
 	const uint32_t *off = D::off(a), *adj = D::adj(a);
-	{
-		const uint32_t vb = b * 32, v = vb + lane;
-		const uint64_t hv = v < a.n ? bb_ldg64(own + v) : 0ull;
-		uint32_t beg = 0, end = 0;
-		if (hv) {
-			beg = __ldg(off + v);
-			end = __ldg(off + v + 1);
+	const uint32_t vb = b * 32, v = vb + lane;
+	const uint64_t hv = v < a.n ? bb_ldg64(own + v) : 0ull;
+	uint32_t beg = 0, end = 0;
+	if (hv) {
+		beg = __ldg(off + v);
+		end = __ldg(off + v + 1);
+	}
+	const bool part = hv != 0ull && end - beg <= kBbBig;
+	const uint32_t pm = __ballot_sync(kFull, part);
+	if (!pm) return;
+	const uint32_t d = part && has_nb ? end - beg : 0u;
+	const uint32_t incl = warp_incl_scan(d);
+	const uint32_t excl = incl - d;
+	const uint32_t total = __shfl_sync(kFull, incl, 31);
+	int cur = -1;
+	T acc0 = T(0), acc1 = T(0);
+	uint64_t hcur = 0;
+	BbPre pcur{0u, 0u};
+	uint32_t flushed = 0;
+	for (uint32_t e0 = 0; e0 < total; e0 += 32) {
+		const uint32_t e = e0 + lane;
+		// the edge's vertex slot: the first lane whose inclusive prefix exceeds e
+		uint32_t o = 0;
+#pragma unroll
+		for (uint32_t s = 16; s; s >>= 1) {
+			const uint32_t x = __shfl_sync(kFull, incl, o + s - 1);
+			if (x <= e) o += s;
 		}
-		const bool part = hv != 0ull && end - beg <= kBbBig;
-		const uint32_t pm = __ballot_sync(kFull, part);
-		if (!pm) return;
-		const uint32_t d = part && has_nb ? end - beg : 0u;
-		const uint32_t incl = warp_incl_scan(d);
-		const uint32_t excl = incl - d;
-		const uint32_t total = __shfl_sync(kFull, incl, 31);
-		int cur = -1;
-		T acc0 = T(0), acc1 = T(0);
-		uint64_t hcur = 0;
-		BbPre pcur{0u, 0u};
-		uint32_t flushed = 0;
-		for (uint32_t e0 = 0; e0 < total; e0 += 32) {
-			const uint32_t e = e0 + lane;
-			// the edge's vertex slot: the first lane whose inclusive prefix exceeds e
-			uint32_t o = 0;
+		const uint32_t obeg = __shfl_sync(kFull, beg, o), oex = __shfl_sync(kFull, excl, o);
+		const uint64_t ohv = bb_shfl64(hv, o);
+		uint32_t u = 0;
+		uint64_t m = 0;
+		if (e < total) {
+			u = __ldg(adj + obeg + (e - oex));
+			m = ohv & bb_ldg64(nb + u);
+		}
+		uint32_t bal = __ballot_sync(kFull, m != 0ull);
+		if (lane == 0) {
+			cnt.edges += min(32u, total - e0);
+			cnt.matched += __popc(bal);
+		}
+		cnt.served += __popcll(m);
+		while (bal) {
+			T x0[kBbUnroll], x1[kBbUnroll];
+			uint32_t oo[kBbUnroll];
+			int took;
+			bb_take<kFwd>(a, bal, u, m, o, x0, x1, oo, &took);
 #pragma unroll
-			for (uint32_t s = 16; s; s >>= 1) {
-				const uint32_t x = __shfl_sync(kFull, incl, o + s - 1);
-				if (x <= e) o += s;
-			}
-			const uint32_t obeg = __shfl_sync(kFull, beg, o), oex = __shfl_sync(kFull, excl, o);
-			const uint64_t ohv = bb_shfl64(hv, o);
-			uint32_t u = 0;
-			uint64_t m = 0;
-			if (e < total) {
-				u = __ldg(adj + obeg + (e - oex));
-				m = ohv & bb_ldg64(nb + u);
-			}
-			uint32_t bal = __ballot_sync(kFull, m != 0ull);
-			if (lane == 0) {
-				cnt.edges += min(32u, total - e0);
-				cnt.matched += __popc(bal);
-			}
-			cnt.served += __popcll(m);
-			while (bal) {
-				T x0[kBbUnroll], x1[kBbUnroll];
-				uint32_t oo[kBbUnroll];
-				int cnt;
-				bb_take<kFwd>(a, bal, u, m, o, x0, x1, oo, &cnt);
-#pragma unroll
-				for (int k = 0; k < kBbUnroll; ++k) {
-					if (k >= cnt) break;
-					if ((int) oo[k] != cur) {
-						if (cur >= 0) {
-							bb_flush<kFwd>(a, vb + cur, hcur, acc0, acc1, pcur);
-							flushed |= 1u << cur;
-						}
-						cur = (int) oo[k];
-						hcur = bb_shfl64(hv, cur);
-						pcur = bb_pre<kFwd>(a, vb + cur, hcur);
-						acc0 = T(0);
-						acc1 = T(0);
+			for (int k = 0; k < kBbUnroll; ++k) {
+				if (k >= took) break;
+				if ((int) oo[k] != cur) {
+					if (cur >= 0) {
+						bb_flush<kFwd>(a, vb + cur, hcur, acc0, acc1, pcur);
+						flushed |= 1u << cur;
 					}
-					acc0 += x0[k];
-					acc1 += x1[k];
+					cur = (int) oo[k];
+					hcur = bb_shfl64(hv, cur);
+					pcur = bb_pre<kFwd>(a, vb + cur, hcur);
+					acc0 = T(0);
+					acc1 = T(0);
 				}
+				acc0 += x0[k];
+				acc1 += x1[k];
 			}
 		}
-		if (cur >= 0) {
-			bb_flush<kFwd>(a, vb + cur, hcur, acc0, acc1, pcur);
-			flushed |= 1u << cur;
-		}
-		// vertices none of whose edges serve their sources (the deepest level,
-		// sinks of the reverse sweep): nothing to add; two at a time, loads first
-		for (uint32_t r = pm & ~flushed; r;) {
-			const int j0 = __ffs(r) - 1;
-			r &= r - 1u;
-			const int j1 = r ? __ffs(r) - 1 : -1;
-			if (r) r &= r - 1u;
-			const uint64_t h0 = bb_shfl64(hv, j0), h1 = bb_shfl64(hv, j1 < 0 ? 0 : j1);
-			const BbPre p0 = bb_pre<kFwd>(a, vb + j0, h0);
-			const BbPre p1 = j1 >= 0 ? bb_pre<kFwd>(a, vb + j1, h1) : BbPre{0u, 0u};
-			bb_flush<kFwd>(a, vb + j0, h0, T(0), T(0), p0);
-			if (j1 >= 0) bb_flush<kFwd>(a, vb + j1, h1, T(0), T(0), p1);
-		}
+	}
+	if (cur >= 0) {
+		bb_flush<kFwd>(a, vb + cur, hcur, acc0, acc1, pcur);
+		flushed |= 1u << cur;
+	}
+	// vertices none of whose edges serve their sources (the deepest level,
+	// sinks of the reverse sweep): nothing to add; two at a time, loads first
+	for (uint32_t r = pm & ~flushed; r;) {
+		const int j0 = __ffs(r) - 1;
+		r &= r - 1u;
+		const int j1 = r ? __ffs(r) - 1 : -1;
+		if (r) r &= r - 1u;
+		const uint64_t h0 = bb_shfl64(hv, j0), h1 = bb_shfl64(hv, j1 < 0 ? 0 : j1);
+		const BbPre p0 = bb_pre<kFwd>(a, vb + j0, h0);
+		const BbPre p1 = j1 >= 0 ? bb_pre<kFwd>(a, vb + j1, h1) : BbPre{0u, 0u};
+		bb_flush<kFwd>(a, vb + j0, h0, T(0), T(0), p0);
+		if (j1 >= 0) bb_flush<kFwd>(a, vb + j1, h1, T(0), T(0), p1);
 	}
 }
 
@@ -257,40 +258,38 @@ __device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, u
 	const unsigned lane = lane_id();
 	const uint64_t *nb = a.hist + (size_t) (kFwd ? L - 1 : L + 1) * a.n;
 	const uint32_t *off = D::off(a), *adj = D::adj(a), *cb = D::chunk_beg(a);
-	{
-		const uint32_t beg = __ldg(cb + c), end = min(beg + kBbChunk, __ldg(off + v + 1));
-		T acc0 = T(0), acc1 = T(0);
-		for (uint32_t e0 = beg; has_nb && e0 < end; e0 += 32) {
-			const uint32_t e = e0 + lane;
-			uint32_t u = 0;
-			uint64_t m = 0;
-			if (e < end) {
-				u = __ldg(adj + e);
-				m = hv & bb_ldg64(nb + u);
-			}
-			uint32_t bal = __ballot_sync(kFull, m != 0ull);
-			if (lane == 0) {
-				cnt.edges += min(32u, end - e0);
-				cnt.matched += __popc(bal);
-			}
-			cnt.served += __popcll(m);
-			while (bal) {
-				T x0[kBbUnroll], x1[kBbUnroll];
-				uint32_t oo[kBbUnroll];
-				int cnt;
-				bb_take<kFwd>(a, bal, u, m, 0u, x0, x1, oo, &cnt);
+	const uint32_t beg = __ldg(cb + c), end = min(beg + kBbChunk, __ldg(off + v + 1));
+	T acc0 = T(0), acc1 = T(0);
+	for (uint32_t e0 = beg; has_nb && e0 < end; e0 += 32) {
+		const uint32_t e = e0 + lane;
+		uint32_t u = 0;
+		uint64_t m = 0;
+		if (e < end) {
+			u = __ldg(adj + e);
+			m = hv & bb_ldg64(nb + u);
+		}
+		uint32_t bal = __ballot_sync(kFull, m != 0ull);
+		if (lane == 0) {
+			cnt.edges += min(32u, end - e0);
+			cnt.matched += __popc(bal);
+		}
+		cnt.served += __popcll(m);
+		while (bal) {
+			T x0[kBbUnroll], x1[kBbUnroll];
+			uint32_t oo[kBbUnroll];
+			int took;
+			bb_take<kFwd>(a, bal, u, m, 0u, x0, x1, oo, &took);
 #pragma unroll
-				for (int k = 0; k < kBbUnroll; ++k) {
-					if (k >= cnt) break;
-					acc0 += x0[k];
-					acc1 += x1[k];
-				}
+			for (int k = 0; k < kBbUnroll; ++k) {
+				if (k >= took) break;
+				acc0 += x0[k];
+				acc1 += x1[k];
 			}
 		}
-		const size_t row = (size_t) c * 64;
-		if ((hv >> lane) & 1ull) a.partial[row + lane] = D::to_bits(acc0);
-		if ((hv >> (lane + 32)) & 1ull) a.partial[row + lane + 32] = D::to_bits(acc1);
 	}
+	const size_t row = (size_t) c * 64;
+	if ((hv >> lane) & 1ull) a.partial[row + lane] = D::to_bits(acc0);
+	if ((hv >> (lane + 32)) & 1ull) a.partial[row + lane + 32] = D::to_bits(acc1);
 }
 
 // After the chunk sums of a level: each chunked vertex of that level adds its
