@@ -48,7 +48,8 @@ namespace {
 
 constexpr int kBbThreads = 512;
 constexpr int kBbWarps = kBbThreads / 32;
-constexpr int kBbUnroll = 4;
+constexpr int kBbUnroll = 4;   // chunk partial rows added per round (finish)
+constexpr int kBbPairs = 2;    // pairs of served edges per round (their rows loaded together)
 constexpr uint32_t kBbOutV = 64;   // output pass: vertices per tile
 constexpr int kBbOutThreads = 256;
 
@@ -73,7 +74,7 @@ template <> struct BbDir<true> {
 	static __device__ __forceinline__ const uint32_t *chunk_v(const BbArgs &a) { return a.ichunk_v; }
 	static __device__ __forceinline__ const uint32_t *chunk_beg(const BbArgs &a) { return a.ichunk_beg; }
 	static __device__ __forceinline__ uint32_t nchunks(const BbArgs &a) { return a.nich; }
-	static __device__ __forceinline__ T load(const BbArgs &a, size_t i) { return __ldcg(a.sigma + i); }
+	static __device__ __forceinline__ const T *vals(const BbArgs &a) { return a.sigma; }
 	static __device__ __forceinline__ T from_bits(uint32_t b) { return b; }
 	static __device__ __forceinline__ uint32_t to_bits(T x) { return x; }
 	static __device__ __forceinline__ uint32_t pre(const BbArgs &, size_t, bool) { return 0u; }
@@ -86,7 +87,7 @@ template <> struct BbDir<false> {
 	static __device__ __forceinline__ const uint32_t *chunk_v(const BbArgs &a) { return a.ochunk_v; }
 	static __device__ __forceinline__ const uint32_t *chunk_beg(const BbArgs &a) { return a.ochunk_beg; }
 	static __device__ __forceinline__ uint32_t nchunks(const BbArgs &a) { return a.noch; }
-	static __device__ __forceinline__ T load(const BbArgs &a, size_t i) { return __ldcg(a.dsum + i); }
+	static __device__ __forceinline__ const T *vals(const BbArgs &a) { return a.dsum; }
 	static __device__ __forceinline__ T from_bits(uint32_t b) { return __uint_as_float(b); }
 	static __device__ __forceinline__ uint32_t to_bits(T x) { return __float_as_uint(x); }
 	// the vertex's path count, loaded when the vertex's first edge is taken so
@@ -124,31 +125,116 @@ __device__ __forceinline__ void bb_flush(const BbArgs &a, uint32_t v, uint64_t h
 	if ((hv >> (lane + 32)) & 1ull) BbDir<kFwd>::store(a, row + lane + 32, acc1, pre.p1);
 }
 
-// The next (up to) kBbUnroll edges of `bal` (lanes holding edges with a
-// non-empty source mask), lowest lane first: their neighbours' row entries for
-// this lane's two sources (0 where the edge does not serve the source) and
-// their vertex slots.  `bal` is warp-uniform; *cnt gets the edges taken.
-template <bool kFwd>
-__device__ __forceinline__ void bb_take(const BbArgs &a, uint32_t &bal, uint32_t u, uint64_t m, uint32_t slot,
-		typename BbDir<kFwd>::T (&x0)[kBbUnroll], typename BbDir<kFwd>::T (&x1)[kBbUnroll],
-		uint32_t (&oo)[kBbUnroll], int *cnt) {
-	using T = typename BbDir<kFwd>::T;
-	const unsigned lane = lane_id();
-	int c = 0;
+// ---- half-warp sums over the edges that serve a source -------------------
+// Lane 16h + i (half h) holds sources 4i .. 4i+3 of a row: 16 bytes, one
+// load.  The served edges of a step are taken two at a time in edge order,
+// the first by half 0 and the second by half 1, so that one round reads two
+// rows; a vertex's sum is its half-0 sum plus its half-1 sum (one xor
+// shuffle), written by half 0.
+
+template <class T> __device__ __forceinline__ T bb_as(uint32_t b);
+template <> __device__ __forceinline__ uint32_t bb_as<uint32_t>(uint32_t b) { return b; }
+template <> __device__ __forceinline__ float bb_as<float>(uint32_t b) { return __uint_as_float(b); }
+
+__device__ __forceinline__ uint32_t bb_quad() { return 4u * (lane_id() & 15u); }  // this lane's first source
+
+// The open vertex's sums for this lane's 4 sources and (reverse sweep, half 0)
+// its path counts for them, loaded when it is opened.
+template <bool kFwd> struct BbOpen {
+	typename BbDir<kFwd>::T acc[4];
+	uint32_t pre[4];
+};
+
+template <bool kFwd> __device__ __forceinline__ void bb_open(const BbArgs &a, uint32_t v, uint64_t h, BbOpen<kFwd> &o) {
 #pragma unroll
-	for (int k = 0; k < kBbUnroll; ++k) {
-		const bool ok = bal != 0u;
-		const int j = ok ? __ffs(bal) - 1 : 0;
-		bal &= bal - 1u;
-		const uint32_t uj = __shfl_sync(kFull, u, j);
-		const uint64_t mj = ok ? bb_shfl64(m, j) : 0ull;
-		oo[k] = __shfl_sync(kFull, slot, j);
-		c += ok ? 1 : 0;
-		const size_t row = (size_t) uj * 64;
-		x0[k] = ((mj >> lane) & 1ull) ? BbDir<kFwd>::load(a, row + lane) : T(0);
-		x1[k] = ((mj >> (lane + 32)) & 1ull) ? BbDir<kFwd>::load(a, row + lane + 32) : T(0);
+	for (int i = 0; i < 4; ++i) o.acc[i] = typename BbDir<kFwd>::T(0);
+	if (!kFwd && lane_id() < 16u && ((h >> bb_quad()) & 0xFull)) {
+		const uint4 p = __ldcg(reinterpret_cast<const uint4 *>(a.sigma + (size_t) v * 64 + bb_quad()));
+		o.pre[0] = p.x;
+		o.pre[1] = p.y;
+		o.pre[2] = p.z;
+		o.pre[3] = p.w;
 	}
-	*cnt = c;
+}
+
+// Adds the halves and writes the open vertex's sums for its sources h.
+template <bool kFwd> __device__ __forceinline__ void bb_close(const BbArgs &a, uint32_t v, uint64_t h, BbOpen<kFwd> &o) {
+#pragma unroll
+	for (int i = 0; i < 4; ++i) o.acc[i] += __shfl_xor_sync(kFull, o.acc[i], 16);
+	const uint32_t bits = (uint32_t) (h >> bb_quad()) & 0xFu;
+	if (lane_id() < 16u && bits) {
+		const size_t row = (size_t) v * 64 + bb_quad();
+#pragma unroll
+		for (int i = 0; i < 4; ++i)
+			if ((bits >> i) & 1u) BbDir<kFwd>::store(a, row + i, o.acc[i], o.pre[i]);
+	}
+}
+
+// This half's edge: the neighbour's row entries for this lane's 4 sources
+// where the edge serves them (mask m), else 0.
+template <bool kFwd>
+__device__ __forceinline__ void bb_vals(const BbArgs &a, uint32_t u, uint64_t m, typename BbDir<kFwd>::T (&x)[4]) {
+	using T = typename BbDir<kFwd>::T;
+	const uint32_t sb = (uint32_t) (m >> bb_quad()) & 0xFu;
+#pragma unroll
+	for (int i = 0; i < 4; ++i) x[i] = T(0);
+	if (sb) {
+		const uint4 r = __ldcg(reinterpret_cast<const uint4 *>(BbDir<kFwd>::vals(a) + (size_t) u * 64 + bb_quad()));
+		x[0] = (sb & 1u) ? bb_as<T>(r.x) : T(0);
+		x[1] = (sb & 2u) ? bb_as<T>(r.y) : T(0);
+		x[2] = (sb & 4u) ? bb_as<T>(r.z) : T(0);
+		x[3] = (sb & 8u) ? bb_as<T>(r.w) : T(0);
+	}
+}
+
+// The next one or two served edges of `bal` (warp-uniform): lane's half
+// takes the first (half 0) or the second (half 1); *j0 / *j1 get their lanes
+// (*j1 = *j0 when there is one).
+__device__ __forceinline__ void bb_pair(uint32_t &bal, uint32_t u, uint64_t m, uint32_t *uj, uint64_t *mj, int *j0,
+		int *j1) {
+	*j0 = __ffs(bal) - 1;
+	bal &= bal - 1u;
+	const bool two = bal != 0u;
+	*j1 = two ? __ffs(bal) - 1 : *j0;
+	bal &= bal - 1u;
+	const int jm = (lane_id() & 16u) ? *j1 : *j0;
+	*uj = __shfl_sync(kFull, u, jm);
+	const uint64_t mm = bb_shfl64(m, jm);
+	*mj = ((lane_id() & 16u) && !two) ? 0ull : mm;
+}
+
+// Adds a pair of served edges (vertex slots oa <= ob, this half's values x)
+// to the open vertex, closing it and opening the next where the slot changes.
+template <bool kFwd>
+__device__ __forceinline__ void bb_add_pair(const BbArgs &a, uint32_t vb, uint64_t hv, int oa, int ob,
+		const typename BbDir<kFwd>::T (&x)[4], int &cur, uint64_t &hcur, BbOpen<kFwd> &op, uint32_t &flushed) {
+	const bool h1 = lane_id() & 16u;
+	if (oa != cur) {
+		if (cur >= 0) {
+			bb_close<kFwd>(a, vb + cur, hcur, op);
+			flushed |= 1u << cur;
+		}
+		cur = oa;
+		hcur = bb_shfl64(hv, cur);
+		bb_open<kFwd>(a, vb + cur, hcur, op);
+	}
+	if (ob == oa) {
+#pragma unroll
+		for (int i = 0; i < 4; ++i) op.acc[i] += x[i];
+		return;
+	}
+	// the pair straddles two vertices: half 0's edge ends the open one
+	if (!h1)
+#pragma unroll
+		for (int i = 0; i < 4; ++i) op.acc[i] += x[i];
+	bb_close<kFwd>(a, vb + cur, hcur, op);
+	flushed |= 1u << cur;
+	cur = ob;
+	hcur = bb_shfl64(hv, cur);
+	bb_open<kFwd>(a, vb + cur, hcur, op);
+	if (h1)
+#pragma unroll
+		for (int i = 0; i < 4; ++i) op.acc[i] += x[i];
 }
 
 // Block b of 32 consecutive vertices in one level of a sweep: those with at
@@ -177,10 +263,9 @@ __device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, B
 	const uint32_t incl = warp_incl_scan(d);
 	const uint32_t excl = incl - d;
 	const uint32_t total = __shfl_sync(kFull, incl, 31);
-	int cur = -1;
-	T acc0 = T(0), acc1 = T(0);
+	int cur = -1;          // the open vertex's slot (warp-uniform)
 	uint64_t hcur = 0;
-	BbPre pcur{0u, 0u};
+	BbOpen<kFwd> op;
 	uint32_t flushed = 0;
 	for (uint32_t e0 = 0; e0 < total; e0 += 32) {
 		const uint32_t e = e0 + lane;
@@ -206,45 +291,59 @@ __device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, B
 		}
 		cnt.served += __popcll(m);
 		while (bal) {
-			T x0[kBbUnroll], x1[kBbUnroll];
-			uint32_t oo[kBbUnroll];
-			int took;
-			bb_take<kFwd>(a, bal, u, m, o, x0, x1, oo, &took);
+			// kBbPairs pairs per round: their rows' loads in flight together
+			uint32_t uj[kBbPairs];
+			uint64_t mj[kBbPairs];
+			int oa[kBbPairs], ob[kBbPairs];
+			bool has[kBbPairs];
 #pragma unroll
-			for (int k = 0; k < kBbUnroll; ++k) {
-				if (k >= took) break;
-				if ((int) oo[k] != cur) {
-					if (cur >= 0) {
-						bb_flush<kFwd>(a, vb + cur, hcur, acc0, acc1, pcur);
-						flushed |= 1u << cur;
-					}
-					cur = (int) oo[k];
-					hcur = bb_shfl64(hv, cur);
-					pcur = bb_pre<kFwd>(a, vb + cur, hcur);
-					acc0 = T(0);
-					acc1 = T(0);
-				}
-				acc0 += x0[k];
-				acc1 += x1[k];
+			for (int p = 0; p < kBbPairs; ++p) {
+				int j0 = 0, j1 = 0;
+				uj[p] = 0;
+				mj[p] = 0;
+				has[p] = bal != 0u;
+				if (has[p]) bb_pair(bal, u, m, &uj[p], &mj[p], &j0, &j1);
+				oa[p] = __shfl_sync(kFull, (int) o, j0);
+				ob[p] = __shfl_sync(kFull, (int) o, j1);
 			}
+			T x[kBbPairs][4];
+#pragma unroll
+			for (int p = 0; p < kBbPairs; ++p) bb_vals<kFwd>(a, uj[p], mj[p], x[p]);
+#pragma unroll
+			for (int p = 0; p < kBbPairs; ++p)
+				if (has[p]) bb_add_pair<kFwd>(a, vb, hv, oa[p], ob[p], x[p], cur, hcur, op, flushed);
 		}
 	}
 	if (cur >= 0) {
-		bb_flush<kFwd>(a, vb + cur, hcur, acc0, acc1, pcur);
+		bb_close<kFwd>(a, vb + cur, hcur, op);
 		flushed |= 1u << cur;
 	}
 	// vertices none of whose edges serve their sources (the deepest level,
-	// sinks of the reverse sweep): nothing to add; two at a time, loads first
+	// sinks of the reverse sweep): nothing to add; two at a time, one per half
 	for (uint32_t r = pm & ~flushed; r;) {
 		const int j0 = __ffs(r) - 1;
 		r &= r - 1u;
 		const int j1 = r ? __ffs(r) - 1 : -1;
 		if (r) r &= r - 1u;
-		const uint64_t h0 = bb_shfl64(hv, j0), h1 = bb_shfl64(hv, j1 < 0 ? 0 : j1);
-		const BbPre p0 = bb_pre<kFwd>(a, vb + j0, h0);
-		const BbPre p1 = j1 >= 0 ? bb_pre<kFwd>(a, vb + j1, h1) : BbPre{0u, 0u};
-		bb_flush<kFwd>(a, vb + j0, h0, T(0), T(0), p0);
-		if (j1 >= 0) bb_flush<kFwd>(a, vb + j1, h1, T(0), T(0), p1);
+		const int jm = (lane & 16u) ? j1 : j0;
+		const uint64_t hj = bb_shfl64(hv, jm < 0 ? 0 : jm);
+		if (jm >= 0) {
+			const uint32_t bits = (uint32_t) (hj >> bb_quad()) & 0xFu;
+			if (bits) {
+				const size_t row = (size_t) (vb + jm) * 64 + bb_quad();
+				uint32_t pre[4] = {0u, 0u, 0u, 0u};
+				if (!kFwd) {
+					const uint4 p = __ldcg(reinterpret_cast<const uint4 *>(a.sigma + row));
+					pre[0] = p.x;
+					pre[1] = p.y;
+					pre[2] = p.z;
+					pre[3] = p.w;
+				}
+#pragma unroll
+				for (int i = 0; i < 4; ++i)
+					if ((bits >> i) & 1u) D::store(a, row + i, T(0), pre[i]);
+			}
+		}
 	}
 }
 
@@ -259,7 +358,7 @@ __device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, u
 	const uint64_t *nb = a.hist + (size_t) (kFwd ? L - 1 : L + 1) * a.n;
 	const uint32_t *off = D::off(a), *adj = D::adj(a), *cb = D::chunk_beg(a);
 	const uint32_t beg = __ldg(cb + c), end = min(beg + kBbChunk, __ldg(off + v + 1));
-	T acc0 = T(0), acc1 = T(0);
+	T acc[4] = {T(0), T(0), T(0), T(0)};
 	for (uint32_t e0 = beg; has_nb && e0 < end; e0 += 32) {
 		const uint32_t e = e0 + lane;
 		uint32_t u = 0;
@@ -275,21 +374,33 @@ __device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, u
 		}
 		cnt.served += __popcll(m);
 		while (bal) {
-			T x0[kBbUnroll], x1[kBbUnroll];
-			uint32_t oo[kBbUnroll];
-			int took;
-			bb_take<kFwd>(a, bal, u, m, 0u, x0, x1, oo, &took);
+			uint32_t uj[kBbPairs];
+			uint64_t mj[kBbPairs];
 #pragma unroll
-			for (int k = 0; k < kBbUnroll; ++k) {
-				if (k >= took) break;
-				acc0 += x0[k];
-				acc1 += x1[k];
+			for (int p = 0; p < kBbPairs; ++p) {
+				int j0, j1;
+				uj[p] = 0;
+				mj[p] = 0;
+				if (bal) bb_pair(bal, u, m, &uj[p], &mj[p], &j0, &j1);
 			}
+			T x[kBbPairs][4];
+#pragma unroll
+			for (int p = 0; p < kBbPairs; ++p) bb_vals<kFwd>(a, uj[p], mj[p], x[p]);
+#pragma unroll
+			for (int p = 0; p < kBbPairs; ++p)
+#pragma unroll
+				for (int i = 0; i < 4; ++i) acc[i] += x[p][i];
 		}
 	}
-	const size_t row = (size_t) c * 64;
-	if ((hv >> lane) & 1ull) a.partial[row + lane] = D::to_bits(acc0);
-	if ((hv >> (lane + 32)) & 1ull) a.partial[row + lane + 32] = D::to_bits(acc1);
+#pragma unroll
+	for (int i = 0; i < 4; ++i) acc[i] += __shfl_xor_sync(kFull, acc[i], 16);
+	const uint32_t bits = (uint32_t) (hv >> bb_quad()) & 0xFu;
+	if (lane < 16u && bits) {
+		const size_t row = (size_t) c * 64 + bb_quad();
+#pragma unroll
+		for (int i = 0; i < 4; ++i)
+			if ((bits >> i) & 1u) a.partial[row + i] = D::to_bits(acc[i]);
+	}
 }
 
 // After the chunk sums of a level: each chunked vertex of that level adds its
