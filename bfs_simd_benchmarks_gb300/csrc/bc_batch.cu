@@ -604,15 +604,24 @@ __global__ void __launch_bounds__(kBbOutThreads) k_bc_batch_out(BbArgs a, BbOut 
 		__syncthreads();
 		if (t < nv) svis[t] = bb_ldg64(a.vis + v0 + t) & smask;
 		__syncthreads();
-		for (uint32_t i = t; i < nv * 64; i += blockDim.x) {
-			const uint32_t j = i / 64, s = i % 64;
-			const bool r = (svis[j] >> s) & 1ull;
-			const size_t x = (size_t) v0 * 64 + i;
-			const uint32_t sg = r ? a.sigma[x] : 0u;
-			const float dv = r ? a.dsum[x] : 0.0f;
-			const float inv = sg ? 1.0f / (float) (int) sg : 0.0f;
-			sd[j][s] = inv != 0.0f ? (dv - inv) / inv : 0.0f;
-			sp[j][s] = sg;
+		// 16-byte loads: 4 sources of a row per thread (streamed, not kept in L2)
+		for (uint32_t i = t; i < nv * 16; i += blockDim.x) {
+			const uint32_t j = i / 16, s0 = 4 * (i % 16);
+			const uint32_t r = (uint32_t) (svis[j] >> s0) & 0xFu;
+			uint4 sg4 = make_uint4(0u, 0u, 0u, 0u), dv4 = make_uint4(0u, 0u, 0u, 0u);
+			if (r) {
+				const size_t x = (size_t) (v0 + j) * 64 + s0;
+				sg4 = __ldcs(reinterpret_cast<const uint4 *>(a.sigma + x));
+				dv4 = __ldcs(reinterpret_cast<const uint4 *>(a.dsum + x));
+			}
+			const uint32_t sg[4] = {sg4.x, sg4.y, sg4.z, sg4.w}, dv[4] = {dv4.x, dv4.y, dv4.z, dv4.w};
+#pragma unroll
+			for (int k = 0; k < 4; ++k) {
+				const uint32_t g = ((r >> k) & 1u) ? sg[k] : 0u;
+				const float inv = g ? 1.0f / (float) (int) g : 0.0f;
+				sd[j][s0 + k] = inv != 0.0f ? (__uint_as_float(dv[k]) - inv) / inv : 0.0f;
+				sp[j][s0 + k] = g;
+			}
 		}
 		__syncthreads();
 		if (o.delta || o.paths)
@@ -620,8 +629,8 @@ __global__ void __launch_bounds__(kBbOutThreads) k_bc_batch_out(BbArgs a, BbOut 
 				const uint32_t s = i / kBbOutV, j = i % kBbOutV;
 				if (j >= nv) continue;
 				const size_t x = (size_t) s * a.n + v0 + j;
-				if (o.delta) o.delta[x] = sd[j][s];
-				if (o.paths) o.paths[x] = sp[j][s];
+				if (o.delta) __stcs(o.delta + x, sd[j][s]);
+				if (o.paths) __stcs(o.paths + x, sp[j][s]);
 			}
 		if (o.acc && t < nv) {
 			const uint32_t v = v0 + t;
@@ -653,7 +662,11 @@ int bb_launch(const BbArgs &a, const BbOut &o, int num_sms, cudaStream_t st, int
 	if (cudaLaunchCooperativeKernel((const void *) k_bc_batch, dim3(g), dim3(kBbThreads), args, 0, st) != cudaSuccess)
 		return BFS_ECUDA;
 	if (between && cudaEventRecord(between, st) != cudaSuccess) return BFS_ECUDA;
-	k_bc_batch_out<<<num_sms * 4, kBbOutThreads, 0, st>>>(a, o);
+	int out_per_sm = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&out_per_sm, k_bc_batch_out, kBbOutThreads, 0) != cudaSuccess ||
+			out_per_sm < 1)
+		return BFS_ECUDA;
+	k_bc_batch_out<<<num_sms * out_per_sm, kBbOutThreads, 0, st>>>(a, o);
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }
 
