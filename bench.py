@@ -934,6 +934,28 @@ def main():
     e2e_s = time.perf_counter() - t0
     e2e_value = e2e_edges / e2e_s / 1e9
 
+    # both bottom-up variants on the same graph and options: one pass over the sources each
+    # (the streamed one is the reference's dense step: packed tiles through bulk copies)
+    variants = {}
+    base_bu = g.get_options()["bottom_up"]
+    for name, bu in (("pull", N.BFS_BU_PULL), ("stream", N.BFS_BU_STREAM)):
+        try:
+            g.set_options(bottom_up=bu)
+            for s in sources[:4]:
+                traverse(int(s), None)
+            tv = []
+            for s in sources:
+                traverse(int(s), tv)
+        except N.BfsError as e:
+            variants[name] = {"error": str(e)}
+            continue
+        vms = sum(a.elapsed_time(b) for a, b, _ in tv)
+        variants[name] = {"gteps": sum(st["edges_traversed"] for _, _, st in tv) / (vms / 1e3) / 1e9,
+                          "ms_per_traversal": vms / len(tv),
+                          "dense_steps_mean": statistics.mean(st["dense_steps"] for _, _, st in tv),
+                          "dense_ms_mean": statistics.mean(st["dense_ms"] for _, _, st in tv)}
+    g.set_options(bottom_up=base_bu)
+
     batched = None
     if args.batch_workload != "none" and world == 1:
         same = args.batch_workload == args.workload
@@ -979,6 +1001,7 @@ def main():
                            "layout_search": shape_tune,
                            "graph_device_bytes": info["device_bytes"], "grid_ctas": timed[0][2]["grid_ctas"],
                            "column_groups": info["num_groups"], "autotune": tuned,
+                           "bottom_up_variants": variants,
                            "graph_build_s": round(t_gen, 2)},
             "single_source": {"gteps": value, "ms_per_traversal_mean": statistics.mean(trav_ms),
                               "ms_per_traversal_p50": statistics.median(trav_ms),
