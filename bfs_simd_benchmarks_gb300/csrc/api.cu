@@ -178,6 +178,41 @@ __global__ void k_unrelabel(uint32_t n, const uint32_t *new_of_old, const uint32
 	}
 }
 
+// Device array -> host memory the device can write (pinned and mapped):
+// 16-byte stores when both ends are 16-byte aligned, else 4-byte ones.
+__global__ void k_to_host(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, size_t words, bool wide) {
+	const size_t t0 = (size_t) blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t) gridDim.x * blockDim.x;
+	if (wide) {
+		const size_t q = words / 4;
+		for (size_t i = t0; i < q; i += stride)
+			reinterpret_cast<uint4 *>(dst)[i] = __ldcs(reinterpret_cast<const uint4 *>(src) + i);
+		for (size_t i = 4 * q + t0; i < words; i += stride) dst[i] = __ldcs(src + i);
+	} else {
+		for (size_t i = t0; i < words; i += stride) dst[i] = __ldcs(src + i);
+	}
+}
+
+// Enqueues the copy of `words` 32-bit words from device memory to a host
+// buffer on `st`: pinned host memory mapped into the device's address space
+// is written by a copy kernel (no copy-engine round trip), any other host
+// memory goes through cudaMemcpyAsync.
+int enqueue_to_host(uint32_t *dst, const uint32_t *src, size_t words, int num_sms, cudaStream_t st) {
+	if (!dst || !words) return BFS_OK;
+	cudaPointerAttributes at{};
+	if (cudaPointerGetAttributes(&at, dst) != cudaSuccess) {
+		cudaGetLastError();
+		at.type = cudaMemoryTypeUnregistered;
+	}
+	if (at.type == cudaMemoryTypeHost && at.devicePointer) {
+		uint32_t *d = (uint32_t *) at.devicePointer;
+		const bool wide = ((uintptr_t) d % 16) == 0 && ((uintptr_t) src % 16) == 0;
+		k_to_host<<<num_sms * 4, 256, 0, st>>>(src, d, words, wide);
+		return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
+	}
+	return cudaMemcpyAsync(dst, src, sizeof(uint32_t) * words, cudaMemcpyDeviceToHost, st) == cudaSuccess ? BFS_OK
+																										: BFS_ECUDA;
+}
+
 template <class T> int dev_alloc(bfs_graph *g, T **out, size_t count) {
 	size_t bytes = std::max<size_t>(sizeof(T) * count, 16);
 	void *p = nullptr;
@@ -1812,15 +1847,22 @@ int bfs_get_options(const bfs_graph *g, bfs_options *opt) {
 int bfs_run(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, bfs_stats *stats) {
 	if (!g) return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);
-	int st = run_impl(g, source, g->level_buf, g->parent_buf, 0);
+	int st = run_impl(g, source, g->level_buf, parents ? g->parent_buf : nullptr, 0);
 	if (st) return st;
-	st = collect_stats(g, stats);
-	if (st) return st;
-	if (levels && cudaMemcpy(levels, g->level_buf, sizeof(int32_t) * g->n, cudaMemcpyDeviceToHost) != cudaSuccess)
-		return BFS_ECUDA;
-	if (parents && cudaMemcpy(parents, g->parent_buf, sizeof(uint32_t) * g->n, cudaMemcpyDeviceToHost) != cudaSuccess)
-		return BFS_ECUDA;
-	return BFS_OK;
+	// the outputs' and the statistics' copies are queued behind the
+	// traversal, then one wait
+	if ((st = enqueue_to_host((uint32_t *) levels, (const uint32_t *) g->level_buf, g->n, g->num_sms, 0)) ||
+			(st = enqueue_to_host(parents, g->parent_buf, g->n, g->num_sms, 0)))
+		return st;
+	static_assert(sizeof(DevStats) % 4 == 0, "the statistics are copied as 32-bit words");
+	if (stats && !g->stepwise_last) {
+		if ((st = enqueue_to_host((uint32_t *) g->h_stats, (const uint32_t *) g->rc.stats, sizeof(DevStats) / 4,
+					 g->num_sms, 0)))
+			return st;
+		if (cudaStreamSynchronize(0) != cudaSuccess) return BFS_ECUDA;
+		g->stats_fresh = true;
+	}
+	return collect_stats(g, stats);
 }
 
 int bfs_run_device(bfs_graph *g, uint32_t source, int32_t *levels, uint32_t *parents, void *stream) {

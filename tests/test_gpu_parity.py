@@ -329,3 +329,44 @@ def test_bfs_order_matches_vertex_id_remap(native, oracle, name, tmp_path):
     host = open(base + "_reorder", "rb").read()
     B.tool_vertex_remap(base, device=True)
     assert open(base + "_reorder", "rb").read() == host
+
+
+def test_bfs_run_into_pinned_host_memory(native, oracle):
+    """bfs_run with pinned (device-mapped) host buffers: the outputs are written
+    by a copy kernel instead of a copy-engine transfer; 16-byte aligned and
+    4-byte aligned destinations, with and without parents, and pageable
+    buffers for comparison."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    import bfs_simd_benchmarks_gb300 as B
+    from bfs_simd_benchmarks_gb300 import _native as N
+    n = (1 << 15) + 3
+    src, dst = B.gen_rmat(n, 16 * n, seed=71, permute=True)
+    arr = oracle.csr_arrays(n, src, dst)
+    lib = N.load()
+    with B.Graph.from_edges(n, src, dst, 1024, 16) as g:
+        sources = B.pick_sources(g.degrees(), 3, seed=2)
+        lev_p = torch.full((n + 4,), 7, dtype=torch.int32).pin_memory()
+        par_p = torch.full((n + 4,), 7, dtype=torch.int32).pin_memory()
+        for off in (0, 1, 3):
+            for with_parents in (True, False):
+                s = int(sources[off % 3])
+                lev_p.fill_(7)
+                par_p.fill_(7)
+                st = N.Stats()
+                lp = C.cast(lev_p.data_ptr() + 4 * off, C.POINTER(C.c_int32))
+                pp = C.cast(par_p.data_ptr() + 4 * off, C.POINTER(C.c_uint32)) if with_parents else None
+                N.check(lib.bfs_run(g.handle, s, lp, pp, C.byref(st)), "bfs_run")
+                lev = lev_p.numpy()[off:off + n].copy()
+                np.testing.assert_array_equal(lev, oracle.bfs_levels(arr, s))
+                # nothing written outside the destination
+                assert (lev_p.numpy()[:off] == 7).all() and (lev_p.numpy()[off + n:] == 7).all()
+                if with_parents:
+                    par = par_p.numpy()[off:off + n].view(np.uint32).copy()
+                    assert oracle.check_parents(arr, s, lev, par) == 0
+                else:
+                    assert (par_p.numpy() == 7).all()
+                assert st.status == 0 and st.reached == int((lev >= 0).sum())
+        # pageable buffers through the same call
+        lev2, par2, _ = g.run(int(sources[0]))
+        np.testing.assert_array_equal(lev2, oracle.bfs_levels(arr, int(sources[0])))

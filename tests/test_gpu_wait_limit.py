@@ -63,6 +63,30 @@ def test_batched_wait_runs_out_then_recovers(native, oracle, hold):
             np.testing.assert_array_equal(rows[i], np.where(ref < 0, 255, ref).astype(np.uint8))
 
 
+@pytest.mark.parametrize("hold", [1, 2])
+def test_batched_betweenness_wait_runs_out_then_recovers(native, oracle, hold):
+    """The batched betweenness call (its traversal and its own launch share the
+    option): the status comes back through bfs_bc_run_batch, and the next call
+    gives the oracle's values."""
+    import bfs_simd_benchmarks_gb300 as B
+    from conftest import bc_close
+    n, src, dst = _graph(B)
+    arr = oracle.csr_arrays(n, src, dst)
+    with B.Graph.from_edges(n, src, dst, 256, 4) as g:
+        sources = B.pick_sources(g.degrees(), 8, seed=8).astype(np.uint32)
+        g.set_options(wait_limit_us=1000, test_hold_barrier=hold)
+        with pytest.raises(B.BfsError) as e:
+            g.bc_batch(sources)
+        assert e.value.status == BFS_ETIMEOUT
+        g.set_options(wait_limit_us=0, test_hold_barrier=0)
+        dep, sig, st = g.bc_batch(sources)
+        assert st["status"] == 0 and st["batched_sources"] == sources.size
+        for i in (0, 7):
+            osig, odep, _, oscale = oracle.bc_single(arr, int(sources[i]))
+            np.testing.assert_array_equal(sig[i], osig)
+            assert bc_close(dep[i], odep, oscale).all()
+
+
 def test_wait_limit_option_round_trips(native):
     import bfs_simd_benchmarks_gb300 as B
     n, src, dst = _graph(B)
