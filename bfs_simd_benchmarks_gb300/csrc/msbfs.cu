@@ -48,8 +48,8 @@ constexpr uint32_t kLaneMaxDeg = 32;    // ... destinations of at most this in-d
 constexpr uint32_t kGroupMaxWords = 8;  // pull: up to this many words, in-neighbour rows in lane groups
 constexpr uint32_t kEmitV = 128;        // output tile: 128 vertices x 4 words (256 sources)
 constexpr uint32_t kEmitW = 4;
-constexpr uint32_t kEmitStride = 132;   // shared row stride in bytes (33 words: column writes spread over banks)
-constexpr uint32_t kEmitBytes = kEmitW * 64 * kEmitStride;
+constexpr uint32_t kEmitRow = kEmitV + 4;  // shared row of one source quad, in words (16-byte aligned rows)
+constexpr uint32_t kEmitBytes = (kEmitW * 16 * kEmitRow + 16) * 4;  // the rows and the nibble table
 
 __device__ __forceinline__ uint64_t ld_cg64(const uint64_t *p) { return __ldcg((const unsigned long long *) p); }
 __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
@@ -622,20 +622,64 @@ __device__ void ms_pull_chunks_finish(const MsArgs &a, uint32_t lvl, uint64_t *n
 }
 
 // Planes [first, last] (levels base + p) -> uint8 levels [source][vertex].
-// A CTA of 512 threads takes tiles of 128 vertices x 4 words (256 sources);
-// thread (vertex, word) -- a warp holds 32 consecutive vertices of one word
-// -- builds the 64 level bytes of its word's sources in 16 registers: for
-// every plane whose word mask says the word is non-zero it loads the word and,
-// four sources at a time, spreads the 4 bits into a byte mask (two integer
-// multiplies) and writes the plane's level under it.  A byte starts at 255
-// and is written at most once (a source reaches a vertex at one level), so
-// "write" is an XOR with 255 ^ level.  The bytes go to a shared tile
-// [source][vertex] (lanes store consecutive bytes) and leave as 128-byte
-// rows.  `merge` combines with the bytes already in `levels` (a later
-// segment of a traversal deeper than the planes) by a byte-wise minimum:
-// every byte is below 255 in at most one segment.
+// A CTA of 512 threads takes tiles of 128 vertices x 4 words (256 sources).
+// 1. thread (vertex, word) -- a warp holds 32 consecutive vertices of one
+//    word -- builds the 64 level bytes of its word's sources in 16 registers:
+//    for every plane whose word mask says the word is non-zero it loads the
+//    word and, four sources at a time, looks the nibble up in a 16-entry
+//    shared table of byte masks and writes the plane's level under it.  A
+//    byte starts at 255 and is written at most once (a source reaches a vertex
+//    at one level), so "write" is an XOR with 255 ^ level.  The 16 words go to
+//    shared memory as [word][source quad][vertex].
+// 2. thread (word, source quad, 16 vertices) reads its 16 words with 16-byte
+//    loads, transposes them 4 x 4 bytes at a time (byte permutes) into the
+//    16-byte pieces of its 4 source rows and stores those.
+// `merge` combines with the bytes already in `levels` (a later segment of a
+// traversal deeper than the planes) by a byte-wise minimum: every byte is
+// below 255 in at most one segment.
 __device__ __forceinline__ uint32_t nibble_bytes(uint32_t nib) {
 	return ((nib * 0x00204081u) & 0x01010101u) * 0xFFu;  // bit i -> byte i all ones
+}
+
+// 16 level bytes (x, vertices in order) -> levels at dst, cnt <= 16 of them,
+// with the widest store the address allows.
+__device__ __forceinline__ void emit_piece(uint8_t *dst, const uint32_t (&x)[4], uint32_t cnt, bool merge) {
+	const uintptr_t al = (uintptr_t) dst;
+	if (cnt == 16 && (al & 15) == 0) {
+		uint4 y = make_uint4(x[0], x[1], x[2], x[3]);
+		if (merge) {
+			const uint4 old = __ldcg((const uint4 *) dst);
+			y.x = __vminu4(y.x, old.x);
+			y.y = __vminu4(y.y, old.y);
+			y.z = __vminu4(y.z, old.z);
+			y.w = __vminu4(y.w, old.w);
+		}
+		*(uint4 *) dst = y;
+	} else if (cnt == 16 && (al & 3) == 0) {
+#pragma unroll
+		for (int q = 0; q < 4; ++q) {
+			uint32_t y = x[q];
+			if (merge) y = __vminu4(y, __ldcg((const unsigned int *) dst + q));
+			((uint32_t *) dst)[q] = y;
+		}
+	} else if (cnt == 16 && (al & 1) == 0) {
+#pragma unroll
+		for (int q = 0; q < 8; ++q) {
+			uint32_t y = (x[q / 2] >> (16 * (q & 1))) & 0xFFFFu;
+			if (merge) {
+				const uint32_t old = __ldcg((const unsigned short *) dst + q);
+				y = __vminu4(y | 0xFFFF0000u, old | 0xFFFF0000u) & 0xFFFFu;
+			}
+			((uint16_t *) dst)[q] = (uint16_t) y;
+		}
+	} else {
+#pragma unroll
+		for (uint32_t b = 0; b < 16; ++b) {
+			if (b >= cnt) break;
+			const uint8_t y = (uint8_t) (x[b / 4] >> (8 * (b & 3)));
+			dst[b] = merge ? min(y, ld_cg_u8(dst + b)) : y;
+		}
+	}
 }
 
 __device__ __noinline__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t ns, uint32_t base, uint32_t first, uint32_t last,
@@ -645,6 +689,12 @@ __device__ __noinline__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t 
 	const uint32_t vtiles = (n + kEmitV - 1) / kEmitV, wtiles = (K + kEmitW - 1) / kEmitW;
 	const uint32_t vi = threadIdx.x % kEmitV, wi = threadIdx.x / kEmitV;
 	const size_t pstride = (size_t) n * K;
+	uint32_t *sw = reinterpret_cast<uint32_t *>(lev);  // [wi * 16 + quad][kEmitRow]
+	uint32_t *lut = sw + kEmitW * 16 * kEmitRow;       // nibble -> byte mask
+	if (threadIdx.x < 16) lut[threadIdx.x] = nibble_bytes(threadIdx.x);
+	// phase 2's item: rows of source quad rq (word rq / 16), vertices 16 cc ...
+	const uint32_t rq = threadIdx.x / (kEmitV / 16), cc = threadIdx.x % (kEmitV / 16);
+	__syncthreads();
 	for (uint32_t tile = blockIdx.x; tile < vtiles * wtiles; tile += gridDim.x) {
 		const uint32_t v0 = (tile % vtiles) * kEmitV, k0 = (tile / vtiles) * kEmitW;
 		const uint32_t nv = min(kEmitV, n - v0);
@@ -670,64 +720,47 @@ __device__ __noinline__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t 
 					const uint32_t inv = ~((uint32_t) (base + l + t) * 0x01010101u);
 					const uint32_t lo = (uint32_t) w[t], hi = (uint32_t) (w[t] >> 32);
 #pragma unroll
-					for (int q = 0; q < 8; ++q) o[q] ^= nibble_bytes((lo >> (4 * q)) & 0xFu) & inv;
+					for (int q = 0; q < 8; ++q) o[q] ^= lut[(lo >> (4 * q)) & 0xFu] & inv;
 #pragma unroll
-					for (int q = 0; q < 8; ++q) o[8 + q] ^= nibble_bytes((hi >> (4 * q)) & 0xFu) & inv;
+					for (int q = 0; q < 8; ++q) o[8 + q] ^= lut[(hi >> (4 * q)) & 0xFu] & inv;
 				}
 			}
-			uint8_t *col = lev + wi * 64 * kEmitStride + vi;
+			uint32_t *col = sw + wi * 16 * kEmitRow + vi;
 #pragma unroll
-			for (int q = 0; q < 16; ++q)
-#pragma unroll
-				for (int b = 0; b < 4; ++b) col[(4 * q + b) * kEmitStride] = (uint8_t) (o[q] >> (8 * b));
+			for (int q = 0; q < 16; ++q) col[q * kEmitRow] = o[q];
 		}
 		__syncthreads();
-		// 2. rows out: 16-byte pieces, stored with the widest unit the row's
-		// alignment allows (rows of an N-byte stride start anywhere)
-		for (uint32_t idx = threadIdx.x; idx < kRows * (kEmitV / 16); idx += blockDim.x) {
-			const uint32_t r = idx / (kEmitV / 16), c = (idx % (kEmitV / 16)) * 16;
-			if (r >= nrows || c >= nv) continue;
-			uint8_t *dst = levels + (size_t) (k0 * 64 + r) * n + v0 + c;
-			const uint8_t *sp = lev + r * kEmitStride + c;
-			uint32_t x[4];
+		// 2. rows out: 16 vertices x 4 source rows per thread
+		const uint32_t c = cc * 16, r0 = rq * 4;
+		if (k0 + rq / 16 < K && r0 < nrows && c < nv) {
+			const uint4 *sp = reinterpret_cast<const uint4 *>(sw + rq * kEmitRow + c);
+			uint32_t x[16];
 #pragma unroll
-			for (int q = 0; q < 4; ++q) x[q] = *(const uint32_t *) (sp + 4 * q);
+			for (int j = 0; j < 4; ++j) {
+				const uint4 u = sp[j];
+				x[4 * j] = u.x;
+				x[4 * j + 1] = u.y;
+				x[4 * j + 2] = u.z;
+				x[4 * j + 3] = u.w;
+			}
+			// y[b][g]: source 4 rq + b, vertices c + 4g .. c + 4g + 3
+			uint32_t y[4][4];
+#pragma unroll
+			for (int g = 0; g < 4; ++g) {
+				const uint32_t t0 = __byte_perm(x[4 * g], x[4 * g + 1], 0x5140);
+				const uint32_t t1 = __byte_perm(x[4 * g + 2], x[4 * g + 3], 0x5140);
+				const uint32_t t2 = __byte_perm(x[4 * g], x[4 * g + 1], 0x7362);
+				const uint32_t t3 = __byte_perm(x[4 * g + 2], x[4 * g + 3], 0x7362);
+				y[0][g] = __byte_perm(t0, t1, 0x5410);
+				y[1][g] = __byte_perm(t0, t1, 0x7632);
+				y[2][g] = __byte_perm(t2, t3, 0x5410);
+				y[3][g] = __byte_perm(t2, t3, 0x7632);
+			}
 			const uint32_t cnt = min(16u, nv - c);
-			const uintptr_t al = (uintptr_t) dst;
-			if (cnt == 16 && (al & 15) == 0) {
-				uint4 y = make_uint4(x[0], x[1], x[2], x[3]);
-				if (merge) {
-					const uint4 old = __ldcg((const uint4 *) dst);
-					y.x = __vminu4(y.x, old.x);
-					y.y = __vminu4(y.y, old.y);
-					y.z = __vminu4(y.z, old.z);
-					y.w = __vminu4(y.w, old.w);
-				}
-				*(uint4 *) dst = y;
-			} else if (cnt == 16 && (al & 3) == 0) {
 #pragma unroll
-				for (int q = 0; q < 4; ++q) {
-					uint32_t y = x[q];
-					if (merge) y = __vminu4(y, __ldcg((const unsigned int *) dst + q));
-					((uint32_t *) dst)[q] = y;
-				}
-			} else if (cnt == 16 && (al & 1) == 0) {
-#pragma unroll
-				for (int q = 0; q < 8; ++q) {
-					uint32_t y = (x[q / 2] >> (16 * (q & 1))) & 0xFFFFu;
-					if (merge) {
-						const uint32_t old = __ldcg((const unsigned short *) dst + q);
-						y = __vminu4(y | 0xFFFF0000u, old | 0xFFFF0000u) & 0xFFFFu;
-					}
-					((uint16_t *) dst)[q] = (uint16_t) y;
-				}
-			} else {
-#pragma unroll
-				for (uint32_t b = 0; b < 16; ++b) {
-					if (b >= cnt) break;
-					const uint8_t y = (uint8_t) (x[b / 4] >> (8 * (b & 3)));
-					dst[b] = merge ? min(y, ld_cg_u8(dst + b)) : y;
-				}
+			for (int b = 0; b < 4; ++b) {
+				if (r0 + b >= nrows) break;
+				emit_piece(levels + (size_t) (k0 * 64 + r0 + b) * n + v0 + c, y[b], cnt, merge);
 			}
 		}
 		__syncthreads();
