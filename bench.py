@@ -650,6 +650,9 @@ def bench_serving(args, torch, dev):
                           "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
                           "max_ms": st["max_ms"], "mean_batch": st["mean_batch"], "batches": int(st["batches"]),
                           "gteps": st["edges_traversed"] / wall / 1e9, "wall_s": wall,
+                          # wall = the arrival window + the drain of the batches in flight at its end
+                          "arrival_window_s": float(arr[-1]) / 1e9,
+                          "drain_ms": max(0.0, wall - float(arr[-1]) / 1e9) * 1e3,
                           "slots_in_flight_mean": st["device_ms"] / 1e3 / wall})
     host = serve_host_check(srv, graphs, edges, pools)
     res = {"graphs": [{"workload": wl.name, "vertices": wl.n, "edges": wl.m} for wl, _ in graphs],
