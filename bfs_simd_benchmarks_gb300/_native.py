@@ -88,7 +88,7 @@ class Options(C.Structure):
 
 
 BFS_BC_TRACE_LEVELS = 64
-BFS_BC_BATCH_MAX_SOURCES = 64
+BFS_BC_BATCH_MAX_SOURCES = 256
 
 
 class BcStats(C.Structure):

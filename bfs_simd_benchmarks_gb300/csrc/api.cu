@@ -121,6 +121,7 @@ struct bfs_graph {
 		cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
 		cudaStream_t stream = nullptr;
 		uint32_t ns = 0;
+		uint32_t words = 0;          // words (launches) of the last batch
 		int grid = 0;
 		size_t bytes = 0;
 		std::vector<DevBuf> bufs;
@@ -1214,6 +1215,8 @@ template <class T> int bb_alloc(bfs_graph *g, T **out, size_t count) {
 	return BFS_OK;
 }
 
+static_assert(BFS_BC_BATCH_MAX_SOURCES == kBbMaxWords * kBbMaxSources, "a batch is at most kBbMaxWords launches");
+
 // Out-edge chunks (once per graph), the per-(vertex, source) state, and
 // (host_out) the [64][n] staging of host outputs.
 int bb_prepare(bfs_graph *g, bool host_deps, bool host_paths) {
@@ -1239,12 +1242,12 @@ int bb_prepare(bfs_graph *g, bool host_deps, bool host_paths) {
 		const size_t rows = (size_t) g->n * kBbMaxSources;
 		const size_t part = (size_t) std::max(g->ms_nchunks, g->bb_noch) * kBbMaxSources;
 		if ((rc = bb_alloc(g, &b.sigma, rows)) || (rc = bb_alloc(g, &b.dsum, rows)) ||
-				(rc = bb_alloc(g, &b.partial, part)) || (rc = bb_alloc(g, &b.ctl, 1)) ||
-				(rc = bb_alloc(g, &b.d_sources, kBbMaxSources))) {
+				(rc = bb_alloc(g, &b.partial, part)) || (rc = bb_alloc(g, &b.ctl, kBbMaxWords)) ||
+				(rc = bb_alloc(g, &b.d_sources, kBbMaxWords * kBbMaxSources))) {
 			release_bb(g);
 			return rc;
 		}
-		if (cudaMallocHost(&b.h_ctl, sizeof(BbControl)) != cudaSuccess ||
+		if (cudaMallocHost(&b.h_ctl, sizeof(BbControl) * kBbMaxWords) != cudaSuccess ||
 				cudaMallocHost(&b.h_ms, sizeof(MsControl)) != cudaSuccess || cudaEventCreate(&b.e0) != cudaSuccess ||
 				cudaEventCreate(&b.e1) != cudaSuccess || cudaEventCreate(&b.e2) != cudaSuccess ||
 				cudaEventCreate(&b.e3) != cudaSuccess) {
@@ -1253,7 +1256,7 @@ int bb_prepare(bfs_graph *g, bool host_deps, bool host_paths) {
 			return BFS_ENOMEM;
 		}
 	}
-	const size_t stage = (size_t) g->n * kBbMaxSources;
+	const size_t stage = (size_t) g->n * kBbMaxWords * kBbMaxSources;
 	if (host_deps && !b.delta && (rc = bb_alloc(g, &b.delta, stage))) return rc;
 	if (host_paths && !b.paths && (rc = bb_alloc(g, &b.paths, stage))) return rc;
 	return BFS_OK;
@@ -1265,8 +1268,9 @@ int bb_prepare(bfs_graph *g, bool host_deps, bool host_paths) {
 int bb_enqueue(bfs_graph *g, const uint32_t *sources, uint32_t ns, float *delta, uint32_t *paths, float *acc,
 		cudaStream_t st) {
 	if (g->relabeled) return BFS_EUNSUPPORTED;
+	const uint32_t K = (ns + kBbMaxSources - 1) / kBbMaxSources;
 	uint32_t planes = 0;
-	int rc = batch_prepare(g, 1, &planes);
+	int rc = batch_prepare(g, K, &planes);
 	if (rc) return rc;
 	auto &b = g->bb;
 	if (b.list_planes < planes) {
@@ -1290,7 +1294,7 @@ int bb_enqueue(bfs_graph *g, const uint32_t *sources, uint32_t ns, float *delta,
 		}
 		b.list_planes = planes;
 	}
-	const MsArgs a = batch_args(g, 1, ns, planes);
+	const MsArgs a = batch_args(g, K, ns, planes);
 	if (cudaEventRecord(b.e0, st) != cudaSuccess) return BFS_ECUDA;
 	if (cudaMemcpyAsync(b.d_sources, sources, sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, st) != cudaSuccess)
 		return BFS_ECUDA;
@@ -1299,7 +1303,7 @@ int bb_enqueue(bfs_graph *g, const uint32_t *sources, uint32_t ns, float *delta,
 	if (cudaEventRecord(b.e1, st) != cudaSuccess) return BFS_ECUDA;
 	BbArgs x{};
 	x.n = g->n;
-	x.ns = ns;
+	x.K = K;
 	x.row_off = g->dg.row_off;
 	x.col = g->dg.col;
 	x.in_off = g->dg.in_off;
@@ -1320,13 +1324,21 @@ int bb_enqueue(bfs_graph *g, const uint32_t *sources, uint32_t ns, float *delta,
 	x.ilist = b.ilist;
 	x.olist = b.olist;
 	x.planes = b.list_planes;
-	x.ctl = b.ctl;
 	x.wait_limit_ns = wait_limit_ns(g->opt);
 	x.hold_barrier = g->opt.test_hold_barrier;
 	x.ctas_per_sm = g->opt.ctas_per_sm;
-	BbOut o{b.d_sources, delta, paths, acc};
-	if ((rc = bb_launch(x, o, g->num_sms, st, &b.grid, b.e2))) return rc;
+	// one launch (and output pass) per word of 64 sources, in source order, so
+	// that acc receives the sources in order
+	for (uint32_t w = 0; w < K; ++w) {
+		x.word = w;
+		x.ns = std::min<uint32_t>(kBbMaxSources, ns - w * kBbMaxSources);
+		x.ctl = b.ctl + w;
+		const size_t row0 = (size_t) w * kBbMaxSources * g->n;
+		BbOut o{b.d_sources + w * kBbMaxSources, delta ? delta + row0 : nullptr, paths ? paths + row0 : nullptr, acc};
+		if ((rc = bb_launch(x, o, g->num_sms, st, &b.grid, w == 0 ? b.e2 : nullptr))) return rc;
+	}
 	if (cudaEventRecord(b.e3, st) != cudaSuccess) return BFS_ECUDA;
+	b.words = K;
 	b.stream = st;
 	b.ns = ns;
 	g->bc_last_batched = true;
@@ -1339,33 +1351,43 @@ int bb_enqueue(bfs_graph *g, const uint32_t *sources, uint32_t ns, float *delta,
 int bb_collect(bfs_graph *g, bfs_bc_stats *out) {
 	auto &b = g->bb;
 	cudaStream_t st = b.stream;
-	if (cudaMemcpyAsync(b.h_ctl, b.ctl, sizeof(BbControl), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+	const uint32_t words = std::max<uint32_t>(1, b.words);
+	if (cudaMemcpyAsync(b.h_ctl, b.ctl, sizeof(BbControl) * words, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
 			cudaMemcpyAsync(b.h_ms, g->mb.args.ctl, sizeof(MsControl), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
 			cudaStreamSynchronize(st) != cudaSuccess)
 		return BFS_ECUDA;
-	const BbControl &c = *b.h_ctl;
+	// per-word launches: counters and times add up; the first status wins;
+	// the per-level times are the first word's
+	const BbControl &c = b.h_ctl[0];
 	const MsStats &ms = b.h_ms->stats;
+	int err = 0;
+	for (uint32_t w = 0; w < words && !err; ++w) err = b.h_ctl[w].err;
 	if (out) {
 		bfs_bc_stats s{};
 		s.num_sources = b.ns;
 		s.batched_sources = b.ns;
 		s.depth = ms.depth ? ms.depth - 1 : 0;
-		s.reached = c.reached[b.ns - 1];
-		s.status = (uint32_t) c.err;
+		s.status = (uint32_t) err;
 		s.edges_reached = ms.traversed;
-		s.edges_forward = c.fwd[0];
-		s.edges_reverse = c.rev[0];
-		s.edges_matched_forward = c.fwd[1];
-		s.edges_matched_reverse = c.rev[1];
-		s.pairs_forward = c.fwd[2];
-		s.pairs_reverse = c.rev[2];
+		for (uint32_t w = 0; w < words; ++w) {
+			const BbControl &cw = b.h_ctl[w];
+			s.edges_forward += cw.fwd[0];
+			s.edges_reverse += cw.rev[0];
+			s.edges_matched_forward += cw.fwd[1];
+			s.edges_matched_reverse += cw.rev[1];
+			s.pairs_forward += cw.fwd[2];
+			s.pairs_reverse += cw.rev[2];
+			if (cw.t[0] && cw.t[1] >= cw.t[0]) s.paths_ms += (float) ((cw.t[1] - cw.t[0]) * 1e-6);
+			if (cw.t[1] && cw.t[2] >= cw.t[1]) s.dependencies_ms += (float) ((cw.t[2] - cw.t[1]) * 1e-6);
+			const uint32_t nsw = std::min<uint32_t>(kBbMaxSources, b.ns - w * kBbMaxSources);
+			for (uint32_t i = 0; i < nsw; ++i) s.source_reached[w * kBbMaxSources + i] = cw.reached[i];
+		}
+		s.reached = s.source_reached[b.ns - 1];
 		float ms_all = 0, tms = 0;
 		cudaEventElapsedTime(&ms_all, b.e0, b.e3);
 		cudaEventElapsedTime(&tms, b.e0, b.e1);
 		s.device_ms = ms_all;
 		s.traversal_ms = tms;
-		if (c.t[0] && c.t[1] >= c.t[0]) s.paths_ms = (float) ((c.t[1] - c.t[0]) * 1e-6);
-		if (c.t[1] && c.t[2] >= c.t[1]) s.dependencies_ms = (float) ((c.t[2] - c.t[1]) * 1e-6);
 		s.grid_ctas = (uint32_t) b.grid;
 		for (uint32_t d = 0; d < ms.depth && d < BFS_BC_TRACE_LEVELS && d < kMsTraceLevels; ++d) {
 			s.level_vertices[d] = ms.frontier[d];
@@ -1379,10 +1401,9 @@ int bb_collect(bfs_graph *g, bfs_bc_stats *out) {
 			const unsigned long long r0 = deepest ? c.t[1] : c.t_rev[d + 1], r1 = c.t_rev[d];
 			if (r0 && r1 >= r0) s.level_dependencies_ms[d] = (float) ((r1 - r0) * 1e-6);
 		}
-		for (uint32_t i = 0; i < b.ns; ++i) s.source_reached[i] = c.reached[i];
 		*out = s;
 	}
-	return c.err;
+	return err;
 }
 
 // Adds one run's statistics into a total over runs.
@@ -2079,8 +2100,8 @@ int bfs_bc_accumulate(bfs_graph *g, const uint32_t *sources, uint32_t num_source
 		rc = bc_sources_one_by_one(g, sources, num_sources, nullptr, nullptr, b.acc, total);
 	} else {
 		// groups of up to 64 sources; a group deeper than the planes one source at a time
-		for (uint32_t i = 0; i < num_sources && rc == BFS_OK; i += kBbMaxSources) {
-			const uint32_t k = std::min<uint32_t>(kBbMaxSources, num_sources - i);
+		for (uint32_t i = 0; i < num_sources && rc == BFS_OK; i += BFS_BC_BATCH_MAX_SOURCES) {
+			const uint32_t k = std::min<uint32_t>(BFS_BC_BATCH_MAX_SOURCES, num_sources - i);
 			bfs_bc_stats one{};
 			rc = bb_enqueue(g, sources + i, k, nullptr, nullptr, b.acc, 0);
 			if (rc == BFS_OK) rc = bb_collect(g, &one);

@@ -57,6 +57,13 @@ __device__ __forceinline__ uint64_t bb_shfl64(uint64_t x, int src) {
 	return (uint64_t) __shfl_sync(kFull, (unsigned long long) x, src);
 }
 __device__ __forceinline__ uint64_t bb_ldg64(const uint64_t *p) { return __ldg((const unsigned long long *) p); }
+// Plane L of the launch's word, and vertex v's entry in it (planes hold K words per vertex).
+__device__ __forceinline__ const uint64_t *bb_plane(const BbArgs &a, uint32_t L) {
+	return a.hist + (size_t) L * a.n * a.K + a.word;
+}
+__device__ __forceinline__ uint64_t bb_word(const uint64_t *plane, const BbArgs &a, uint32_t v) {
+	return bb_ldg64(plane + (size_t) v * a.K);
+}
 
 // A warp's counts over a sweep: edges read (lane 0), edges that serve a
 // source (lane 0), and (edge, source) pairs summed (every lane its own edges).
@@ -246,11 +253,11 @@ __device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, B
 	using D = BbDir<kFwd>;
 	using T = typename D::T;
 	const unsigned lane = lane_id();
-	const uint64_t *own = a.hist + (size_t) L * a.n;
-	const uint64_t *nb = a.hist + (size_t) (kFwd ? L - 1 : L + 1) * a.n;
+	const uint64_t *own = bb_plane(a, L);
+	const uint64_t *nb = bb_plane(a, kFwd ? L - 1 : L + 1);
 	const uint32_t *off = D::off(a), *adj = D::adj(a);
 	const uint32_t vb = b * 32, v = vb + lane;
-	const uint64_t hv = v < a.n ? bb_ldg64(own + v) : 0ull;
+	const uint64_t hv = v < a.n ? bb_word(own, a, v) : 0ull;
 	uint32_t beg = 0, end = 0;
 	if (hv) {
 		beg = __ldg(off + v);
@@ -282,7 +289,7 @@ __device__ void bb_block(const BbArgs &a, uint32_t L, bool has_nb, uint32_t b, B
 		uint64_t m = 0;
 		if (e < total) {
 			u = __ldg(adj + obeg + (e - oex));
-			m = ohv & bb_ldg64(nb + u);
+			m = ohv & bb_word(nb, a, u);
 		}
 		uint32_t bal = __ballot_sync(kFull, m != 0ull);
 		if (lane == 0) {
@@ -355,7 +362,7 @@ __device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, u
 	using D = BbDir<kFwd>;
 	using T = typename D::T;
 	const unsigned lane = lane_id();
-	const uint64_t *nb = a.hist + (size_t) (kFwd ? L - 1 : L + 1) * a.n;
+	const uint64_t *nb = bb_plane(a, kFwd ? L - 1 : L + 1);
 	const uint32_t *off = D::off(a), *adj = D::adj(a), *cb = D::chunk_beg(a);
 	const uint32_t beg = __ldg(cb + c), end = min(beg + kBbChunk, __ldg(off + v + 1));
 	T acc[4] = {T(0), T(0), T(0), T(0)};
@@ -365,7 +372,7 @@ __device__ void bb_chunk(const BbArgs &a, uint32_t L, bool has_nb, uint32_t c, u
 		uint64_t m = 0;
 		if (e < end) {
 			u = __ldg(adj + e);
-			m = hv & bb_ldg64(nb + u);
+			m = hv & bb_word(nb, a, u);
 		}
 		uint32_t bal = __ballot_sync(kFull, m != 0ull);
 		if (lane == 0) {
@@ -413,7 +420,7 @@ __device__ void bb_finish(const BbArgs &a, uint32_t L) {
 	const uint32_t ncl = ld_volatile(kFwd ? &a.ctl->ni_at[L] : &a.ctl->no_at[L]);
 	const uint32_t *clist = (kFwd ? a.ilist : a.olist) + (size_t) L * D::nchunks(a);
 	const unsigned lane = lane_id();
-	const uint64_t *own = a.hist + (size_t) L * a.n;
+	const uint64_t *own = bb_plane(a, L);
 	const uint32_t *off = D::off(a), *cv = D::chunk_v(a), *cb = D::chunk_beg(a);
 	const uint32_t gwarp = blockIdx.x * kBbWarps + warp_id(), nwarps = gridDim.x * kBbWarps;
 	for (uint32_t i = gwarp; i < ncl; i += nwarps) {
@@ -421,7 +428,7 @@ __device__ void bb_finish(const BbArgs &a, uint32_t L) {
 		const uint32_t v = __ldg(cv + c);
 		const uint32_t b0 = __ldg(off + v);
 		if (__ldg(cb + c) != b0) continue;
-		const uint64_t hv = bb_ldg64(own + v);
+		const uint64_t hv = bb_word(own, a, v);
 		const uint32_t k = (__ldg(off + v + 1) - b0 + kBbChunk - 1) / kBbChunk;
 		const bool w0 = (hv >> lane) & 1ull, w1 = (hv >> (lane + 32)) & 1ull;
 		T acc0 = T(0), acc1 = T(0);
@@ -456,12 +463,12 @@ __device__ void bb_lists(const BbArgs &a, uint32_t depth) {
 	const uint32_t nblk = (a.n + 31) / 32;
 	for (uint32_t wb = gwarp; wb * 32 < nblk; wb += nwarps) {
 		for (uint32_t L = 0; L < depth; ++L) {
-			const uint64_t *pl = a.hist + (size_t) L * a.n;
+			const uint64_t *pl = bb_plane(a, L);
 			uint32_t act = 0;
 #pragma unroll 8
 			for (uint32_t j = 0; j < 32; ++j) {
 				const uint32_t v = (wb * 32 + j) * 32 + lane;
-				const uint64_t h = v < a.n ? bb_ldg64(pl + v) : 0ull;
+				const uint64_t h = v < a.n ? bb_word(pl, a, v) : 0ull;
 				if (__any_sync(kFull, h != 0ull)) act |= 1u << j;
 			}
 			if (!act) continue;
@@ -480,7 +487,7 @@ __device__ void bb_lists(const BbArgs &a, uint32_t depth) {
 			const uint32_t c = c0 + lane;
 			const uint32_t v = c < nch ? __ldg(cv + c) : 0u;
 			for (uint32_t L = 0; L < depth; ++L) {
-				const bool at = c < nch && bb_ldg64(a.hist + (size_t) L * a.n + v) != 0ull;
+				const bool at = c < nch && bb_word(bb_plane(a, L), a, v) != 0ull;
 				const uint32_t m = __ballot_sync(kFull, at);
 				if (!m) continue;
 				uint32_t base = 0;
@@ -514,7 +521,7 @@ __device__ void bb_level(const BbArgs &a, uint32_t L, bool has_nb, unsigned *cou
 		if (item < ncl) {
 			const uint32_t c = __ldcg(clist + item);
 			const uint32_t v = __ldg(D::chunk_v(a) + c);
-			bb_chunk<kFwd>(a, L, has_nb, c, v, bb_ldg64(a.hist + (size_t) L * a.n + v), cnt);
+			bb_chunk<kFwd>(a, L, has_nb, c, v, bb_word(bb_plane(a, L), a, v), cnt);
 		} else {
 			bb_block<kFwd>(a, L, has_nb, __ldcg(blist + (item - ncl)), cnt);
 		}
@@ -551,7 +558,7 @@ __global__ void __launch_bounds__(kBbThreads, 2) k_bc_batch(BbArgs a) {
 	unsigned epoch = 0;
 	const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
 	for (uint32_t v = t0; v < a.n; v += stride) {
-		uint64_t h = bb_ldg64(a.hist + v);
+		uint64_t h = bb_word(bb_plane(a, 0), a, v);
 		while (h) {
 			a.sigma[(size_t) v * 64 + (__ffsll((long long) h) - 1)] = 1u;
 			h &= h - 1ull;
@@ -602,7 +609,7 @@ __global__ void __launch_bounds__(kBbOutThreads) k_bc_batch_out(BbArgs a, BbOut 
 	for (uint32_t v0 = blockIdx.x * kBbOutV; v0 < a.n; v0 += gridDim.x * kBbOutV) {
 		const uint32_t nv = min(kBbOutV, a.n - v0);
 		__syncthreads();
-		if (t < nv) svis[t] = bb_ldg64(a.vis + v0 + t) & smask;
+		if (t < nv) svis[t] = bb_ldg64(a.vis + (size_t) (v0 + t) * a.K + a.word) & smask;
 		__syncthreads();
 		// 16-byte loads: 4 sources of a row per thread (streamed, not kept in L2)
 		for (uint32_t i = t; i < nv * 16; i += blockDim.x) {

@@ -9,7 +9,8 @@
 
 namespace bfsg {
 
-constexpr uint32_t kBbMaxSources = 64;       // one 64-bit word of sources per vertex
+constexpr uint32_t kBbMaxSources = 64;       // sources per launch: one 64-bit word of the traversal
+constexpr uint32_t kBbMaxWords = 4;          // words per call (BFS_BC_BATCH_MAX_SOURCES = 256 sources)
 constexpr uint32_t kBbBig = kMsPullBig;      // degree above which a vertex's edges are summed in chunks ...
 constexpr uint32_t kBbChunk = kMsChunk;      // ... of this many edges (the batched pull's in-edge chunks)
 constexpr uint32_t kBbTraceLevels = 64;      // per-level timers kept for the first levels
@@ -33,11 +34,12 @@ struct BbControl {
 };
 
 struct BbArgs {
-	uint32_t n, ns;
+	uint32_t n, ns;                    // ns: sources of this launch's word (1..64)
+	uint32_t K, word;                  // the traversal's words per vertex; the word this launch takes
 	const uint32_t *row_off, *col;     // CSR
 	const uint32_t *in_off, *in_src;   // in-edge lists
-	const uint64_t *hist;              // plane L at hist + L * n: sources that reached v first at level L
-	const uint64_t *vis;               // [n] sources that reached v
+	const uint64_t *hist;              // [planes][n][K]: sources that reached v first at level L
+	const uint64_t *vis;               // [n][K] sources that reached v
 	const MsControl *ms;               // the traversal's control block (depth, completion, status)
 	const uint32_t *ichunk_v, *ichunk_beg;  // in-edge chunks of vertices with in-degree > kBbBig
 	uint32_t nich;
@@ -65,8 +67,8 @@ struct BbOut {
 };
 
 // Enqueues, after the batched traversal that filled a.hist / a.vis / a.ms,
-// the cooperative path-count and dependency launch and the output pass; the
-// control block is cleared first.  `between` (may be null) is recorded
+// the cooperative path-count and dependency launch for the sources of word
+// a.word and the output pass; the control block is cleared first.  `between` (may be null) is recorded
 // between the two launches; *grid gets the CTA count.
 int bb_launch(const BbArgs &a, const BbOut &o, int num_sms, cudaStream_t st, int *grid, cudaEvent_t between);
 

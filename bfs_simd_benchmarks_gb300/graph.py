@@ -247,7 +247,7 @@ class Graph:
                                            C.c_void_p(stream) if stream else None), "bfs_bc_run_device")
 
     def bc_batch(self, sources, paths: bool = True):
-        """Betweenness of up to 64 sources at once (bfs_bc_run_batch): float32
+        """Betweenness of up to 256 sources at once (bfs_bc_run_batch): float32
         [k, N] dependencies, uint32 [k, N] shortest-path counts (or None) and
         the stats."""
         src = _u32(sources)

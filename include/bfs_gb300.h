@@ -166,7 +166,7 @@ typedef struct bfs_options {
 	uint32_t td_beta;          /* BFS_SWITCH_UNVISITED: beta (default 24) */
 	uint32_t ctas_per_sm;      /* CTAs per SM of the cooperative traversal grids: 0 = as many as fit (at most
 	                              2), or 1 or 2 */
-	uint32_t bc_batch;         /* bfs_bc_accumulate: 1 (default) = sources in groups of up to 64 through the
+	uint32_t bc_batch;         /* bfs_bc_accumulate: 1 (default) = sources in groups of up to 256 through the
 	                              batched betweenness kernel (bfs_bc_run_batch); 0 = one source at a time */
 } bfs_options;
 
@@ -493,6 +493,7 @@ int bfs_graph_bfs_order(bfs_graph *g, uint32_t source, uint32_t *vertex_map);
  * computes it the same way).  Sums are taken in a fixed order: repeated runs
  * give identical bits.  Traversals deeper than 2^19 levels: BFS_EUNSUPPORTED. */
 #define BFS_BC_TRACE_LEVELS 64
+#define BFS_BC_BATCH_MAX_SOURCES 256 /* sources per bfs_bc_run_batch call */
 typedef struct bfs_bc_stats {
 	uint32_t num_sources;     /* dependency runs counted here */
 	uint32_t depth;           /* deepest level (the largest over the runs) */
@@ -524,7 +525,8 @@ typedef struct bfs_bc_stats {
 	uint64_t edges_matched_reverse;  /* ... by the dependency sweeps */
 	uint64_t pairs_forward;          /* (edge, source) pairs summed by the path-count sweeps */
 	uint64_t pairs_reverse;          /* ... by the dependency sweeps */
-	uint32_t source_reached[64];     /* the last batch: vertices reached from each of its sources */
+	uint32_t source_reached[BFS_BC_BATCH_MAX_SOURCES];  /* the last batch: vertices reached from each of its
+	                                                       sources */
 } bfs_bc_stats;
 
 /* dependencies[N] and num_paths[N] are HOST buffers (either may be NULL). */
@@ -535,17 +537,16 @@ int bfs_bc_run_device(bfs_graph *g, uint32_t source, float *dependencies, uint32
 /* Statistics of the last bfs_bc_* run (synchronises with it). */
 int bfs_bc_last_stats(bfs_graph *g, bfs_bc_stats *stats);
 /* Batched betweenness (no counterpart in the reference, whose BC() takes one
- * source per call): the dependencies and path counts of up to 64 sources from
- * one bit-sliced traversal (the bfs_run_batch kernel) and one pass over the
- * graph per level and direction, every (vertex, source) pair in 8 bytes of
- * state.  Per source the values are bfs_bc_run's (path counts bit-exact;
+ * source per call): the dependencies and path counts of up to 256 sources from
+ * one bit-sliced traversal (the bfs_run_batch kernel) and, for every 64 of
+ * them, one pass over the graph per level and direction, every (vertex,
+ * source) pair in 8 bytes of state.  Per source the values are bfs_bc_run's (path counts bit-exact;
  * dependencies the same formulas, float sums in another fixed order: repeated
  * calls give identical bits).  dependencies [num_sources][N] and num_paths
  * [num_sources][N] are HOST buffers (either may be NULL).  A batch whose
  * traversal is deeper than its level planes (bfs_options.batch_planes /
  * batch_budget_mb; or more than 254 levels) runs one source at a time
  * through bfs_bc_run's kernel instead (stats->fallback_sources). */
-#define BFS_BC_BATCH_MAX_SOURCES 64
 int bfs_bc_run_batch(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *dependencies,
 		uint32_t *num_paths, bfs_bc_stats *stats);
 /* The same enqueued on `stream` into DEVICE buffers [num_sources][N] (either
@@ -558,7 +559,7 @@ int bfs_bc_run_batch_device(bfs_graph *g, const uint32_t *sources, uint32_t num_
  * overwritten) = sum over the sources s != v of the dependencies of s on v,
  * added in source order; over all N sources it is the unnormalised directed
  * betweenness.  With bfs_options.bc_batch = 1 (default) the sources go through
- * the batched kernel 64 at a time. */
+ * the batched kernel 256 at a time. */
 int bfs_bc_accumulate(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *centrality,
 		bfs_bc_stats *stats);
 /* The same into a DEVICE buffer that is added to (not cleared), enqueued on

@@ -97,6 +97,27 @@ def test_bc_batch_rmat_64_sources_with_hubs(native, oracle):
             _check_rows(oracle, arr, sources[:k], d1, s1)
 
 
+def test_bc_batch_several_words(native, oracle):
+    """150 sources in one call: three words of the traversal (64, 64, 22
+    sources), one launch each; every row against the oracle, the statistics
+    summed over the launches."""
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 13
+    src, dst = B.gen_rmat(n, 16 * n, seed=515, permute=True)
+    arr = oracle.csr_arrays(n, src, dst)
+    with B.Graph.from_edges(n, src, dst, 256, 4) as g:
+        sources = B.pick_sources(g.degrees(), 150, seed=12).astype(np.uint32)
+        dep, sig, st = g.bc_batch(sources)
+        assert st["status"] == 0 and st["batched_sources"] == 150 and len(st["source_reached"]) == 150
+        _check_rows(oracle, arr, sources, dep, sig, st)
+        lev = [oracle.bfs_levels(arr, int(x)) for x in sources]
+        dag = sum(int(((lv[src] >= 0) & (lv[dst] == lv[src] + 1)).sum()) for lv in lev)
+        assert st["pairs_forward"] == dag and st["pairs_reverse"] == dag
+        # the first 64 rows equal a batch of those 64 alone
+        d64, s64, _ = g.bc_batch(sources[:64])
+        assert d64.tobytes() == dep[:64].tobytes() and s64.tobytes() == sig[:64].tobytes()
+
+
 def test_bc_batch_fallback_when_planes_run_out(native, oracle):
     import bfs_simd_benchmarks_gb300 as B
     n = 1 << 12
@@ -133,21 +154,21 @@ def test_bc_batch_device_matches_host(native):
 
 
 def test_bc_accumulate_batched_matches_one_by_one(native, oracle):
-    """bfs_bc_accumulate over 150 sources (groups of 64, 64, 22) against the
-    one-source-at-a-time accumulation and the oracle's sum."""
+    """bfs_bc_accumulate over 300 sources (a batch of 256, four words, then one
+    of 44) against the one-source-at-a-time accumulation and the oracle's sum."""
     import bfs_simd_benchmarks_gb300 as B
     n = 1 << 12
     src, dst = B.gen_rmat(n, 8 * n, seed=31, permute=True)
     arr = oracle.csr_arrays(n, src, dst)
     with B.Graph.from_edges(n, src, dst, 256, 4) as g:
-        sources = B.pick_sources(g.degrees(), 150, seed=4).astype(np.uint32)
+        sources = B.pick_sources(g.degrees(), 300, seed=4).astype(np.uint32)
         bc1, st1 = g.betweenness(sources)
-        assert st1["batched_sources"] == 150 and st1["num_sources"] == 150
+        assert st1["batched_sources"] == 300 and st1["num_sources"] == 300
         bc1b, _ = g.betweenness(sources)
         assert bc1b.tobytes() == bc1.tobytes()
         g.set_options(bc_batch=0)
         bc0, st0 = g.betweenness(sources)
-        assert st0["batched_sources"] == 0 and st0["num_sources"] == 150
+        assert st0["batched_sources"] == 0 and st0["num_sources"] == 300
         assert st0["edges_reached"] == st1["edges_reached"]
         want = np.zeros(n)
         scale = np.zeros(n)
@@ -169,7 +190,7 @@ def test_bc_batch_arguments(native):
     c = load_case("sparse15_w16_s2")
     with B.Graph.from_edges(c["n"], c["src"], c["dst"], c["w"], c["s"]) as g:
         with pytest.raises(N.BfsError) as e:
-            g.bc_batch(np.arange(65, dtype=np.uint32))
+            g.bc_batch(np.arange(257, dtype=np.uint32))
         assert e.value.status == N.BFS_EARG
         with pytest.raises(N.BfsError) as e:
             g.bc_batch(np.array([0, c["n"]], np.uint32))
