@@ -1028,7 +1028,9 @@ def main():
             "e2e": {"value": e2e_value, "unit": "GTEPS", "h2d_bytes_per_step": 4 * len(sources),
                     "d2h_bytes_per_step": 4 * n * len(sources),
                     "note": "bfs_run(): source as a launch parameter, int32 levels to pinned host memory"},
-            "gpu_launches": 2 * len(timed),
+            # per timed traversal: k_bfs_persistent, and k_unrelabel on a degree-ordered layout
+            # (the L2 flush before it is torch's fill kernel, not counted)
+            "gpu_launches": (2 if degree_order else 1) * len(timed),
             "clocks": clocks,
             "cpu_baseline": cpu,
             "parity": parity,
