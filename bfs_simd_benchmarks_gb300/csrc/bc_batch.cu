@@ -1,4 +1,5 @@
-// bc_batch.cu -- betweenness dependencies of up to 64 sources in one pass.
+// bc_batch.cu -- betweenness dependencies of 64 sources (one word of a batched
+// traversal) in one pass.
 //
 // No counterpart in the reference, whose BC() (apps/betweennessCentrality_simd/
 // bc.cpp:1717-2097) handles one source per call; for every source the results
@@ -9,11 +10,11 @@
 // count is 0).
 //
 // The batched traversal (msbfs.cu) leaves, for every level L, the plane
-// hist[L][v]: the sources that reached v first at level L.  u -> v is a
-// shortest-path edge of source s exactly when bit s is set in both
-// hist[L-1][u] and hist[L][v], so one AND of two words gives all the sources
-// an edge serves.  The state is per (vertex, source): sigma[v][64] and
-// dsum[v][64], a 256-byte row each; lane l of a warp owns sources l and l+32.
+// hist[L][v]: the sources that reached v first at level L (a launch takes one
+// 64-bit word of it).  u -> v is a shortest-path edge of source s exactly when
+// bit s is set in both hist[L-1][u] and hist[L][v], so one AND of two words
+// gives all the sources an edge serves.  The state is per (vertex, source):
+// sigma[v][64] and dsum[v][64], a 256-byte row each.
 //
 // One cooperative launch, levels separated by grid barriers:
 //   forward, L = 1 .. depth-1, every v with hist[L][v] != 0:
@@ -27,8 +28,11 @@
 // block and walks the concatenated edge lists of its vertices at that level,
 // 32 edges per step (each edge's vertex found by a binary search over the
 // warp's degree prefix); an edge's source mask is one AND.  The edges with a
-// non-empty mask are then taken in edge order, four at a time, each a
-// coalesced read of the neighbour's row by the lanes whose bit is set.
+// non-empty mask are then taken in edge order by half-warps, two pairs per
+// round (lane 16h + i holds sources 4i .. 4i+3: one 16-byte piece of the
+// neighbour's row, read where any of the 4 is served); a vertex's sum is its
+// half-0 sum plus its half-1 sum.  The finish of chunked vertices keeps lane l
+// on sources l and l + 32.
 // Vertices with more than kBbBig edges in the sweep's direction are cut into
 // kBbChunk-edge chunks, one list item each; the partial rows are added in
 // chunk order after a grid barrier.  Every sum has a fixed order, so repeated

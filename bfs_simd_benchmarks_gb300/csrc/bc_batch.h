@@ -1,5 +1,6 @@
-// bc_batch.h -- betweenness dependencies of up to 64 sources at once, on the
-// bit-sliced batched traversal (internal).
+// bc_batch.h -- betweenness dependencies of many sources at once (64 per
+// launch, up to 4 launches per call), on the bit-sliced batched traversal
+// (internal).
 #pragma once
 
 #include <cstdint>
