@@ -101,8 +101,7 @@ template <> struct BbDir<false> {
 	static __device__ __forceinline__ const T *vals(const BbArgs &a) { return a.dsum; }
 	static __device__ __forceinline__ T from_bits(uint32_t b) { return __uint_as_float(b); }
 	static __device__ __forceinline__ uint32_t to_bits(T x) { return __float_as_uint(x); }
-	// the vertex's path count, loaded when the vertex's first edge is taken so
-	// that the load is done by the time its sum is
+	// the vertex's path count, loaded ahead of its sum's store
 	static __device__ __forceinline__ uint32_t pre(const BbArgs &a, size_t i, bool mine) {
 		return mine ? __ldcg(a.sigma + i) : 0u;
 	}
@@ -113,8 +112,9 @@ template <> struct BbDir<false> {
 	}
 };
 
-// What a vertex's finished sums need besides the sums (the reverse sweep: its
-// path counts for this lane's two sources), loaded ahead.
+// The finish of chunked vertices (lane l: sources l and l + 32): what a
+// vertex's finished sums need besides the sums (the reverse sweep: its path
+// counts for this lane's two sources), loaded ahead.
 struct BbPre {
 	uint32_t p0, p1;
 };
