@@ -153,6 +153,26 @@ def test_bc_batch_device_matches_host(native):
         assert d_sig.cpu().numpy().view(np.uint32).tobytes() == sig.tobytes()
 
 
+def test_bc_batch_device_two_words_matches_host(native):
+    """bfs_bc_run_batch_device with 100 sources (two words, two launches) into
+    device buffers: the same bits as the host entry point."""
+    import torch
+    import bfs_simd_benchmarks_gb300 as B
+    n = 1 << 12
+    src, dst = B.gen_rmat(n, 8 * n, seed=919, permute=True)
+    with B.Graph.from_edges(n, src, dst, 256, 4) as g:
+        sources = B.pick_sources(g.degrees(), 100, seed=5).astype(np.uint32)
+        dep, sig, _ = g.bc_batch(sources)
+        d_dep = torch.empty((sources.size, n), dtype=torch.float32, device="cuda")
+        d_sig = torch.empty((sources.size, n), dtype=torch.int32, device="cuda")
+        g.bc_batch_device(sources, d_dep.data_ptr(), d_sig.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        st = g.bc_stats()
+        assert st["status"] == 0 and st["batched_sources"] == 100 and len(st["source_reached"]) == 100
+        assert d_dep.cpu().numpy().tobytes() == dep.tobytes()
+        assert d_sig.cpu().numpy().view(np.uint32).tobytes() == sig.tobytes()
+
+
 def test_bc_accumulate_batched_matches_one_by_one(native, oracle):
     """bfs_bc_accumulate over 300 sources (a batch of 256, four words, then one
     of 44) against the one-source-at-a-time accumulation and the oracle's sum."""
