@@ -682,6 +682,15 @@ __device__ __forceinline__ void emit_piece(uint8_t *dst, const uint32_t (&x)[4],
 	}
 }
 
+// kCached: the planes may be read through L1 (a launch of its own after the
+// traversal; the four warps of a tile read neighbouring words of the same
+// sectors); inside the traversal kernel they are read around L1.
+template <bool kCached>
+__device__ __forceinline__ uint64_t emit_ld(const uint64_t *p) {
+	return kCached ? (uint64_t) __ldg((const unsigned long long *) p) : ld_cg64(p);
+}
+
+template <bool kCached>
 __device__ __noinline__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t ns, uint32_t base, uint32_t first, uint32_t last,
 		bool merge, uint8_t *lev) {
 	constexpr uint32_t kRows = kEmitW * 64;
@@ -711,8 +720,8 @@ __device__ __noinline__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t 
 				uint64_t w[4];
 #pragma unroll
 				for (int t = 0; t < 4; ++t) {
-					const uint64_t m = l + t <= last ? ld_cg64(pm + (size_t) (l - first + t) * n) : 0ull;
-					w[t] = ((m >> k) & 1ull) ? ld_cg64(pw + (size_t) (l - first + t) * pstride) : 0ull;
+					const uint64_t m = l + t <= last ? emit_ld<kCached>(pm + (size_t) (l - first + t) * n) : 0ull;
+					w[t] = ((m >> k) & 1ull) ? emit_ld<kCached>(pw + (size_t) (l - first + t) * pstride) : 0ull;
 				}
 #pragma unroll
 				for (int t = 0; t < 4; ++t) {
@@ -830,7 +839,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 				break;
 			}
 			// planes full: write them out, keep the frontier's plane as plane 0
-			ms_emit(a, levels, ns, base, base == 0 ? 0 : 1, lvl - base, base != 0, lev);
+			ms_emit<false>(a, levels, ns, base, base == 0 ? 0 : 1, lvl - base, base != 0, lev);
 			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 			const uint64_t *src = a.hist + (size_t) (lvl - base) * nK;
 			for (size_t i = t0; i < nK; i += stride) a.hist[i] = ld_cg64(src + i);
@@ -942,7 +951,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_emit(MsArgs a, uint32_t ns
 	const uint32_t base = st.base, depth = st.depth;
 	const uint32_t first = base == 0 ? 0 : 1;
 	if (depth < base + first + 1) return;
-	ms_emit(a, levels, ns, base, first, depth - 1 - base, base != 0, lev);
+	ms_emit<true>(a, levels, ns, base, first, depth - 1 - base, base != 0, lev);
 }
 
 int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *levels, int num_sms, cudaStream_t st,
