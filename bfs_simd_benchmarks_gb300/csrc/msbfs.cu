@@ -46,10 +46,14 @@ constexpr int kMsGather = 4;            // pull: frontier rows gathered per roun
 constexpr uint32_t kLaneMaxWords = 2;   // pull: up to this many words per vertex ...
 constexpr uint32_t kLaneMaxDeg = 32;    // ... destinations of at most this in-degree go one per lane
 constexpr uint32_t kGroupMaxWords = 8;  // pull: up to this many words, in-neighbour rows in lane groups
-constexpr uint32_t kEmitV = 128;        // output tile: 128 vertices x 4 words (256 sources)
-constexpr uint32_t kEmitW = 4;
-constexpr uint32_t kEmitRow = kEmitV + 4;  // shared row of one source quad, in words (16-byte aligned rows)
-constexpr uint32_t kEmitBytes = (kEmitW * 16 * kEmitRow + 16) * 4;  // the rows and the nibble table
+constexpr uint32_t kEmitW = 4;          // output tile: kV vertices x 4 words (256 sources), kV = threads / 4
+// shared bytes of an output tile of kV vertices: rows of one source quad (kV + 4
+// words, 16-byte aligned) and the nibble table
+__host__ __device__ constexpr uint32_t emit_bytes(uint32_t kV) { return (kEmitW * 16 * (kV + 4) + 16) * 4; }
+constexpr uint32_t kEmitV = kMsThreads / kEmitW;  // the traversal kernel's tiles (its early output passes)
+constexpr uint32_t kEmitBytes = emit_bytes(kEmitV);
+constexpr int kEmitThreads = 256;                 // the output pass launch
+constexpr uint32_t kEmitOutV = kEmitThreads / kEmitW;
 
 __device__ __forceinline__ uint64_t ld_cg64(const uint64_t *p) { return __ldcg((const unsigned long long *) p); }
 __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
@@ -690,9 +694,10 @@ __device__ __forceinline__ uint64_t emit_ld(const uint64_t *p) {
 	return kCached ? (uint64_t) __ldg((const unsigned long long *) p) : ld_cg64(p);
 }
 
-template <bool kCached>
+template <bool kCached, uint32_t kV>
 __device__ __noinline__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t ns, uint32_t base, uint32_t first, uint32_t last,
 		bool merge, uint8_t *lev) {
+	constexpr uint32_t kEmitV = kV, kEmitRow = kV + 4;
 	constexpr uint32_t kRows = kEmitW * 64;
 	const uint32_t K = a.K, n = a.n;
 	const uint32_t vtiles = (n + kEmitV - 1) / kEmitV, wtiles = (K + kEmitW - 1) / kEmitW;
@@ -839,7 +844,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 				break;
 			}
 			// planes full: write them out, keep the frontier's plane as plane 0
-			ms_emit<false>(a, levels, ns, base, base == 0 ? 0 : 1, lvl - base, base != 0, lev);
+			ms_emit<false, kEmitV>(a, levels, ns, base, base == 0 ? 0 : 1, lvl - base, base != 0, lev);
 			if (!(ok = grid_sync(ctl->bar, epoch, &ctl->err, a.wait_limit_ns, a.hold_barrier))) break;
 			const uint64_t *src = a.hist + (size_t) (lvl - base) * nK;
 			for (size_t i = t0; i < nK; i += stride) a.hist[i] = ld_cg64(src + i);
@@ -944,14 +949,16 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 // The final output pass, its own launch after k_ms_bfs (more CTAs per SM than
 // the cooperative kernel, so more plane loads in flight).  Plane depth - base
 // is the empty frontier; after an early output pass, plane 0 was written too.
-__global__ void __launch_bounds__(kMsThreads, 2) k_ms_emit(MsArgs a, uint32_t ns, uint8_t *levels) {
-	__shared__ __align__(16) uint8_t lev[kEmitBytes];
+// Smaller CTAs than the traversal's: a tile's plane loads and its barriers
+// form a chain of round trips, and more CTAs per SM keep more chains going.
+__global__ void __launch_bounds__(kEmitThreads, 4) k_ms_emit(MsArgs a, uint32_t ns, uint8_t *levels) {
+	__shared__ __align__(16) uint8_t lev[emit_bytes(kEmitOutV)];
 	const MsStats &st = a.ctl->stats;
 	if (!st.complete) return;
 	const uint32_t base = st.base, depth = st.depth;
 	const uint32_t first = base == 0 ? 0 : 1;
 	if (depth < base + first + 1) return;
-	ms_emit<true>(a, levels, ns, base, first, depth - 1 - base, base != 0, lev);
+	ms_emit<true, kEmitOutV>(a, levels, ns, base, first, depth - 1 - base, base != 0, lev);
 }
 
 int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *levels, int num_sms, cudaStream_t st,
@@ -973,7 +980,7 @@ int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *
 		return BFS_ECUDA;
 	if (between && cudaEventRecord(between, st) != cudaSuccess) return BFS_ECUDA;
 	if (between2 && cudaEventRecord(between2, st) != cudaSuccess) return BFS_ECUDA;
-	if (levels) k_ms_emit<<<num_sms * 2, kMsThreads, 0, st>>>(a, ns, levels);
+	if (levels) k_ms_emit<<<num_sms * 4, kEmitThreads, 0, st>>>(a, ns, levels);
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }
 
