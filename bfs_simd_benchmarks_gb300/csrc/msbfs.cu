@@ -721,15 +721,20 @@ __device__ __noinline__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t 
 			uint32_t o[16];
 #pragma unroll
 			for (int q = 0; q < 16; ++q) o[q] = 0xFFFFFFFFu;
-			for (uint32_t l = first; l <= last; l += 4) {
-				uint64_t w[4];
+			// 8 planes per round: their word masks (one round trip), then the
+			// non-zero words (one more)
+			for (uint32_t l = first; l <= last; l += 8) {
+				uint32_t nz = 0;
 #pragma unroll
-				for (int t = 0; t < 4; ++t) {
-					const uint64_t m = l + t <= last ? emit_ld<kCached>(pm + (size_t) (l - first + t) * n) : 0ull;
-					w[t] = ((m >> k) & 1ull) ? emit_ld<kCached>(pw + (size_t) (l - first + t) * pstride) : 0ull;
-				}
+				for (int t = 0; t < 8; ++t)
+					if (l + t <= last)
+						nz |= (uint32_t) ((emit_ld<kCached>(pm + (size_t) (l - first + t) * n) >> k) & 1ull) << t;
+				uint64_t w[8];
 #pragma unroll
-				for (int t = 0; t < 4; ++t) {
+				for (int t = 0; t < 8; ++t)
+					w[t] = ((nz >> t) & 1u) ? emit_ld<kCached>(pw + (size_t) (l - first + t) * pstride) : 0ull;
+#pragma unroll
+				for (int t = 0; t < 8; ++t) {
 					if (!w[t]) continue;
 					const uint32_t inv = ~((uint32_t) (base + l + t) * 0x01010101u);
 					const uint32_t lo = (uint32_t) w[t], hi = (uint32_t) (w[t] >> 32);
