@@ -48,8 +48,10 @@ constexpr uint32_t kLaneMaxDeg = 32;    // ... destinations of at most this in-d
 constexpr uint32_t kGroupMaxWords = 8;  // pull: up to this many words, in-neighbour rows in lane groups
 constexpr uint32_t kEmitW = 4;          // output tile: kV vertices x 4 words (256 sources), kV = threads / 4
 // shared bytes of an output tile of kV vertices: rows of one source quad (kV + 4
-// words, 16-byte aligned) and the nibble table
-__host__ __device__ constexpr uint32_t emit_bytes(uint32_t kV) { return (kEmitW * 16 * (kV + 4) + 16) * 4; }
+// words, 16-byte aligned; `bufs` copies) and the nibble table
+__host__ __device__ constexpr uint32_t emit_bytes(uint32_t kV, uint32_t bufs = 1) {
+	return (bufs * kEmitW * 16 * (kV + 4) + 16) * 4;
+}
 constexpr uint32_t kEmitV = kMsThreads / kEmitW;  // the traversal kernel's tiles (its early output passes)
 constexpr uint32_t kEmitBytes = emit_bytes(kEmitV);
 constexpr int kEmitThreads = 256;                 // the output pass launch
@@ -694,22 +696,28 @@ __device__ __forceinline__ uint64_t emit_ld(const uint64_t *p) {
 	return kCached ? (uint64_t) __ldg((const unsigned long long *) p) : ld_cg64(p);
 }
 
+// kCached also selects two row buffers used in turn, so that a tile needs one
+// barrier (between its two phases): a buffer is written again two tiles
+// later, after the barrier that every thread reaches once done reading it.
 template <bool kCached, uint32_t kV>
 __device__ __noinline__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t ns, uint32_t base, uint32_t first, uint32_t last,
 		bool merge, uint8_t *lev) {
 	constexpr uint32_t kEmitV = kV, kEmitRow = kV + 4;
+	constexpr uint32_t kBufs = kCached ? 2 : 1, kBufWords = kEmitW * 16 * kEmitRow;
 	constexpr uint32_t kRows = kEmitW * 64;
 	const uint32_t K = a.K, n = a.n;
 	const uint32_t vtiles = (n + kEmitV - 1) / kEmitV, wtiles = (K + kEmitW - 1) / kEmitW;
 	const uint32_t vi = threadIdx.x % kEmitV, wi = threadIdx.x / kEmitV;
 	const size_t pstride = (size_t) n * K;
-	uint32_t *sw = reinterpret_cast<uint32_t *>(lev);  // [wi * 16 + quad][kEmitRow]
-	uint32_t *lut = sw + kEmitW * 16 * kEmitRow;       // nibble -> byte mask
+	uint32_t *const sw0 = reinterpret_cast<uint32_t *>(lev);  // [buffer][wi * 16 + quad][kEmitRow]
+	uint32_t *lut = sw0 + kBufs * kBufWords;                 // nibble -> byte mask
 	if (threadIdx.x < 16) lut[threadIdx.x] = nibble_bytes(threadIdx.x);
 	// phase 2's item: rows of source quad rq (word rq / 16), vertices 16 cc ...
 	const uint32_t rq = threadIdx.x / (kEmitV / 16), cc = threadIdx.x % (kEmitV / 16);
 	__syncthreads();
-	for (uint32_t tile = blockIdx.x; tile < vtiles * wtiles; tile += gridDim.x) {
+	uint32_t turn = 0;
+	for (uint32_t tile = blockIdx.x; tile < vtiles * wtiles; tile += gridDim.x, ++turn) {
+		uint32_t *sw = sw0 + (turn % kBufs) * kBufWords;
 		const uint32_t v0 = (tile % vtiles) * kEmitV, k0 = (tile / vtiles) * kEmitW;
 		const uint32_t nv = min(kEmitV, n - v0);
 		const uint32_t nrows = min(kRows, ns - k0 * 64);
@@ -782,7 +790,7 @@ __device__ __noinline__ void ms_emit(const MsArgs &a, uint8_t *levels, uint32_t 
 				emit_piece(levels + (size_t) (k0 * 64 + r0 + b) * n + v0 + c, y[b], cnt, merge);
 			}
 		}
-		__syncthreads();
+		if (kBufs == 1) __syncthreads();
 	}
 }
 
@@ -957,7 +965,7 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 // Smaller CTAs than the traversal's: a tile's plane loads and its barriers
 // form a chain of round trips, and more CTAs per SM keep more chains going.
 __global__ void __launch_bounds__(kEmitThreads, 4) k_ms_emit(MsArgs a, uint32_t ns, uint8_t *levels) {
-	__shared__ __align__(16) uint8_t lev[emit_bytes(kEmitOutV)];
+	__shared__ __align__(16) uint8_t lev[emit_bytes(kEmitOutV, 2)];
 	const MsStats &st = a.ctl->stats;
 	if (!st.complete) return;
 	const uint32_t base = st.base, depth = st.depth;
