@@ -993,7 +993,13 @@ int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *
 		return BFS_ECUDA;
 	if (between && cudaEventRecord(between, st) != cudaSuccess) return BFS_ECUDA;
 	if (between2 && cudaEventRecord(between2, st) != cudaSuccess) return BFS_ECUDA;
-	if (levels) k_ms_emit<<<num_sms * 4, kEmitThreads, 0, st>>>(a, ns, levels);
+	if (levels) {
+		int out_per_sm = 0;
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&out_per_sm, k_ms_emit, kEmitThreads, 0) != cudaSuccess ||
+				out_per_sm < 1)
+			return BFS_ECUDA;
+		k_ms_emit<<<num_sms * out_per_sm, kEmitThreads, 0, st>>>(a, ns, levels);
+	}
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }
 
