@@ -84,6 +84,7 @@ class Options(C.Structure):
         ("td_beta", C.c_uint32),
         ("ctas_per_sm", C.c_uint32),
         ("bc_batch", C.c_uint32),
+        ("batch_output_tile", C.c_uint32),
     ]
 
 

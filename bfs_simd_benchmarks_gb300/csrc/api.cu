@@ -925,6 +925,7 @@ MsArgs batch_args(const bfs_graph *g, uint32_t K, uint32_t ns, uint32_t planes) 
 	a.wait_limit_ns = wait_limit_ns(g->opt);
 	a.hold_barrier = g->opt.test_hold_barrier;
 	a.ctas_per_sm = g->opt.ctas_per_sm;
+	a.out_tile = g->opt.batch_output_tile;
 	a.row_off = g->dg.row_off;
 	a.col = g->dg.col;
 	a.in_off = g->dg.in_off;
@@ -1849,7 +1850,8 @@ int bfs_set_options(bfs_graph *g, const bfs_options *opt) {
 			opt->warp_max_degree == 0 || opt->cta_max_degree < opt->warp_max_degree || opt->batch_planes == 1 ||
 			opt->batch_planes > kMsMaxLevel + 1 || (opt->batch_planes == 0 && opt->batch_budget_mb == 0) ||
 			opt->batch_push_div == 0 || opt->bc_level_bytes > 2 || opt->switch_rule > BFS_SWITCH_UNVISITED ||
-			opt->bu_alpha == 0 || opt->td_beta == 0 || opt->ctas_per_sm > 2 || opt->bc_batch > 1)
+			opt->bu_alpha == 0 || opt->td_beta == 0 || opt->ctas_per_sm > 2 || opt->bc_batch > 1 ||
+			(opt->batch_output_tile != 0 && opt->batch_output_tile != 64 && opt->batch_output_tile != 128))
 		return BFS_EARG;
 	std::lock_guard<std::mutex> lk(g->mu);
 	g->opt = *opt;

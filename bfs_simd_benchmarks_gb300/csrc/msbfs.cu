@@ -54,8 +54,11 @@ __host__ __device__ constexpr uint32_t emit_bytes(uint32_t kV, uint32_t bufs = 1
 }
 constexpr uint32_t kEmitV = kMsThreads / kEmitW;  // the traversal kernel's tiles (its early output passes)
 constexpr uint32_t kEmitBytes = emit_bytes(kEmitV);
-constexpr int kEmitThreads = 256;                 // the output pass launch
-constexpr uint32_t kEmitOutV = kEmitThreads / kEmitW;
+// The output pass launch: tiles of 64 vertices (256 threads, 4 CTAs per SM)
+// or 128 vertices (512 threads, 2 per SM); by default the wide tiles from
+// kEmitWideMinVertices vertices (measured: 64 wins on 2^22 vertices, 128 on
+// 4.2e7, where the half-line row pieces of narrow tiles cost more)
+constexpr uint32_t kEmitWideMinVertices = 1u << 24;
 
 __device__ __forceinline__ uint64_t ld_cg64(const uint64_t *p) { return __ldcg((const unsigned long long *) p); }
 __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
@@ -962,16 +965,18 @@ __global__ void __launch_bounds__(kMsThreads, 2) k_ms_bfs(MsArgs a, const uint32
 // The final output pass, its own launch after k_ms_bfs (more CTAs per SM than
 // the cooperative kernel, so more plane loads in flight).  Plane depth - base
 // is the empty frontier; after an early output pass, plane 0 was written too.
-// Smaller CTAs than the traversal's: a tile's plane loads and its barriers
-// form a chain of round trips, and more CTAs per SM keep more chains going.
-__global__ void __launch_bounds__(kEmitThreads, 4) k_ms_emit(MsArgs a, uint32_t ns, uint8_t *levels) {
-	__shared__ __align__(16) uint8_t lev[emit_bytes(kEmitOutV, 2)];
+// A tile's plane loads and its barriers form a chain of round trips; narrow
+// tiles on small CTAs keep more chains going per SM.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 2) k_ms_emit(MsArgs a, uint32_t ns, uint8_t *levels) {
+	constexpr uint32_t kV = kThreads / kEmitW;
+	__shared__ __align__(16) uint8_t lev[emit_bytes(kV, 2)];
 	const MsStats &st = a.ctl->stats;
 	if (!st.complete) return;
 	const uint32_t base = st.base, depth = st.depth;
 	const uint32_t first = base == 0 ? 0 : 1;
 	if (depth < base + first + 1) return;
-	ms_emit<true, kEmitOutV>(a, levels, ns, base, first, depth - 1 - base, base != 0, lev);
+	ms_emit<true, kV>(a, levels, ns, base, first, depth - 1 - base, base != 0, lev);
 }
 
 int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *levels, int num_sms, cudaStream_t st,
@@ -994,11 +999,14 @@ int ms_launch(const MsArgs &a, const uint32_t *d_sources, uint32_t ns, uint8_t *
 	if (between && cudaEventRecord(between, st) != cudaSuccess) return BFS_ECUDA;
 	if (between2 && cudaEventRecord(between2, st) != cudaSuccess) return BFS_ECUDA;
 	if (levels) {
+		const bool wide = a.out_tile ? a.out_tile == 128 : a.n >= kEmitWideMinVertices;
+		const void *fn = wide ? (const void *) k_ms_emit<512> : (const void *) k_ms_emit<256>;
+		const int threads = wide ? 512 : 256;
 		int out_per_sm = 0;
-		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&out_per_sm, k_ms_emit, kEmitThreads, 0) != cudaSuccess ||
-				out_per_sm < 1)
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&out_per_sm, fn, threads, 0) != cudaSuccess || out_per_sm < 1)
 			return BFS_ECUDA;
-		k_ms_emit<<<num_sms * out_per_sm, kEmitThreads, 0, st>>>(a, ns, levels);
+		if (wide) k_ms_emit<512><<<num_sms * out_per_sm, 512, 0, st>>>(a, ns, levels);
+		else k_ms_emit<256><<<num_sms * out_per_sm, 256, 0, st>>>(a, ns, levels);
 	}
 	return cudaGetLastError() == cudaSuccess ? BFS_OK : BFS_ECUDA;
 }

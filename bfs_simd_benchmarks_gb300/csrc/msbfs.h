@@ -74,6 +74,7 @@ struct MsArgs {
 	unsigned long long wait_limit_ns;  // bound of every grid-barrier wait
 	uint32_t hold_barrier;             // tests: CTA 0 skips its arrival at this barrier (0 = off)
 	uint32_t ctas_per_sm;              // 0 = as many as fit (at most 2)
+	uint32_t out_tile;                 // output pass tile width in vertices: 64, 128, or 0 = by graph size
 };
 
 // Enqueues the whole batched traversal (one cooperative launch and the

@@ -168,6 +168,8 @@ typedef struct bfs_options {
 	                              2), or 1 or 2 */
 	uint32_t bc_batch;         /* bfs_bc_accumulate: 1 (default) = sources in groups of up to 256 through the
 	                              batched betweenness kernel (bfs_bc_run_batch); 0 = one source at a time */
+	uint32_t batch_output_tile; /* bfs_run_batch output pass: vertices per tile, 64 or 128; 0 (default) = 128
+	                              from 2^24 vertices, else 64; the levels are identical */
 } bfs_options;
 
 #define BFS_SWITCH_REFERENCE 0u

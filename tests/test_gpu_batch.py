@@ -268,3 +268,33 @@ def test_rmat22_4096_sources_against_the_oracle(native, oracle):
             np.testing.assert_array_equal(out[i].cpu().numpy(), np.where(ref < 0, 255, ref).astype(np.uint8))
         del out
         torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("num_sources", [70, 4096])
+def test_output_tile_widths_give_the_same_levels(native, oracle, num_sources):
+    """The output pass's two tile widths (64 vertices on 256-thread CTAs, 128 on
+    512-thread CTAs; option batch_output_tile, by graph size when 0) write the
+    same bytes, also when the traversal outgrows its planes (early output
+    passes merged into the final one)."""
+    import bfs_simd_benchmarks_gb300 as B
+    n = (1 << 14) + 37   # not a multiple of either tile width
+    src, dst = B.gen_rmat(n, 16 * n, seed=1717, permute=True)
+    arr = oracle.csr_arrays(n, src, dst)
+    with B.Graph.from_edges(n, src, dst, 256, 4) as g:
+        sources = B.pick_sources(g.degrees(), num_sources, seed=21)
+        outs = {}
+        for planes in (0, 3):
+            for tile in (0, 64, 128):
+                g.set_options(batch_output_tile=tile, batch_planes=planes)
+                out, st = g.run_batch(sources)
+                assert st["status"] == 0
+                outs[(planes, tile)] = out.cpu().numpy()
+        ref = outs[(0, 64)]
+        for key, rows in outs.items():
+            assert rows.tobytes() == ref.tobytes(), key
+        for i in (0, num_sources // 2, num_sources - 1):
+            want = oracle.bfs_levels(arr, int(sources[i]))
+            np.testing.assert_array_equal(ref[i], np.where(want < 0, 255, want).astype(np.uint8))
+        import bfs_simd_benchmarks_gb300._native as N
+        with pytest.raises(N.BfsError):
+            g.set_options(batch_output_tile=96)
