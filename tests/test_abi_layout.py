@@ -67,3 +67,19 @@ def test_ctypes_structs_match_the_header(tmp_path):
         for name, _ in cls._fields_:
             off = getattr(cls, name).offset
             assert got[(py, name)] == off, f"{py}.{name}: C offset {got[(py, name)]} vs ctypes {off}"
+
+
+def test_ctypes_signatures_have_the_header_arity():
+    """Every function the ctypes mirror declares takes as many arguments as its
+    prototype in include/bfs_gb300.h."""
+    import re
+    from bfs_simd_benchmarks_gb300 import _native as N
+    text = open(os.path.join(ROOT, "include", "bfs_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    protos = {}
+    for m in re.finditer(r"\b(bfs_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        args = m.group(2).strip()
+        protos[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    for name, _, argtypes in N._SIGNATURES:
+        assert name in protos, f"{name} has no prototype in the header"
+        assert len(argtypes) == protos[name], f"{name}: {len(argtypes)} ctypes arguments, {protos[name]} in the header"
