@@ -554,7 +554,9 @@ int bfs_bc_run_batch(bfs_graph *g, const uint32_t *sources, uint32_t num_sources
 /* The same enqueued on `stream` into DEVICE buffers [num_sources][N] (either
  * may be NULL); sources is a host array.  No fallback: a batch deeper than its
  * planes ends with status BFS_EUNSUPPORTED (bfs_bc_last_stats) and leaves the
- * buffers unwritten. */
+ * buffers unwritten.  The batched betweenness state (2 x 256 bytes per vertex,
+ * the level lists) and the batched traversal's state are kept with the graph:
+ * calls on one graph must not overlap on the GPU. */
 int bfs_bc_run_batch_device(bfs_graph *g, const uint32_t *sources, uint32_t num_sources, float *dependencies,
 		uint32_t *num_paths, void *stream);
 /* Betweenness centrality over a set of sources: centrality[v] (HOST, N floats,
